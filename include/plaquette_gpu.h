@@ -1,0 +1,156 @@
+/*
+ * plaquette_gpu.h -- C ABI of the GB300 batched stabilizer-tableau library
+ * (libps_gpu.so).
+ *
+ * It is a drop-in for the state API of the reference,
+ * Plaquette::CliffordState<int> (plaquette_simulator/src/CliffordState.hpp)
+ * and its Python binding (plaquette_simulator/src/Bindings.cpp:13-31).  Each
+ * entry point below names the reference interface it replaces.  All compute
+ * runs in hand-written sm_103a CUDA kernels; there is no CPU fallback.
+ *
+ * Conventions
+ *  - Every call returns a ps_status (PS_OK = 0).  On error, ps_last_error()
+ *    returns a thread-local message in the reference's error format
+ *    (Error.hpp:94-97: "[file][Line:N][Method:f]: Error in Plaquette: msg").
+ *  - A handle owns its device tableau, its measurement records and one CUDA
+ *    stream.  Calls that return host data synchronise that stream (the
+ *    reference's deep_copy is blocking too).  One handle must not be used from
+ *    several host threads at once (as in the reference, whose measurement
+ *    list is unsynchronised, CliffordState.hpp:593).
+ *  - Host tableau buffers use the reference's int32 layout: x and z are
+ *    [batch][2n+1][n], r is [batch][2n+1], row-major
+ *    (CliffordState.hpp:207-259).
+ *  - Random measurement outcomes: `forced` is NULL (per-shot Philox4x32-10
+ *    draws keyed by (seed, event index, global shot)) or ceil(batch/8) bytes
+ *    of LSB-first bits; a forced bit stands for the uniform draw 0.25 (bit 1)
+ *    or 0.75 (bit 0), and the outcome is draw < bias, as `frand(0,1) < bias`
+ *    in MeasurementFunctors.hpp:245-247.
+ */
+#ifndef PLAQUETTE_GPU_H
+#define PLAQUETTE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ps_status;
+#define PS_OK 0
+#define PS_E_ARG 1     /* invalid argument (qubit out of range, bad size ...) */
+#define PS_E_RANGE 2   /* id/shot out of range; GetMeasurement's nullopt     */
+#define PS_E_CUDA 3    /* CUDA runtime error                                 */
+#define PS_E_NOMEM 4   /* device allocation failed / over budget             */
+#define PS_E_STATE 5   /* call not valid in the handle's current state       */
+#define PS_E_TIMEOUT 6 /* a bounded device wait gave up                      */
+
+typedef struct ps_state ps_state;
+
+/* Thread-local message of the last failed call ("" if none). */
+const char *ps_last_error(void);
+/* Replaces CliffordState::GetKokkosBackend (CliffordState.hpp:280-282):
+ * "CUDA sm_103a (<device name>)". */
+const char *ps_backend_name(void);
+/* Library version string. */
+const char *ps_version(void);
+
+/* ---------------------------------------------------------------- state */
+/* CliffordState(num_qubits, batch_size, seed = -1, init_to_zero_state)
+ * (CliffordState.hpp:97-139).  seed < 0 falls back to 213434232223 as there. */
+ps_status ps_create(uint64_t num_qubits, uint64_t batch_size, int64_t seed, int init_to_zero_state,
+                    ps_state **out);
+/* CliffordState(x, z, r, num_qubits, batch_size, seed) (CliffordState.hpp:153-159). */
+ps_status ps_create_from_host(const int32_t *x, const int32_t *z, const int32_t *r, uint64_t num_qubits,
+                              uint64_t batch_size, int64_t seed, ps_state **out);
+/* Copy constructor (CliffordState.hpp:168-174): tableau, seed and event
+ * counter are copied; measurement records are not (as in the reference). */
+ps_status ps_clone(const ps_state *h, ps_state **out);
+/* ~CliffordState (CliffordState.hpp:665-688).  NULL is a no-op. */
+ps_status ps_destroy(ps_state *h);
+
+ps_status ps_get_num_qubits(const ps_state *h, uint64_t *out); /* GetNumQubits :289 */
+ps_status ps_get_batch_size(const ps_state *h, uint64_t *out); /* GetBatchSize :296 */
+ps_status ps_get_seed(const ps_state *h, int64_t *out);        /* GetSeed :303      */
+/* Number of random events (measurements and Pauli channels) consumed so far;
+ * the next one draws with this event index. */
+ps_status ps_get_event_counter(const ps_state *h, uint64_t *out);
+ps_status ps_set_event_counter(ps_state *h, uint64_t events);
+
+/* ResetCliffordState (CliffordState.hpp:309-316).  Implements the intended
+ * semantics (the tableau of a fresh constructor); the reference's launch
+ * policy {B, W, W} writes out of bounds. */
+ps_status ps_reset(ps_state *h);
+/* CheckSum(starting_batch_id, ending_batch_id) (CliffordState.hpp:327-338):
+ * sum of all x, z, r entries of shots [s0, s1); s1 < 0 means batch_size. */
+ps_status ps_checksum(ps_state *h, int64_t s0, int64_t s1, int64_t *out);
+/* DeviceToHost / HostToDevice (CliffordState.hpp:207-259), reference layout. */
+ps_status ps_device_to_host(ps_state *h, int32_t *x, int32_t *z, int32_t *r);
+ps_status ps_host_to_device(ps_state *h, const int32_t *x, const int32_t *z, const int32_t *r);
+
+/* ---------------------------------------------------------------- gates */
+/* Apply{Hadamard,Phase,PauliX,PauliY,PauliZ}Gate (CliffordState.hpp:389-531). */
+ps_status ps_h(ps_state *h, uint64_t q);
+ps_status ps_s(ps_state *h, uint64_t q);
+ps_status ps_x(ps_state *h, uint64_t q);
+ps_status ps_y(ps_state *h, uint64_t q);
+ps_status ps_z(ps_state *h, uint64_t q);
+/* ApplyControlNotGate / ApplyControlPhaseGate (CliffordState.hpp:412-449). */
+ps_status ps_cx(ps_state *h, uint64_t control, uint64_t target);
+ps_status ps_cz(ps_state *h, uint64_t control, uint64_t target);
+/* Apply*GateToQubits (CliffordState.hpp:379-531): one gate per target (per
+ * consecutive pair for CX / CZ). */
+ps_status ps_apply_to_qubits(ps_state *h, int32_t op_code, const uint64_t *targets, uint64_t count);
+/* Apply{Hadamard,Phase}GateWithApplyFlag (CliffordState.hpp:348-372); the
+ * apply flag is the result array of measurement record `meas_id` (the
+ * reference passes that record's device View). */
+ps_status ps_h_flag(ps_state *h, uint64_t q, uint64_t meas_id);
+ps_status ps_s_flag(ps_state *h, uint64_t q, uint64_t meas_id);
+
+/* ---------------------------------------------------------- measurement */
+/* MeasureQubit(target_qubit, bias, measurement_id) (CliffordState.hpp:587-623).
+ * id < 0 creates a new record; an existing id is overwritten (the
+ * reference's "Measurement id is out of range" check at :609-610 becomes
+ * PS_E_RANGE).  *out_id receives the record id. */
+ps_status ps_measure(ps_state *h, uint64_t q, float bias, int64_t id, const uint8_t *forced, uint64_t *out_id);
+/* MeasureQubits(targets, bias) (CliffordState.hpp:543-548): one record per
+ * target; ids are consecutive starting at *first_id. */
+ps_status ps_measure_qubits(ps_state *h, const uint64_t *targets, uint64_t count, float bias,
+                            uint64_t *first_id);
+/* GetMeasurement(id, shot) (CliffordState.hpp:635-648): PS_E_RANGE where the
+ * reference returns nullopt. */
+ps_status ps_get_measurement(ps_state *h, uint64_t id, uint64_t shot, int32_t *result, int32_t *determined);
+/* All shots of one record, bit-packed LSB-first (ceil(batch/8) bytes each;
+ * either pointer may be NULL). */
+ps_status ps_get_record_bits(ps_state *h, uint64_t id, uint8_t *result_bits, uint8_t *determined_bits);
+ps_status ps_num_records(const ps_state *h, uint64_t *out);
+/* Qubit that record `id` measured (Measurement::qubit_measured, :33). */
+ps_status ps_record_qubit(const ps_state *h, uint64_t id, uint64_t *out);
+
+/* --------------------------------------------------- ops with no counterpart */
+/* ResetQubit: MeasureQubit into a new record, then X on the shots whose
+ * outcome is 1 (the reference composes that X as H,S,S,H with the record as
+ * apply flag, Test_CliffordState.hpp:703-711). */
+ps_status ps_reset_qubit(ps_state *h, uint64_t q, const uint8_t *forced, uint64_t *out_id);
+/* Pauli channel on q: per shot X / Y / Z with probabilities p[0..2], drawn
+ * from Philox keyed by (seed, event index, shot).  Mirrors the E_PAULI
+ * parameter count of CliffordCircuit.hpp:44-49. */
+ps_status ps_pauli_channel_1(ps_state *h, uint64_t q, const float p[3]);
+/* Two-qubit Pauli channel on (a, b); p[15] in the order IX IY IZ XI XX XY XZ
+ * YI YX YY YZ ZI ZX ZY ZZ.  Mirrors E_PAULI2 (CliffordCircuit.hpp:50-55). */
+ps_status ps_pauli_channel_2(ps_state *h, uint64_t a, uint64_t b, const float p[15]);
+
+/* ------------------------------------------------------------ streaming */
+/* Block until all work queued on the handle's stream is done. */
+ps_status ps_synchronize(ps_state *h);
+/* The handle's cudaStream_t (as void*), for callers that order their own work
+ * after the library's. */
+ps_status ps_get_stream(const ps_state *h, void **stream);
+/* Device pointers of the packed tableau planes and their geometry (words per
+ * qubit column).  For integration and benchmarking. */
+ps_status ps_get_device_tableau(const ps_state *h, void **x, void **z, void **r, uint64_t *words);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PLAQUETTE_GPU_H */

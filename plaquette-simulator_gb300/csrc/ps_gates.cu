@@ -1,0 +1,231 @@
+// ps_gates.cu -- the plain per-gate form: one launch per gate (or per Pauli
+// channel), each a coalesced 128-bit pass over the touched tableau columns
+// of all W rows.  This is the drop-in for the reference's per-gate
+// parallel_for launches (CliffordState.hpp:348-531) and the baseline the
+// fused circuit form is measured against.
+#include <cmath>
+
+#include "ps_internal.h"
+
+namespace ps {
+
+namespace {
+
+struct W2 {
+    u64 a, b;
+};
+
+__device__ __forceinline__ W2 ld2(const u64 *p) {
+    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(p);
+    return {v.x, v.y};
+}
+__device__ __forceinline__ void st2(u64 *p, u64 a, u64 b) {
+    *reinterpret_cast<ulonglong2 *>(p) = make_ulonglong2(a, b);
+}
+
+// Per-word gate algebra (GateFunctors.hpp), 64 shots at a time.
+template <int CODE>
+__device__ __forceinline__ void apply_1q(u64 &x, u64 &z, u64 &r, u64 f) {
+    if (CODE == OP_H) {  // GateFunctors.hpp:90-93
+        r ^= x & z;
+        const u64 t = x;
+        x = z;
+        z = t;
+    } else if (CODE == OP_S) {  // :165-169
+        r ^= x & z;
+        z ^= x;
+    } else if (CODE == OP_X) {  // :304-307
+        r ^= z;
+    } else if (CODE == OP_Y) {  // :324-327
+        r ^= x ^ z;
+    } else if (CODE == OP_Z) {  // :373-376
+        r ^= x;
+    } else if (CODE == OP_H_IF) {  // :143-148, per-shot flag f
+        r ^= f & x & z;
+        const u64 nx = (x & ~f) | (z & f);
+        z = (z & ~f) | (x & f);
+        x = nx;
+    } else if (CODE == OP_S_IF) {  // :221-228
+        r ^= f & x & z;
+        z ^= f & x;
+    }
+}
+
+// One thread per (row, pair of shot-words): W * w/2 threads.
+template <int CODE>
+__global__ void __launch_bounds__(256) gate1_kernel(u64 *__restrict__ X, u64 *__restrict__ Z, u64 *__restrict__ R,
+                                                   int64_t n, int64_t W, int64_t w, int64_t q,
+                                                   const u64 *__restrict__ flag) {
+    const int64_t half = w >> 1;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= W * half) return;
+    const int64_t i = idx / half, k = (idx - i * half) * 2;
+    const int64_t off = (i * n + q) * w + k;
+    W2 x = ld2(X + off), z = ld2(Z + off), r = ld2(R + i * w + k);
+    u64 f0 = 0, f1 = 0;
+    if (CODE == OP_H_IF || CODE == OP_S_IF) {
+        const W2 f = ld2(flag + k);
+        f0 = f.a;
+        f1 = f.b;
+    }
+    apply_1q<CODE>(x.a, z.a, r.a, f0);
+    apply_1q<CODE>(x.b, z.b, r.b, f1);
+    if (CODE == OP_H || CODE == OP_H_IF || CODE == OP_S || CODE == OP_S_IF) {
+        st2(X + off, x.a, x.b);
+        st2(Z + off, z.a, z.b);
+    }
+    st2(R + i * w + k, r.a, r.b);
+}
+
+// CX (GateFunctors.hpp:248-253) and CZ (:30-35).
+template <int CODE>
+__global__ void __launch_bounds__(256) gate2_kernel(u64 *__restrict__ X, u64 *__restrict__ Z, u64 *__restrict__ R,
+                                                   int64_t n, int64_t W, int64_t w, int64_t c, int64_t t) {
+    const int64_t half = w >> 1;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= W * half) return;
+    const int64_t i = idx / half, k = (idx - i * half) * 2;
+    const int64_t oc = (i * n + c) * w + k, ot = (i * n + t) * w + k;
+    W2 xc = ld2(X + oc), zc = ld2(Z + oc), xt = ld2(X + ot), zt = ld2(Z + ot), r = ld2(R + i * w + k);
+    if (CODE == OP_CX) {
+        r.a ^= xc.a & zt.a & ~(xt.a ^ zc.a);
+        r.b ^= xc.b & zt.b & ~(xt.b ^ zc.b);
+        st2(X + ot, xt.a ^ xc.a, xt.b ^ xc.b);
+        st2(Z + oc, zc.a ^ zt.a, zc.b ^ zt.b);
+    } else {
+        r.a ^= xc.a & xt.a & (zt.a ^ zc.a);
+        r.b ^= xc.b & xt.b & (zt.b ^ zc.b);
+        st2(Z + ot, zt.a ^ xc.a, zt.b ^ xc.b);
+        st2(Z + oc, zc.a ^ xt.a, zc.b ^ xt.b);
+    }
+    st2(R + i * w + k, r.a, r.b);
+}
+
+// Pauli-channel sampling: one thread per (shot-word, qubit slot).  For each
+// shot one Philox draw u picks Pauli k = first index with u < thr[k]
+// (0 = identity).  Output masks: fx = shots with X or Y, fz = Y or Z, for
+// qubit a (slot 0) and b (slot 1).
+__global__ void channel_sample_kernel(u64 *__restrict__ masks, int64_t w, uint64_t seed, uint64_t event,
+                                      uint64_t word0, int count, uint64_t t0, uint64_t t1, uint64_t t2,
+                                      const uint64_t *__restrict__ thr15) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= w) return;
+    u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
+    for (uint32_t sub = 0; sub < 16; ++sub) {
+        const u32x4 u = draw_block(seed, event, word0 + (uint64_t)k, sub, TAG_NOISE);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const uint64_t v = u.v[l];
+            int idx = 0;
+            if (count == 3) {
+                idx = v < t0 ? 1 : v < t1 ? 2 : v < t2 ? 3 : 0;
+            } else {
+                for (int j = 0; j < 15; ++j)
+                    if (v < thr15[j]) {
+                        idx = j + 1;
+                        break;
+                    }
+            }
+            if (idx) {
+                const u64 bit = 1ull << (sub * 4 + l);
+                const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
+                if (pa == 1 || pa == 2) fxa |= bit;
+                if (pa == 2 || pa == 3) fza |= bit;
+                if (pb == 1 || pb == 2) fxb |= bit;
+                if (pb == 2 || pb == 3) fzb |= bit;
+            }
+        }
+    }
+    masks[k] = fxa;
+    masks[w + k] = fza;
+    masks[2 * w + k] = fxb;
+    masks[3 * w + k] = fzb;
+}
+
+// r ^= (fx & z_q) ^ (fz & x_q) over all rows: X flips rows with Z on q, Z
+// flips rows with X on q (the reference's Pauli functors, GateFunctors.hpp:
+// 303-307 and :372-376, applied per shot).
+__global__ void __launch_bounds__(256) sign_flip_kernel(const u64 *__restrict__ X, const u64 *__restrict__ Z,
+                                                       u64 *__restrict__ R, int64_t n, int64_t W, int64_t w,
+                                                       int64_t q, const u64 *__restrict__ fx,
+                                                       const u64 *__restrict__ fz) {
+    const int64_t half = w >> 1;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= W * half) return;
+    const int64_t i = idx / half, k = (idx - i * half) * 2;
+    const int64_t off = (i * n + q) * w + k;
+    const W2 x = ld2(X + off), z = ld2(Z + off), a = ld2(fx + k), b = ld2(fz + k);
+    W2 r = ld2(R + i * w + k);
+    r.a ^= (a.a & z.a) ^ (b.a & x.a);
+    r.b ^= (a.b & z.b) ^ (b.b & x.b);
+    st2(R + i * w + k, r.a, r.b);
+}
+
+inline int blocks_for(int64_t threads) { return (int)((threads + 255) / 256); }
+
+}  // namespace
+
+int launch_gate(ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag) {
+    const int64_t work = h->W * (h->w >> 1);
+    const int grid = blocks_for(work);
+    if (h->n == 0 || work == 0) return OK;
+    switch (code) {
+    case OP_H: gate1_kernel<OP_H><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_S: gate1_kernel<OP_S><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_X: gate1_kernel<OP_X><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_Y: gate1_kernel<OP_Y><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_Z: gate1_kernel<OP_Z><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_H_IF:
+        gate1_kernel<OP_H_IF><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, flag);
+        break;
+    case OP_S_IF:
+        gate1_kernel<OP_S_IF><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, flag);
+        break;
+    case OP_CX: gate2_kernel<OP_CX><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, b); break;
+    case OP_CZ: gate2_kernel<OP_CZ><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, b); break;
+    default: return fail(E_ARG, "unknown gate code " + std::to_string(code));
+    }
+    PS_CUDA(cudaGetLastError());
+    return OK;
+}
+
+void channel_thresholds(const float *p, int count, uint64_t *thr) {
+    double cum = 0.0;
+    for (int k = 0; k < count; ++k) {
+        cum += (double)p[k];
+        if (!(cum > 0.0))
+            thr[k] = 0;
+        else if (cum >= 1.0)
+            thr[k] = (uint64_t)1 << 32;
+        else
+            thr[k] = (uint64_t)std::floor(cum * 4294967296.0);
+    }
+}
+
+int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thr, int count) {
+    const uint64_t event = h->events++;
+    const uint64_t *thr15 = nullptr;
+    uint64_t *dthr = nullptr;
+    if (count == 15) {
+        PS_CUDA(cudaMallocAsync(&dthr, 15 * sizeof(uint64_t), h->stream));
+        PS_CUDA(cudaMemcpyAsync(dthr, thr, 15 * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+        thr15 = dthr;
+    }
+    channel_sample_kernel<<<blocks_for(h->w), 256, 0, h->stream>>>(
+        h->mask_buf, h->w, (uint64_t)h->seed, event, 0, count, thr[0], count == 3 ? thr[1] : 0,
+        count == 3 ? thr[2] : 0, thr15);
+    PS_CUDA(cudaGetLastError());
+    const int64_t work = h->W * (h->w >> 1);
+    if (h->n > 0 && work > 0) {
+        sign_flip_kernel<<<blocks_for(work), 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, h->mask_buf,
+                                                                  h->mask_buf + h->w);
+        if (count == 15)
+            sign_flip_kernel<<<blocks_for(work), 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, b,
+                                                                      h->mask_buf + 2 * h->w, h->mask_buf + 3 * h->w);
+    }
+    PS_CUDA(cudaGetLastError());
+    if (dthr) PS_CUDA(cudaFreeAsync(dthr, h->stream));
+    return OK;
+}
+
+}  // namespace ps

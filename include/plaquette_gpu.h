@@ -54,6 +54,12 @@ const char *ps_last_error(void);
 const char *ps_backend_name(void);
 /* Library version string. */
 const char *ps_version(void);
+/* Selects the CUDA device used by handles created afterwards on the calling
+ * thread (one process per GPU). */
+ps_status ps_set_device(int device);
+/* Waits for all work of this library on the current device (also run
+ * automatically at process exit, before the CUDA runtime shuts down). */
+ps_status ps_device_synchronize(void);
 
 /* ---------------------------------------------------------------- state */
 /* CliffordState(num_qubits, batch_size, seed = -1, init_to_zero_state)
@@ -139,6 +145,91 @@ ps_status ps_pauli_channel_1(ps_state *h, uint64_t q, const float p[3]);
 /* Two-qubit Pauli channel on (a, b); p[15] in the order IX IY IZ XI XX XY XZ
  * YI YX YY YZ ZI ZX ZY ZZ.  Mirrors E_PAULI2 (CliffordCircuit.hpp:50-55). */
 ps_status ps_pauli_channel_2(ps_state *h, uint64_t a, uint64_t b, const float p[15]);
+
+/* ------------------------------------------------------------- circuits */
+/* A circuit is an op table (see the PS_OP_* codes) plus a float parameter
+ * table.  It replaces the reference's CliffordCircuit driver
+ * (CliffordCircuit.hpp:131-135, one parallel_for per target) with a compiled
+ * plan bound to one state:
+ *   PS_MODE_PLAIN  one kernel launch per op (the reference's structure);
+ *   PS_MODE_FUSED  every run of gates / Pauli gates / channels / reset-X
+ *                  between measurement phases is one fused pass over the
+ *                  tableau; each run of consecutive measurements is one
+ *                  launch.
+ * With use_graph the whole plan is captured once into a CUDA graph and each
+ * run is one graph launch. */
+typedef struct {
+    int32_t code, a, b, c;
+} ps_op;
+#define PS_OP_H 0
+#define PS_OP_S 1
+#define PS_OP_X 2
+#define PS_OP_Y 3
+#define PS_OP_Z 4
+#define PS_OP_CX 5      /* a = control, b = target                           */
+#define PS_OP_CZ 6
+#define PS_OP_M 7       /* bias = params[c] (c < 0: 0.5)                      */
+#define PS_OP_R 8       /* measure into a record, then X where the outcome is 1 */
+#define PS_OP_PAULI1 9  /* params[c..c+2] = pX, pY, pZ                        */
+#define PS_OP_PAULI2 10 /* params[c..c+14], order IX IY ... ZZ                 */
+#define PS_OP_H_IF 11   /* H on a where circuit record c (k-th M/R) is 1       */
+#define PS_OP_S_IF 12
+
+#define PS_MODE_PLAIN 0
+#define PS_MODE_FUSED 1
+
+typedef struct {
+    int32_t mode;        /* PS_MODE_PLAIN or PS_MODE_FUSED                      */
+    int32_t use_graph;   /* capture the plan in a CUDA graph                     */
+    int32_t seg_rows;    /* fused tile: tableau rows per CTA (0 = auto)          */
+    int32_t seg_words;   /* fused tile: 64-shot words per CTA (0 = auto)         */
+    int32_t seg_threads; /* fused tile: threads per CTA (0 = auto)               */
+} ps_circuit_options;
+
+typedef struct {
+    uint64_t num_ops, num_gates, num_measurements, num_channels, num_events;
+    uint64_t num_segments, num_measure_phases, launches_per_run;
+    uint64_t first_record;          /* state record id of the first M/R      */
+    double segment_bytes;           /* algorithmic HBM bytes of all segments  */
+    int32_t seg_rows, seg_words, seg_threads;
+} ps_circuit_stats;
+
+typedef struct ps_circuit ps_circuit;
+
+/* Compiles ops for state h; allocates one measurement record per M / R (ids
+ * first_record .. first_record + num_measurements - 1). */
+ps_status ps_circuit_compile(ps_state *h, const ps_op *ops, uint64_t nops, const float *params, uint64_t nparams,
+                             const ps_circuit_options *opts, ps_circuit **out);
+/* Forced random draws for the circuit's measurements: num_measurements rows
+ * of ceil(batch/8) bytes, or NULL to return to Philox draws. */
+ps_status ps_circuit_set_forced(ps_circuit *c, const uint8_t *forced_all);
+/* Enqueues one run on the state's stream (returns without waiting).  The run
+ * draws with event indices starting at the state's event counter, which it
+ * advances by num_events.  reset_state != 0 first re-initialises the tableau
+ * to |0...0> (inside the same graph). */
+ps_status ps_circuit_run(ps_circuit *c, int reset_state);
+ps_status ps_circuit_get_stats(const ps_circuit *c, ps_circuit_stats *out);
+ps_status ps_circuit_destroy(ps_circuit *c);
+
+/* Per-kernel-kind device time of one run, measured with CUDA events around
+ * every launch (the plan is enqueued launch by launch, not as a graph, and
+ * the call waits for it).  Kinds: 0 tableau init, 1 channel sampling (fused),
+ * 2 fused segment, 3 measurement, 4 per-op gate, 5 per-op channel. */
+#define PS_PROFILE_KINDS 6
+typedef struct {
+    double ms[PS_PROFILE_KINDS];
+    uint64_t launches[PS_PROFILE_KINDS];
+} ps_circuit_profile_t;
+ps_status ps_circuit_profile(ps_circuit *c, int reset_state, ps_circuit_profile_t *out);
+/* Runs the circuit once (launch by launch) and reports, for each of its
+ * measurements in order and for shots 0..63, whether the random branch was
+ * taken and how many tableau rows were multiplied.  Used to count the
+ * algorithmic bytes of the measurement phases. */
+ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *random_branch, int32_t *rows);
+/* Copies the results / determined words of every record of the circuit to
+ * host memory: num_measurements rows of `words` uint64 each (bit s of word
+ * k = shot 64k+s).  Either pointer may be NULL.  Waits for the stream. */
+ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *determined, uint64_t *words);
 
 /* ------------------------------------------------------------ streaming */
 /* Block until all work queued on the handle's stream is done. */

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -31,6 +32,12 @@ int cuda_fail(cudaError_t e, const char *what) {
     return fail(E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+void ps_enter(const char *method, int line) {
+    g_method = method;
+    g_line = line;
+    g_last_error.clear();
+}
+
 }  // namespace ps
 
 using namespace ps;
@@ -54,7 +61,18 @@ using namespace ps;
 
 namespace {
 
+// Work still queued when the process exits must finish before the CUDA
+// runtime unregisters this library's kernels; the handler is registered
+// after the runtime initialised, so it runs before the runtime's own.
+void drain_at_exit() { cudaDeviceSynchronize(); }
+
 ps_status create_common(uint64_t n, uint64_t S, int64_t seed, ps_state **out) {
+    static bool exit_hook = false;
+    if (!exit_hook) {
+        cudaFree(nullptr);  // initialise the runtime first
+        std::atexit(drain_at_exit);
+        exit_hook = true;
+    }
     if (!out) return fail(E_ARG, "null output pointer");
     *out = nullptr;
     if (n > (uint64_t)1 << 20 || S > (uint64_t)1 << 36) return fail(E_ARG, "num_qubits or batch_size too large");
@@ -81,7 +99,7 @@ int measure_one(ps_state *h, int64_t q, float bias, int64_t id, const uint8_t *f
     rec.qubit = q;
     const u64 *dforced = nullptr;
     TRY(upload_forced(h, forced, &dforced));
-    MeasOp op;
+    MeasOp op{};
     op.q = (int32_t)q;
     op.reset = reset;
     op.bias = bias;
@@ -102,6 +120,18 @@ const char *ps_last_error(void) { return ps::g_last_error.c_str(); }
 
 const char *ps_version(void) { return "plaquette-gb300 0.1.0"; }
 
+ps_status ps_set_device(int device) {
+    ENTER();
+    PS_CUDA(cudaSetDevice(device));
+    return OK;
+}
+
+ps_status ps_device_synchronize(void) {
+    ENTER();
+    PS_CUDA(cudaDeviceSynchronize());
+    return OK;
+}
+
 const char *ps_backend_name(void) {
     static std::string name;
     if (name.empty()) {
@@ -121,6 +151,7 @@ ps_status ps_create(uint64_t n, uint64_t S, int64_t seed, int init_zero, ps_stat
     TRY(create_common(n, S, seed, out));
     if (init_zero && n > 0 && S > 0) {
         int rc = launch_init_zero(*out);
+        (*out)->valid = true;
         if (rc != OK) {
             state_free(*out);
             delete *out;
@@ -157,6 +188,7 @@ ps_status ps_clone(const ps_state *o, ps_state **out) {
     TRY(create_common((uint64_t)o->n, (uint64_t)o->S, o->seed, out));
     ps_state *h = *out;
     h->events = o->events;
+    h->valid = o->valid;
     const size_t plane = (size_t)o->W * o->n * o->w * 8;
     PS_CUDA(cudaStreamSynchronize(o->stream));
     PS_CUDA(cudaMemcpyAsync(h->X, o->X, plane, cudaMemcpyDeviceToDevice, h->stream));
@@ -211,6 +243,7 @@ ps_status ps_set_event_counter(ps_state *h, uint64_t events) {
 ps_status ps_reset(ps_state *h) {
     ENTER();
     CHECK_HANDLE(h);
+    h->valid = true;
     if (h->n == 0 || h->S == 0) return OK;
     return launch_init_zero(h);
 }
@@ -235,6 +268,7 @@ ps_status ps_host_to_device(ps_state *h, const int32_t *x, const int32_t *z, con
     ENTER();
     CHECK_HANDLE(h);
     if (!x || !z || !r) return fail(E_ARG, "null host buffer");
+    h->valid = false;
     return pack_from_host(h, x, z, r);
 }
 

@@ -1,0 +1,663 @@
+// ps_circuit.cpp -- compiled circuits: plain (one launch per op) and fused
+// (segments of gates applied in one tableau pass + measurement phases), with
+// optional CUDA-graph capture.  Replaces the reference's op-by-op driver
+// CliffordCircuit::Execute (CliffordCircuit.hpp:131-135).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../../include/plaquette_gpu.h"
+#include "ps_internal.h"
+#include "ps_segment.cuh"
+
+namespace ps {
+
+namespace {
+
+__global__ void set_params_kernel(RunParams *p, uint64_t seed, uint64_t event_base) {
+    p->seed = seed;
+    p->event_base = event_base;
+}
+
+enum StepKind { K_GATE, K_CHANNEL, K_MEAS, K_SEGMENT, K_INIT };
+
+struct Step {
+    StepKind kind;
+    int32_t code = 0;
+    int64_t a = 0, b = 0;
+    int32_t rec = -1;       // K_GATE: flag record (circuit-local)
+    int32_t count = 0;      // K_CHANNEL: 3 / 15; K_MEAS: number of ops
+    int32_t first = 0;      // K_MEAS: first MeasOp; K_SEGMENT: segment index; K_CHANNEL: thr offset
+    uint32_t event = 0;     // K_CHANNEL event offset
+};
+
+struct SegHost {
+    std::vector<SegLayer> layers;
+    std::vector<SegGate> gates;
+    std::vector<SegSign> signs;
+    std::vector<int32_t> cols;
+    std::vector<NoiseSlot> slots;
+    SegmentDev dev{};
+    void *dev_block = nullptr;
+};
+
+template <class T> int upload(std::vector<void *> &owned, const std::vector<T> &v, T **out) {
+    *out = nullptr;
+    if (v.empty()) return OK;
+    void *p = nullptr;
+    PS_CUDA(cudaMalloc(&p, v.size() * sizeof(T)));
+    owned.push_back(p);
+    PS_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *out = static_cast<T *>(p);
+    return OK;
+}
+
+}  // namespace
+
+}  // namespace ps
+
+using namespace ps;
+
+struct ps_circuit {
+    ps_state *h = nullptr;
+    ps_circuit_options opts{};
+    ps_circuit_stats stats{};
+    std::vector<Step> steps;
+    std::vector<MeasOp> meas;       // host copy
+    MeasOp *d_meas = nullptr;
+    RunParams *d_params = nullptr;
+    uint64_t *d_thr = nullptr;
+    u64 **d_recs = nullptr;
+    u64 *d_masks = nullptr;         // plain-mode channel masks (4w)
+    u64 *d_forced = nullptr;        // [nm][w]
+    NoiseEntry *d_entries = nullptr;
+    u64 *d_dense = nullptr;
+    int32_t *d_entry_count = nullptr;
+    int32_t entry_cap = 0;
+    std::vector<SegHost> segs;
+    std::vector<void *> owned;
+    std::vector<int64_t> rec_ids;   // state record ids of the circuit's M/R
+    u64 *d_res_block = nullptr;     // [nm][w] (owned by the state)
+    u64 *d_det_block = nullptr;
+    uint64_t num_events = 0;
+    cudaGraph_t graph[2] = {nullptr, nullptr};      // [reset_state]
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+};
+
+namespace ps {
+namespace {
+
+bool is_gate(int32_t c) { return c == OP_H || c == OP_S || c == OP_CX || c == OP_CZ || c == OP_H_IF || c == OP_S_IF; }
+bool is_sign(int32_t c) { return c == OP_X || c == OP_Y || c == OP_Z; }
+bool is_meas(int32_t c) { return c == OP_M || c == OP_R; }
+bool is_channel(int32_t c) { return c == OP_PAULI1 || c == OP_PAULI2; }
+
+// Builds the layered schedule of one segment.  Gates go to the first layer
+// after the last use of their qubits; sign ops (Pauli gates, channel
+// outcomes, reset X) are applied after the gates of the layer where their
+// qubits were last touched, which keeps every op's order relative to the
+// gates on its own qubits.
+int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_t i1,
+                  const std::vector<uint32_t> &event_of, const std::vector<int32_t> &rec_of,
+                  const std::vector<int32_t> &thr_off, const std::vector<std::pair<int64_t, int32_t>> &pre_signs,
+                  SegHost &seg) {
+    std::set<int32_t> qset;
+    for (auto &ps_ : pre_signs) qset.insert((int32_t)ps_.first);
+    for (size_t i = i0; i < i1; ++i) {
+        qset.insert(ops[i].a);
+        if (ops[i].code == OP_CX || ops[i].code == OP_CZ || ops[i].code == OP_PAULI2) qset.insert(ops[i].b);
+    }
+    seg.cols.assign(qset.begin(), qset.end());
+    std::map<int32_t, int32_t> loc;
+    for (size_t l = 0; l < seg.cols.size(); ++l) loc[seg.cols[l]] = (int32_t)l;
+
+    struct LayerBuild {
+        std::vector<SegGate> gates;
+        std::vector<SegSign> signs;
+        std::vector<NoiseSlot> slots;
+    };
+    std::vector<LayerBuild> L(1);  // layer 0: no gates (signs before any gate)
+    std::map<int32_t, int32_t> last;  // local col -> layer of last touch
+    auto lastof = [&](int32_t q) { auto it = last.find(q); return it == last.end() ? 0 : it->second; };
+    auto ensure = [&](int32_t layer) { while ((int32_t)L.size() <= layer) L.emplace_back(); };
+
+    for (auto &pr : pre_signs) {
+        SegSign s{SIGN_REC_X, loc[(int32_t)pr.first], pr.second, 0};
+        L[0].signs.push_back(s);
+    }
+    for (size_t i = i0; i < i1; ++i) {
+        const ps_op &o = ops[i];
+        const int32_t a = loc[o.a];
+        if (is_gate(o.code)) {
+            int32_t layer;
+            SegGate g{o.code, a, 0, -1};
+            if (o.code == OP_CX || o.code == OP_CZ) {
+                const int32_t b = loc[o.b];
+                layer = std::max(lastof(a), lastof(b)) + 1;
+                g.b = b;
+                last[a] = last[b] = layer;
+            } else {
+                layer = lastof(a) + 1;
+                last[a] = layer;
+                if (o.code == OP_H_IF || o.code == OP_S_IF) g.rec = o.c;
+            }
+            ensure(layer);
+            L[layer].gates.push_back(g);
+        } else if (is_sign(o.code)) {
+            const int32_t layer = lastof(a);
+            SegSign s{o.code == OP_X ? SIGN_X : o.code == OP_Y ? SIGN_Y : SIGN_Z, a, -1, 0};
+            L[layer].signs.push_back(s);
+        } else if (is_channel(o.code)) {
+            NoiseSlot sl{};
+            sl.a = a;
+            sl.b = o.code == OP_PAULI2 ? loc[o.b] : -1;
+            int32_t layer = lastof(a);
+            if (sl.b >= 0) {
+                layer = std::max(layer, lastof(sl.b));
+                last[sl.b] = layer;
+            }
+            last[a] = layer;
+            sl.layer = layer;
+            sl.count = o.code == OP_PAULI2 ? 15 : 3;
+            sl.thr_off = thr_off[i];
+            sl.event = event_of[i];
+            L[layer].slots.push_back(sl);
+        }
+    }
+    for (size_t l = 0; l < L.size(); ++l) {
+        SegLayer ly;
+        ly.g0 = (int32_t)seg.gates.size();
+        seg.gates.insert(seg.gates.end(), L[l].gates.begin(), L[l].gates.end());
+        ly.g1 = (int32_t)seg.gates.size();
+        ly.s0 = (int32_t)seg.signs.size();
+        seg.signs.insert(seg.signs.end(), L[l].signs.begin(), L[l].signs.end());
+        ly.s1 = (int32_t)seg.signs.size();
+        seg.layers.push_back(ly);
+        seg.slots.insert(seg.slots.end(), L[l].slots.begin(), L[l].slots.end());
+    }
+    (void)c;
+    (void)rec_of;
+    return OK;
+}
+
+void pick_tile(ps_circuit *c, int nq_max) {
+    ps_circuit_options &o = c->opts;
+    const ps_state *h = c->h;
+    if (o.seg_words <= 0) {
+        int bw = 8;
+        while (bw > 2 && (segment_smem_bytes(nq_max, 1, bw) > 200 * 1024 || bw > h->w)) bw >>= 1;
+        o.seg_words = bw;
+    }
+    if (o.seg_rows <= 0) o.seg_rows = 1;
+    if (o.seg_threads <= 0) o.seg_threads = std::min(512, std::max(64, 32 * o.seg_rows * o.seg_words));
+}
+
+// Optional per-launch timing: an event pair around every launch, by kind.
+struct Profiler {
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    cudaStream_t st;
+    int begin(int kind) {
+        cudaEvent_t a, b;
+        PS_CUDA(cudaEventCreate(&a));
+        PS_CUDA(cudaEventCreate(&b));
+        PS_CUDA(cudaEventRecord(a, st));
+        marks.push_back({kind, {a, b}});
+        return OK;
+    }
+    int end() {
+        PS_CUDA(cudaEventRecord(marks.back().second.second, st));
+        return OK;
+    }
+    ~Profiler() {
+        for (auto &m : marks) {
+            cudaEventDestroy(m.second.first);
+            cudaEventDestroy(m.second.second);
+        }
+    }
+};
+
+enum ProfKind { P_INIT = 0, P_SAMPLE = 1, P_SEGMENT = 2, P_MEASURE = 3, P_GATE = 4, P_CHANNEL = 5 };
+
+int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nullptr) {
+    ps_state *h = c->h;
+    auto timed = [&](int kind, auto &&launch) -> int {
+        if (prof && prof->begin(kind) != OK) return E_CUDA;
+        int rc = launch();
+        if (prof && rc == OK && prof->end() != OK) return E_CUDA;
+        return rc;
+    };
+    if (reset) {
+        int rc = timed(P_INIT, [&] { return launch_init_zero_on(st, h); });
+        if (rc != OK) return rc;
+    }
+    for (const Step &s : c->steps) {
+        int rc = OK;
+        switch (s.kind) {
+        case K_GATE:
+            rc = timed(P_GATE, [&] {
+                return launch_gate_on(st, h, s.code, s.a, s.b,
+                                      s.rec >= 0 ? h->recs[(size_t)c->rec_ids[(size_t)s.rec]].res : nullptr);
+            });
+            break;
+        case K_CHANNEL:
+            rc = timed(P_CHANNEL, [&] {
+                return launch_channel_rp(st, h, s.a, s.b, c->d_thr + s.first, s.count, s.event, c->d_params,
+                                         c->d_masks);
+            });
+            break;
+        case K_MEAS:
+            rc = timed(P_MEASURE, [&] {
+                return launch_measure_list(st, h->X, h->Z, h->R, h->n, h->w, c->d_meas + s.first, s.count,
+                                           (uint64_t)h->seed, 0, c->d_params);
+            });
+            break;
+        case K_SEGMENT: {
+            const SegHost &sg = c->segs[(size_t)s.first];
+            if (!sg.slots.empty()) rc = timed(P_SAMPLE, [&] { return launch_noise_sample(st, sg.dev, h->w, c->d_params); });
+            if (rc == OK)
+                rc = timed(P_SEGMENT, [&] {
+                    return launch_segment(st, h->X, h->Z, h->R, h->n, h->w, sg.dev, c->opts.seg_rows,
+                                          c->opts.seg_words, c->opts.seg_threads, c->d_recs);
+                });
+            break;
+        }
+        default: break;
+        }
+        if (rc != OK) return rc;
+    }
+    return OK;
+}
+
+}  // namespace
+}  // namespace ps
+
+extern "C" {
+
+ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, const float *params, uint64_t nparams,
+                             const ps_circuit_options *opts, ps_circuit **out) {
+    ps_enter(__func__, __LINE__);
+    if (!h || !out) return fail(E_ARG, "null handle");
+    if (nops && !ops_in) return fail(E_ARG, "null op table");
+    *out = nullptr;
+    std::vector<ps_op> ops(ops_in, ops_in + nops);
+    auto *c = new ps_circuit;
+    c->h = h;
+    if (opts) c->opts = *opts;
+    const bool fused = c->opts.mode == PS_MODE_FUSED;
+    auto bail = [&](int rc) {
+        ps_circuit_destroy(c);
+        return rc;
+    };
+
+    // ---- validate ops, assign events / records / thresholds
+    std::vector<uint32_t> event_of(ops.size(), 0);
+    std::vector<int32_t> rec_of(ops.size(), -1), thr_off(ops.size(), -1);
+    std::vector<uint64_t> thr;
+    uint32_t ev = 0;
+    int32_t nrec = 0;
+    for (size_t i = 0; i < ops.size(); ++i) {
+        const ps_op &o = ops[i];
+        auto qok = [&](int32_t q) { return q >= 0 && q < h->n; };
+        if (o.code < OP_H || o.code > OP_S_IF) return bail(fail(E_ARG, "op " + std::to_string(i) + ": bad code"));
+        if (!qok(o.a)) return bail(fail(E_ARG, "op " + std::to_string(i) + ": qubit out of range"));
+        if ((o.code == OP_CX || o.code == OP_CZ || o.code == OP_PAULI2) && (!qok(o.b) || o.b == o.a))
+            return bail(fail(E_ARG, "op " + std::to_string(i) + ": bad second qubit"));
+        if (o.code == OP_H_IF || o.code == OP_S_IF) {
+            if (o.c < 0 || o.c >= nrec) return bail(fail(E_ARG, "op " + std::to_string(i) + ": record not measured yet"));
+        }
+        if (o.code == OP_M && o.c >= 0 && (uint64_t)o.c >= nparams)
+            return bail(fail(E_ARG, "op " + std::to_string(i) + ": bias index out of range"));
+        if (is_channel(o.code)) {
+            const int cnt = o.code == OP_PAULI2 ? 15 : 3;
+            if (o.c < 0 || (uint64_t)o.c + cnt > nparams)
+                return bail(fail(E_ARG, "op " + std::to_string(i) + ": channel parameters out of range"));
+            uint64_t t[15];
+            channel_thresholds(params + o.c, cnt, t);
+            thr_off[i] = (int32_t)thr.size();
+            thr.insert(thr.end(), t, t + cnt);
+        }
+        if (is_meas(o.code)) rec_of[i] = nrec++;
+        if (is_meas(o.code) || is_channel(o.code)) event_of[i] = ev++;
+    }
+    c->num_events = ev;
+
+    // ---- records: one contiguous block, so a run's records copy out at once
+    c->stats.first_record = h->recs.size();
+    {
+        std::vector<int64_t> qubits;
+        for (size_t i = 0; i < ops.size(); ++i)
+            if (is_meas(ops[i].code)) qubits.push_back(ops[i].a);
+        int rc = record_block(h, qubits, c->rec_ids, &c->d_res_block, &c->d_det_block);
+        if (rc != OK) return bail(rc);
+    }
+    std::vector<u64 *> rec_ptrs;
+    for (int64_t id : c->rec_ids) rec_ptrs.push_back(h->recs[(size_t)id].res);
+    if (upload(c->owned, rec_ptrs, &c->d_recs) != OK) return bail(E_CUDA);
+    if (thr.empty()) thr.push_back(0);
+    if (upload(c->owned, thr, &c->d_thr) != OK) return bail(E_CUDA);
+    {
+        void *p = nullptr;
+        if (cudaMalloc(&p, sizeof(RunParams)) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "cudaMalloc"));
+        c->owned.push_back(p);
+        c->d_params = (RunParams *)p;
+        if (cudaMalloc(&p, 4 * (size_t)h->w * sizeof(u64)) != cudaSuccess)
+            return bail(cuda_fail(cudaGetLastError(), "cudaMalloc"));
+        c->owned.push_back(p);
+        c->d_masks = (u64 *)p;
+    }
+
+    // ---- plan
+    auto add_meas = [&](size_t i, int reset) {
+        MeasOp m{};
+        m.q = ops[i].a;
+        m.reset = reset;
+        m.bias = (ops[i].code == OP_M && ops[i].c >= 0) ? params[ops[i].c] : 0.5f;
+        m.event = event_of[i];
+        m.forced = nullptr;
+        const Record &r = h->recs[(size_t)c->rec_ids[(size_t)rec_of[i]]];
+        m.res = r.res;
+        m.det = r.det;
+        c->meas.push_back(m);
+    };
+    size_t max_slots = 0;
+    int nq_max = 1;
+    if (!fused) {
+        for (size_t i = 0; i < ops.size(); ++i) {
+            const ps_op &o = ops[i];
+            Step s{};
+            if (is_meas(o.code)) {
+                s.kind = K_MEAS;
+                s.first = (int32_t)c->meas.size();
+                s.count = 1;
+                add_meas(i, o.code == OP_R);
+            } else if (is_channel(o.code)) {
+                s.kind = K_CHANNEL;
+                s.a = o.a;
+                s.b = o.code == OP_PAULI2 ? o.b : 0;
+                s.count = o.code == OP_PAULI2 ? 15 : 3;
+                s.first = thr_off[i];
+                s.event = event_of[i];
+            } else {
+                s.kind = K_GATE;
+                s.code = o.code;
+                s.a = o.a;
+                s.b = (o.code == OP_CX || o.code == OP_CZ) ? o.b : 0;
+                s.rec = (o.code == OP_H_IF || o.code == OP_S_IF) ? o.c : -1;
+            }
+            c->steps.push_back(s);
+        }
+    } else {
+        std::vector<std::pair<int64_t, int32_t>> pending;  // deferred reset X: (qubit, record)
+        size_t i = 0;
+        while (i < ops.size()) {
+            size_t j = i;
+            if (is_meas(ops[i].code)) {
+                while (j < ops.size() && is_meas(ops[j].code)) ++j;
+                const bool more_segments = j < ops.size();
+                Step s{};
+                s.kind = K_MEAS;
+                s.first = (int32_t)c->meas.size();
+                s.count = (int32_t)(j - i);
+                for (size_t k = i; k < j; ++k) {
+                    bool later_same = false;
+                    for (size_t t = k + 1; t < j; ++t) later_same |= ops[t].a == ops[k].a;
+                    const bool defer = ops[k].code == OP_R && h->valid && more_segments && !later_same;
+                    add_meas(k, ops[k].code == OP_R && !defer);
+                    if (defer) pending.emplace_back(ops[k].a, rec_of[k]);
+                }
+                c->steps.push_back(s);
+            } else {
+                while (j < ops.size() && !is_meas(ops[j].code)) ++j;
+                SegHost seg;
+                build_segment(c, ops, i, j, event_of, rec_of, thr_off, pending, seg);
+                pending.clear();
+                nq_max = std::max(nq_max, (int)seg.cols.size());
+                max_slots = std::max(max_slots, seg.slots.size());
+                Step s{};
+                s.kind = K_SEGMENT;
+                s.first = (int32_t)c->segs.size();
+                c->segs.push_back(std::move(seg));
+                c->steps.push_back(s);
+            }
+            i = j;
+        }
+    }
+    pick_tile(c, nq_max);
+    if (fused) {
+        c->entry_cap = (int32_t)std::max<size_t>(1, max_slots);
+        void *p = nullptr;
+        if (cudaMalloc(&p, (size_t)c->entry_cap * h->w * sizeof(NoiseEntry)) != cudaSuccess)
+            return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
+        c->owned.push_back(p);
+        c->d_entries = (NoiseEntry *)p;
+        if (cudaMalloc(&p, (size_t)h->w * sizeof(int32_t)) != cudaSuccess)
+            return bail(fail(E_NOMEM, "device allocation failed"));
+        c->owned.push_back(p);
+        c->d_entry_count = (int32_t *)p;
+        if (cudaMalloc(&p, (size_t)c->entry_cap * h->w * 4 * sizeof(u64)) != cudaSuccess)
+            return bail(fail(E_NOMEM, "device allocation of channel sampling scratch failed"));
+        c->owned.push_back(p);
+        c->d_dense = (u64 *)p;
+        for (SegHost &sg : c->segs) {
+            SegmentDev d{};
+            SegLayer *dl;
+            SegGate *dg;
+            SegSign *ds;
+            int32_t *dc;
+            NoiseSlot *dsl;
+            if (upload(c->owned, sg.layers, &dl) || upload(c->owned, sg.gates, &dg) || upload(c->owned, sg.signs, &ds) ||
+                upload(c->owned, sg.cols, &dc) || upload(c->owned, sg.slots, &dsl))
+                return bail(E_CUDA);
+            d.layers = dl;
+            d.nlayers = (int32_t)sg.layers.size();
+            d.gates = dg;
+            d.signs = ds;
+            d.cols = dc;
+            d.nq = (int32_t)sg.cols.size();
+            d.slots = dsl;
+            d.nslots = (int32_t)sg.slots.size();
+            d.thr = c->d_thr;
+            d.entries = sg.slots.empty() ? nullptr : c->d_entries;
+            d.entry_count = c->d_entry_count;
+            d.cap = c->entry_cap;
+            d.dense = c->d_dense;
+            sg.dev = d;
+            const double W = (double)h->W, B8 = (double)h->S / 8.0;
+            c->stats.segment_bytes += 2.0 * (2.0 * (double)sg.cols.size() + 1.0) * W * B8;
+            if (segment_smem_bytes(d.nq, c->opts.seg_rows, c->opts.seg_words) > 227 * 1024)
+                return bail(fail(E_ARG, "too many touched qubits for one fused tile"));
+        }
+    }
+    if (upload(c->owned, c->meas, &c->d_meas) != OK) return bail(E_CUDA);
+
+    // ---- stats
+    ps_circuit_stats &st = c->stats;
+    st.num_ops = ops.size();
+    for (auto &o : ops) {
+        if (o.code <= OP_R) st.num_gates++;
+        if (is_meas(o.code)) st.num_measurements++;
+        if (is_channel(o.code)) st.num_channels++;
+    }
+    st.num_events = c->num_events;
+    for (auto &s : c->steps) {
+        if (s.kind == K_SEGMENT) {
+            st.num_segments++;
+            st.launches_per_run += c->segs[(size_t)s.first].slots.empty() ? 1 : 3;
+        } else if (s.kind == K_MEAS) {
+            st.num_measure_phases++;
+            st.launches_per_run += 1;
+        } else if (s.kind == K_CHANNEL) {
+            st.launches_per_run += s.count == 15 ? 3 : 2;
+        } else {
+            st.launches_per_run += 1;
+        }
+    }
+    st.launches_per_run += 1;  // run-parameter update
+    st.seg_rows = c->opts.seg_rows;
+    st.seg_words = c->opts.seg_words;
+    st.seg_threads = c->opts.seg_threads;
+
+    // ---- graph capture
+    if (c->opts.use_graph) {
+        for (int reset = 0; reset < 2; ++reset) {
+            cudaStream_t cs;
+            if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+                return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            int rc = e == cudaSuccess ? enqueue_plan(c, cs, reset != 0) : cuda_fail(e, "cudaStreamBeginCapture");
+            cudaGraph_t g = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+            cudaStreamDestroy(cs);
+            if (rc != OK) {
+                if (g) cudaGraphDestroy(g);
+                return bail(rc);
+            }
+            if (e2 != cudaSuccess) return bail(cuda_fail(e2, "cudaStreamEndCapture"));
+            c->graph[reset] = g;
+            e = cudaGraphInstantiate(&c->exec[reset], g, 0);
+            if (e != cudaSuccess) return bail(cuda_fail(e, "cudaGraphInstantiate"));
+        }
+    }
+    *out = c;
+    return OK;
+}
+
+ps_status ps_circuit_set_forced(ps_circuit *c, const uint8_t *forced_all) {
+    ps_enter(__func__, __LINE__);
+    if (!c) return fail(E_ARG, "null circuit");
+    ps_state *h = c->h;
+    const size_t nm = c->meas.size();
+    if (forced_all && nm) {
+        if (!c->d_forced) {
+            if (cudaMalloc(&c->d_forced, nm * (size_t)h->w * sizeof(u64)) != cudaSuccess)
+                return fail(E_NOMEM, "device allocation of forced draws failed");
+        }
+        std::vector<u64> buf(nm * (size_t)h->w, 0ull);
+        const size_t nb = (size_t)(h->S + 7) / 8;
+        for (size_t k = 0; k < nm; ++k) {
+            std::memcpy(&buf[k * (size_t)h->w], forced_all + k * nb, nb);
+            if (h->S % 8) reinterpret_cast<uint8_t *>(&buf[k * (size_t)h->w])[nb - 1] &= (uint8_t)((1u << (h->S % 8)) - 1u);
+        }
+        PS_CUDA(cudaMemcpy(c->d_forced, buf.data(), buf.size() * sizeof(u64), cudaMemcpyHostToDevice));
+    }
+    // Measurement k of the circuit (program order) is meas[] entry k.
+    std::vector<MeasOp> m = c->meas;
+    for (size_t k = 0; k < nm; ++k) m[k].forced = forced_all ? c->d_forced + k * (size_t)h->w : nullptr;
+    PS_CUDA(cudaStreamSynchronize(h->stream));
+    PS_CUDA(cudaMemcpy(c->d_meas, m.data(), nm * sizeof(MeasOp), cudaMemcpyHostToDevice));
+    c->meas = m;
+    return OK;
+}
+
+ps_status ps_circuit_run(ps_circuit *c, int reset_state) {
+    ps_enter(__func__, __LINE__);
+    if (!c) return fail(E_ARG, "null circuit");
+    ps_state *h = c->h;
+    for (int64_t id : c->rec_ids) h->recs[(size_t)id].host_valid = false;
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, (uint64_t)h->seed, h->events);
+    PS_CUDA(cudaGetLastError());
+    h->events += c->num_events;
+    if (reset_state) h->valid = true;
+    if (c->exec[reset_state ? 1 : 0]) {
+        PS_CUDA(cudaGraphLaunch(c->exec[reset_state ? 1 : 0], h->stream));
+        return OK;
+    }
+    return enqueue_plan(c, h->stream, reset_state != 0);
+}
+
+ps_status ps_circuit_profile(ps_circuit *c, int reset_state, ps_circuit_profile_t *out) {
+    ps_enter(__func__, __LINE__);
+    if (!c || !out) return fail(E_ARG, "null argument");
+    ps_state *h = c->h;
+    std::memset(out, 0, sizeof(*out));
+    for (int64_t id : c->rec_ids) h->recs[(size_t)id].host_valid = false;
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, (uint64_t)h->seed, h->events);
+    PS_CUDA(cudaGetLastError());
+    h->events += c->num_events;
+    if (reset_state) h->valid = true;
+    Profiler prof;
+    prof.st = h->stream;
+    int rc = enqueue_plan(c, h->stream, reset_state != 0, &prof);
+    if (rc != OK) return rc;
+    PS_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto &m : prof.marks) {
+        float ms = 0.f;
+        PS_CUDA(cudaEventElapsedTime(&ms, m.second.first, m.second.second));
+        out->ms[m.first] += ms;
+        out->launches[m.first] += 1;
+    }
+    return OK;
+}
+
+ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *random_branch, int32_t *rows) {
+    ps_enter(__func__, __LINE__);
+    if (!c || !random_branch || !rows) return fail(E_ARG, "null argument");
+    ps_state *h = c->h;
+    const size_t nm = c->meas.size();
+    if (nm == 0) return OK;
+    int32_t *d = nullptr;
+    PS_CUDA(cudaMalloc(&d, nm * 2 * sizeof(int32_t)));
+    std::vector<MeasOp> m = c->meas;
+    for (size_t k = 0; k < nm; ++k) m[k].kstat = d + 2 * k;
+    PS_CUDA(cudaStreamSynchronize(h->stream));
+    PS_CUDA(cudaMemcpy(c->d_meas, m.data(), nm * sizeof(MeasOp), cudaMemcpyHostToDevice));
+    for (int64_t id : c->rec_ids) h->recs[(size_t)id].host_valid = false;
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, (uint64_t)h->seed, h->events);
+    h->events += c->num_events;
+    if (reset_state) h->valid = true;
+    int rc = enqueue_plan(c, h->stream, reset_state != 0);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    std::vector<int32_t> host(nm * 2);
+    if (rc == OK && e == cudaSuccess) e = cudaMemcpy(host.data(), d, nm * 2 * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(c->d_meas, c->meas.data(), nm * sizeof(MeasOp), cudaMemcpyHostToDevice);
+    cudaFree(d);
+    if (rc != OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "measure stats");
+    for (size_t k = 0; k < nm; ++k) {
+        random_branch[k] = host[2 * k];
+        rows[k] = host[2 * k + 1];
+    }
+    return OK;
+}
+
+ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *determined, uint64_t *words) {
+    ps_enter(__func__, __LINE__);
+    if (!c) return fail(E_ARG, "null circuit");
+    ps_state *h = c->h;
+    const size_t bytes = c->rec_ids.size() * (size_t)h->w * sizeof(u64);
+    if (words) *words = (uint64_t)h->w;
+    if (results && bytes)
+        PS_CUDA(cudaMemcpyAsync(results, c->d_res_block, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (determined && bytes)
+        PS_CUDA(cudaMemcpyAsync(determined, c->d_det_block, bytes, cudaMemcpyDeviceToHost, h->stream));
+    PS_CUDA(cudaStreamSynchronize(h->stream));
+    return OK;
+}
+
+ps_status ps_circuit_get_stats(const ps_circuit *c, ps_circuit_stats *out) {
+    ps_enter(__func__, __LINE__);
+    if (!c || !out) return fail(E_ARG, "null argument");
+    *out = c->stats;
+    return OK;
+}
+
+ps_status ps_circuit_destroy(ps_circuit *c) {
+    ps_enter(__func__, __LINE__);
+    if (!c) return OK;
+    if (c->h && c->h->stream) cudaStreamSynchronize(c->h->stream);
+    for (int k = 0; k < 2; ++k) {
+        if (c->exec[k]) cudaGraphExecDestroy(c->exec[k]);
+        if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
+    }
+    for (void *p : c->owned) cudaFree(p);
+    cudaFree(c->d_forced);
+    delete c;
+    return OK;
+}
+
+}  // extern "C"

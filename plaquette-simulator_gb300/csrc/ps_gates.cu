@@ -6,6 +6,7 @@
 #include <cmath>
 
 #include "ps_internal.h"
+#include "ps_segment.cuh"
 
 namespace ps {
 
@@ -105,41 +106,47 @@ __global__ void __launch_bounds__(256) gate2_kernel(u64 *__restrict__ X, u64 *__
 // shot one Philox draw u picks Pauli k = first index with u < thr[k]
 // (0 = identity).  Output masks: fx = shots with X or Y, fz = Y or Z, for
 // qubit a (slot 0) and b (slot 1).
-__global__ void channel_sample_kernel(u64 *__restrict__ masks, int64_t w, uint64_t seed, uint64_t event,
-                                      uint64_t word0, int count, uint64_t t0, uint64_t t1, uint64_t t2,
-                                      const uint64_t *__restrict__ thr15) {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= w) return;
+// 16 threads per 64-shot word: thread `sub` computes Philox block `sub`
+// (shots 4*sub .. 4*sub+3); the four masks are OR-reduced over the 16 lanes.
+__global__ void __launch_bounds__(256) channel_sample_kernel(u64 *__restrict__ masks, int64_t w, uint64_t seed_arg,
+                                                            uint64_t event_arg, const RunParams *__restrict__ rp,
+                                                            int count, const uint64_t *__restrict__ thr) {
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t k = gt >> 4;
+    const uint32_t sub = (uint32_t)(gt & 15);
+    const uint64_t seed = rp ? rp->seed : seed_arg;
+    const uint64_t event = (rp ? rp->event_base : 0ull) + event_arg;
     u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
-    for (uint32_t sub = 0; sub < 16; ++sub) {
-        const u32x4 u = draw_block(seed, event, word0 + (uint64_t)k, sub, TAG_NOISE);
+    if (k < w) {
+        const uint64_t total = thr[count - 1];
+        const u32x4 u = draw_block(seed, event, (uint64_t)k, sub, TAG_NOISE);
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
             const uint64_t v = u.v[l];
-            int idx = 0;
-            if (count == 3) {
-                idx = v < t0 ? 1 : v < t1 ? 2 : v < t2 ? 3 : 0;
-            } else {
-                for (int j = 0; j < 15; ++j)
-                    if (v < thr15[j]) {
-                        idx = j + 1;
-                        break;
-                    }
-            }
-            if (idx) {
-                const u64 bit = 1ull << (sub * 4 + l);
-                const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
-                if (pa == 1 || pa == 2) fxa |= bit;
-                if (pa == 2 || pa == 3) fza |= bit;
-                if (pb == 1 || pb == 2) fxb |= bit;
-                if (pb == 2 || pb == 3) fzb |= bit;
-            }
+            if (v >= total) continue;  // identity, the common case
+            int idx = 1;
+            while (v >= thr[idx - 1]) ++idx;
+            const u64 bit = 1ull << (sub * 4 + l);
+            const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
+            if (pa == 1 || pa == 2) fxa |= bit;
+            if (pa == 2 || pa == 3) fza |= bit;
+            if (pb == 1 || pb == 2) fxb |= bit;
+            if (pb == 2 || pb == 3) fzb |= bit;
         }
     }
-    masks[k] = fxa;
-    masks[w + k] = fza;
-    masks[2 * w + k] = fxb;
-    masks[3 * w + k] = fzb;
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) {
+        fxa |= __shfl_xor_sync(0xffffffffu, fxa, off);
+        fza |= __shfl_xor_sync(0xffffffffu, fza, off);
+        fxb |= __shfl_xor_sync(0xffffffffu, fxb, off);
+        fzb |= __shfl_xor_sync(0xffffffffu, fzb, off);
+    }
+    if (sub == 0 && k < w) {
+        masks[k] = fxa;
+        masks[w + k] = fza;
+        masks[2 * w + k] = fxb;
+        masks[3 * w + k] = fzb;
+    }
 }
 
 // r ^= (fx & z_q) ^ (fz & x_q) over all rows: X flips rows with Z on q, Z
@@ -165,25 +172,41 @@ inline int blocks_for(int64_t threads) { return (int)((threads + 255) / 256); }
 
 }  // namespace
 
-int launch_gate(ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag) {
+int launch_gate_on(cudaStream_t st, ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag) {
     const int64_t work = h->W * (h->w >> 1);
     const int grid = blocks_for(work);
     if (h->n == 0 || work == 0) return OK;
     switch (code) {
-    case OP_H: gate1_kernel<OP_H><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
-    case OP_S: gate1_kernel<OP_S><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
-    case OP_X: gate1_kernel<OP_X><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
-    case OP_Y: gate1_kernel<OP_Y><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
-    case OP_Z: gate1_kernel<OP_Z><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
-    case OP_H_IF:
-        gate1_kernel<OP_H_IF><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, flag);
-        break;
-    case OP_S_IF:
-        gate1_kernel<OP_S_IF><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, flag);
-        break;
-    case OP_CX: gate2_kernel<OP_CX><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, b); break;
-    case OP_CZ: gate2_kernel<OP_CZ><<<grid, 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, b); break;
+    case OP_H: gate1_kernel<OP_H><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_S: gate1_kernel<OP_S><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_X: gate1_kernel<OP_X><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_Y: gate1_kernel<OP_Y><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_Z: gate1_kernel<OP_Z><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, nullptr); break;
+    case OP_H_IF: gate1_kernel<OP_H_IF><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, flag); break;
+    case OP_S_IF: gate1_kernel<OP_S_IF><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, flag); break;
+    case OP_CX: gate2_kernel<OP_CX><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, b); break;
+    case OP_CZ: gate2_kernel<OP_CZ><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, b); break;
     default: return fail(E_ARG, "unknown gate code " + std::to_string(code));
+    }
+    PS_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int launch_gate(ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag) {
+    return launch_gate_on(h->stream, h, code, a, b, flag);
+}
+
+int launch_channel_rp(cudaStream_t st, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,
+                      uint32_t event_off, const RunParams *rp, u64 *masks) {
+    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, st>>>(masks, h->w, (uint64_t)h->seed, event_off, rp, count,
+                                                             dev_thr);
+    PS_CUDA(cudaGetLastError());
+    const int64_t work = h->W * (h->w >> 1);
+    if (h->n > 0 && work > 0) {
+        sign_flip_kernel<<<blocks_for(work), 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, masks, masks + h->w);
+        if (count == 15)
+            sign_flip_kernel<<<blocks_for(work), 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, b,
+                                                                masks + 2 * h->w, masks + 3 * h->w);
     }
     PS_CUDA(cudaGetLastError());
     return OK;
@@ -204,16 +227,11 @@ void channel_thresholds(const float *p, int count, uint64_t *thr) {
 
 int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thr, int count) {
     const uint64_t event = h->events++;
-    const uint64_t *thr15 = nullptr;
     uint64_t *dthr = nullptr;
-    if (count == 15) {
-        PS_CUDA(cudaMallocAsync(&dthr, 15 * sizeof(uint64_t), h->stream));
-        PS_CUDA(cudaMemcpyAsync(dthr, thr, 15 * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
-        thr15 = dthr;
-    }
-    channel_sample_kernel<<<blocks_for(h->w), 256, 0, h->stream>>>(
-        h->mask_buf, h->w, (uint64_t)h->seed, event, 0, count, thr[0], count == 3 ? thr[1] : 0,
-        count == 3 ? thr[2] : 0, thr15);
+    PS_CUDA(cudaMallocAsync(&dthr, 15 * sizeof(uint64_t), h->stream));
+    PS_CUDA(cudaMemcpyAsync(dthr, thr, (size_t)count * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, h->stream>>>(h->mask_buf, h->w, (uint64_t)h->seed, event,
+                                                                    nullptr, count, dthr);
     PS_CUDA(cudaGetLastError());
     const int64_t work = h->W * (h->w >> 1);
     if (h->n > 0 && work > 0) {
@@ -224,7 +242,7 @@ int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thr,
                                                                       h->mask_buf + 2 * h->w, h->mask_buf + 3 * h->w);
     }
     PS_CUDA(cudaGetLastError());
-    if (dthr) PS_CUDA(cudaFreeAsync(dthr, h->stream));
+    PS_CUDA(cudaFreeAsync(dthr, h->stream));
     return OK;
 }
 

@@ -27,6 +27,7 @@ struct Record {
 // records instead of one per measurement).
 struct RecordArena {
     std::vector<u64 *> chunks;
+    std::vector<u64 *> blocks;  // contiguous blocks of compiled circuits
     size_t per_chunk = 64;
     size_t used_in_last = 0;
     size_t words = 0;  // words per record array
@@ -47,6 +48,8 @@ struct MeasOp {
     const u64 *forced;  // device packed bits (w words) or nullptr
     u64 *res;           // record words
     u64 *det;
+    int32_t *kstat;     // optional: {random branch taken, rows multiplied} of shot word 0
+    int32_t pad;
 };
 
 } // namespace ps
@@ -68,14 +71,27 @@ struct ps_state {
     std::vector<ps::Record> recs;
     ps::RecordArena arena;
     int device = 0;
+    // True while the tableau is known to be a valid stabilizer tableau
+    // (built from |0...0> by gates and measurements).  A tableau loaded from
+    // the host may not be; compiled circuits then keep every reset's X
+    // inside its measurement phase instead of deferring it.
+    bool valid = false;
 };
 
 namespace ps {
+// ps_capi.cpp: records the entry point for error messages, clears the error.
+void ps_enter(const char *method, int line);
+
 // ps_state.cu
 int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed);
 void state_free(ps_state *h);
 int launch_init_zero(ps_state *h);
+int launch_init_zero_on(cudaStream_t stream, ps_state *h);
 int record_new(ps_state *h, int64_t q, int64_t *id);
+// One contiguous device block for many records (results rows, then
+// determined rows); the state owns it.
+int record_block(ps_state *h, const std::vector<int64_t> &qubits, std::vector<int64_t> &ids, u64 **res_block,
+                 u64 **det_block);
 int record_fetch(ps_state *h, int64_t id);
 int pack_from_host(ps_state *h, const int32_t *x, const int32_t *z, const int32_t *r);
 int unpack_to_host(ps_state *h, int32_t *x, int32_t *z, int32_t *r);
@@ -89,5 +105,20 @@ int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thre
 void channel_thresholds(const float *p, int count, uint64_t *thr);
 
 // ps_measure.cu
+struct RunParams;
 int launch_measure(ps_state *h, const MeasOp *ops_host, int nops);
+int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops,
+                        int nops, uint64_t seed, uint64_t word_base, const RunParams *rp);
+
+// ps_segment.cu
+struct SegmentDev;
+size_t segment_smem_bytes(int nq, int rows, int bw);
+int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp);
+int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
+                   int rows, int bw, int threads, const u64 *const *recs);
+
+// ps_gates.cu (compiled-circuit form of the per-op kernels)
+int launch_channel_rp(cudaStream_t stream, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,
+                      uint32_t event_off, const RunParams *rp, u64 *dev_masks);
+int launch_gate_on(cudaStream_t stream, ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag);
 } // namespace ps

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "ps_internal.h"
+#include "ps_segment.cuh"
 
 namespace ps {
 
@@ -52,8 +53,10 @@ __device__ __forceinline__ void warp_phase_reduce(u64 &c1, u64 &c0) {
 }
 
 __global__ void __launch_bounds__(1024) measure_kernel(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w,
-                                                      const MeasOp *__restrict__ ops, int nops, uint64_t seed,
-                                                      uint64_t word_base) {
+                                                      const MeasOp *__restrict__ ops, int nops, uint64_t seed_arg,
+                                                      uint64_t word_base, const RunParams *__restrict__ rp) {
+    const uint64_t seed = rp ? rp->seed : seed_arg;
+    const uint64_t event_base = rp ? rp->event_base : 0ull;
     extern __shared__ u64 dyn[];
     __shared__ MeasSmem sm;
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = T >> 5;
@@ -117,7 +120,7 @@ __global__ void __launch_bounds__(1024) measure_kernel(u64 *X, u64 *Z, u64 *R, i
                             if (u < op.bias) bits |= 1ull << b;
                         }
                     } else {
-                        const u32x4 u = draw_block(seed, op.event, word_base + (uint64_t)k, (uint32_t)lane, TAG_MEASURE);
+                        const u32x4 u = draw_block(seed, event_base + op.event, word_base + (uint64_t)k, (uint32_t)lane, TAG_MEASURE);
 #pragma unroll
                         for (int l = 0; l < 4; ++l)
                             if (unit_float(u.v[l]) < op.bias) bits |= 1ull << (lane * 4 + l);
@@ -132,6 +135,7 @@ __global__ void __launch_bounds__(1024) measure_kernel(u64 *X, u64 *Z, u64 *R, i
         const int ng = sm.ngroups;
         const u64 outcome = sm.outcome;
         u64 res_word = 0ull;
+        int rows_done = 0;
         // 3. random branch, one group of shots (same pivot) at a time
         for (int g = 0; g < ng; ++g) {
             const int64_t p = sm.gp[g];
@@ -162,6 +166,7 @@ __global__ void __launch_bounds__(1024) measure_kernel(u64 *X, u64 *Z, u64 *R, i
                 if (i != p && i != p + n && (col[i] & m)) rowlist[atomicAdd(&sm.cnt, 1)] = (int)i;
             __syncthreads();
             const int cnt = sm.cnt;
+            rows_done += cnt;
             for (int t = warp; t < cnt; t += nwarps) {
                 const int64_t i = rowlist[t];
                 const u64 mi = col[i] & m;
@@ -198,6 +203,7 @@ __global__ void __launch_bounds__(1024) measure_kernel(u64 *X, u64 *Z, u64 *R, i
             }
             __syncthreads();
             const int cnt = sm.cnt;
+            rows_done += cnt;
             u64 ax[MAXC], az[MAXC];
 #pragma unroll
             for (int u = 0; u < MAXC; ++u) ax[u] = az[u] = 0ull;
@@ -254,6 +260,10 @@ __global__ void __launch_bounds__(1024) measure_kernel(u64 *X, u64 *Z, u64 *R, i
         if (tid == 0) {
             op.res[k] = res_word;
             op.det[k] = dm;
+            if (op.kstat && k == 0) {
+                op.kstat[0] = ng > 0;
+                op.kstat[1] = rows_done;
+            }
         }
         __syncthreads();
         // ResetQubit: X on shots with outcome 1 flips rows with Z on q.
@@ -272,13 +282,13 @@ size_t measure_smem_bytes(int64_t n, int threads) {
 int measure_threads(int64_t n) { return n <= 256 * MAXC ? 256 : 1024; }
 
 int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops,
-                        int nops, uint64_t seed, uint64_t word_base) {
+                        int nops, uint64_t seed, uint64_t word_base, const RunParams *rp) {
     const int T = measure_threads(n);
     if (n > (int64_t)T * MAXC) return fail(E_ARG, "too many qubits for the measurement kernel (max 8192)");
     const size_t smem = measure_smem_bytes(n, T);
     if (smem > 48 * 1024)
         PS_CUDA(cudaFuncSetAttribute(measure_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    measure_kernel<<<(unsigned)w, T, smem, stream>>>(X, Z, R, n, w, dev_ops, nops, seed, word_base);
+    measure_kernel<<<(unsigned)w, T, smem, stream>>>(X, Z, R, n, w, dev_ops, nops, seed, word_base, rp);
     PS_CUDA(cudaGetLastError());
     return OK;
 }
@@ -292,7 +302,7 @@ int launch_measure(ps_state *h, const MeasOp *ops_host, int nops) {
         h->meas_cap = (size_t)nops;
     }
     PS_CUDA(cudaMemcpyAsync(h->meas_buf, ops_host, (size_t)nops * sizeof(MeasOp), cudaMemcpyHostToDevice, h->stream));
-    return launch_measure_list(h->stream, h->X, h->Z, h->R, h->n, h->w, h->meas_buf, nops, (uint64_t)h->seed, 0);
+    return launch_measure_list(h->stream, h->X, h->Z, h->R, h->n, h->w, h->meas_buf, nops, (uint64_t)h->seed, 0, nullptr);
 }
 
 }  // namespace ps

@@ -139,17 +139,21 @@ void state_free(ps_state *h) {
     cudaFree(h->mask_buf);
     cudaFree(h->meas_buf);
     for (u64 *c : h->arena.chunks) cudaFree(c);
+    for (u64 *c : h->arena.blocks) cudaFree(c);
     h->arena.chunks.clear();
+    h->arena.blocks.clear();
     if (h->stream) cudaStreamDestroy(h->stream);
     h->X = h->Z = h->R = nullptr;
 }
 
-int launch_init_zero(ps_state *h) {
+int launch_init_zero_on(cudaStream_t stream, ps_state *h) {
     if (h->n == 0) return OK;
-    init_zero_kernel<<<grid_for(h->W * h->n * h->w), 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w);
+    init_zero_kernel<<<grid_for(h->W * h->n * h->w), 256, 0, stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w);
     PS_CUDA(cudaGetLastError());
     return OK;
 }
+
+int launch_init_zero(ps_state *h) { return launch_init_zero_on(h->stream, h); }
 
 int record_new(ps_state *h, int64_t q, int64_t *id) {
     RecordArena &a = h->arena;
@@ -170,6 +174,33 @@ int record_new(ps_state *h, int64_t q, int64_t *id) {
     PS_CUDA(cudaMemsetAsync(rec.res, 0, 2 * a.words * sizeof(u64), h->stream));
     h->recs.push_back(std::move(rec));
     *id = (int64_t)h->recs.size() - 1;
+    return OK;
+}
+
+int record_block(ps_state *h, const std::vector<int64_t> &qubits, std::vector<int64_t> &ids, u64 **res_block,
+                 u64 **det_block) {
+    const size_t nm = qubits.size(), wds = (size_t)h->w;
+    ids.clear();
+    *res_block = *det_block = nullptr;
+    if (nm == 0) return OK;
+    u64 *blk = nullptr;
+    if (cudaMalloc(&blk, 2 * nm * wds * sizeof(u64)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(E_NOMEM, "device allocation of measurement records failed");
+    }
+    PS_CUDA(cudaMemsetAsync(blk, 0, 2 * nm * wds * sizeof(u64), h->stream));
+    // The state owns the block (freed with the state), like its other records.
+    h->arena.blocks.push_back(blk);
+    *res_block = blk;
+    *det_block = blk + nm * wds;
+    for (size_t k = 0; k < nm; ++k) {
+        Record rec;
+        rec.qubit = qubits[k];
+        rec.res = blk + k * wds;
+        rec.det = blk + (nm + k) * wds;
+        h->recs.push_back(std::move(rec));
+        ids.push_back((int64_t)h->recs.size() - 1);
+    }
     return OK;
 }
 

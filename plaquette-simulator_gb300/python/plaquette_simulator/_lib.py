@@ -6,6 +6,7 @@ package raises ImportError.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
 
@@ -22,6 +23,8 @@ _SIGS = {
     "ps_last_error": (C.c_char_p, []),
     "ps_backend_name": (C.c_char_p, []),
     "ps_version": (C.c_char_p, []),
+    "ps_set_device": (C.c_int, [C.c_int]),
+    "ps_device_synchronize": (C.c_int, []),
     "ps_create": (C.c_int, [_u64, _u64, _i64, C.c_int, _pp]),
     "ps_create_from_host": (C.c_int, [_vp, _vp, _vp, _u64, _u64, _i64, _pp]),
     "ps_clone": (C.c_int, [_vp, _pp]),
@@ -54,12 +57,38 @@ _SIGS = {
     "ps_reset_qubit": (C.c_int, [_vp, _u64, _vp, _pu64]),
     "ps_pauli_channel_1": (C.c_int, [_vp, _u64, _vp]),
     "ps_pauli_channel_2": (C.c_int, [_vp, _u64, _u64, _vp]),
+    "ps_circuit_compile": (C.c_int, [_vp, _vp, _u64, _vp, _u64, _vp, _pp]),
+    "ps_circuit_set_forced": (C.c_int, [_vp, _vp]),
+    "ps_circuit_run": (C.c_int, [_vp, C.c_int]),
+    "ps_circuit_get_stats": (C.c_int, [_vp, _vp]),
+    "ps_circuit_destroy": (C.c_int, [_vp]),
+    "ps_circuit_profile": (C.c_int, [_vp, C.c_int, _vp]),
+    "ps_circuit_copy_records": (C.c_int, [_vp, _vp, _vp, _pu64]),
+    "ps_circuit_measure_stats": (C.c_int, [_vp, C.c_int, _vp, _vp]),
     "ps_synchronize": (C.c_int, [_vp]),
     "ps_get_stream": (C.c_int, [_vp, _pp]),
     "ps_get_device_tableau": (C.c_int, [_vp, _pp, _pp, _pp, _pu64]),
 }
 
 _lib = None
+_exiting = False
+
+
+def _mark_exiting():
+    global _exiting
+    _exiting = True
+    if _lib is not None:
+        _lib.ps_device_synchronize()  # drain queued kernels before native teardown
+
+
+# Once the interpreter starts shutting down, finalizers no longer call into
+# the library: module teardown order is arbitrary and the process releases
+# all device memory on exit anyway.
+atexit.register(_mark_exiting)
+
+
+def exiting() -> bool:
+    return _exiting
 
 
 class PlaquetteError(RuntimeError):

@@ -1,0 +1,134 @@
+"""Compiled circuits on one ``CliffordState`` (C ABI ``ps_circuit_*``).
+
+``CompiledCircuit(circuit, state, fused=True, graph=True)`` binds a
+``circuits.Circuit`` to a state.  ``fused=False`` is the plain form (one
+kernel launch per op, the reference's CliffordCircuit::Execute structure,
+CliffordCircuit.hpp:131-135); ``fused=True`` applies every run of gates
+between measurement phases in one tableau pass.  ``graph=True`` captures the
+plan once in a CUDA graph.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+from .circuits import Circuit
+from .simulator import CliffordState, _ptr
+
+
+class CircuitOptions(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("use_graph", C.c_int32), ("seg_rows", C.c_int32),
+                ("seg_words", C.c_int32), ("seg_threads", C.c_int32)]
+
+
+class CircuitStats(C.Structure):
+    _fields_ = [("num_ops", C.c_uint64), ("num_gates", C.c_uint64), ("num_measurements", C.c_uint64),
+                ("num_channels", C.c_uint64), ("num_events", C.c_uint64), ("num_segments", C.c_uint64),
+                ("num_measure_phases", C.c_uint64), ("launches_per_run", C.c_uint64),
+                ("first_record", C.c_uint64), ("segment_bytes", C.c_double), ("seg_rows", C.c_int32),
+                ("seg_words", C.c_int32), ("seg_threads", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CompiledCircuit:
+    def __init__(self, circuit: Circuit, state: CliffordState, fused: bool = True, graph: bool = True,
+                 seg_rows: int = 0, seg_words: int = 0, seg_threads: int = 0):
+        if circuit.num_qubits != state.get_num_qubits():
+            raise ValueError("circuit and state have different qubit counts")
+        self._L = _lib.load()
+        self.state = state
+        self.circuit = circuit
+        self._ops = np.ascontiguousarray(circuit.op_array(), dtype=np.int32)
+        self._params = np.ascontiguousarray(circuit.param_array(), dtype=np.float32)
+        opts = CircuitOptions(1 if fused else 0, 1 if graph else 0, seg_rows, seg_words, seg_threads)
+        h = C.c_void_p()
+        check(self._L.ps_circuit_compile(state.handle, _ptr(self._ops), len(self._ops), _ptr(self._params),
+                                         len(self._params), C.byref(opts), C.byref(h)))
+        self._h = h
+        self.stats = self.get_stats()
+
+    def get_stats(self) -> dict:
+        st = CircuitStats()
+        check(self._L.ps_circuit_get_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    @property
+    def first_record(self) -> int:
+        return int(self.stats["first_record"])
+
+    def set_forced(self, forced_all: Optional[np.ndarray]) -> None:
+        """Forced draws: one row of ceil(batch/8) packed bytes per M / R."""
+        if forced_all is None:
+            check(self._L.ps_circuit_set_forced(self._h, None))
+            return
+        f = np.ascontiguousarray(forced_all, dtype=np.uint8)
+        nb = (self.state.get_batch_size() + 7) // 8
+        if f.shape != (self.stats["num_measurements"], nb):
+            raise ValueError(f"forced draws must have shape ({self.stats['num_measurements']}, {nb})")
+        check(self._L.ps_circuit_set_forced(self._h, _ptr(f)))
+
+    def run(self, reset: bool = False) -> None:
+        """Enqueue one run on the state's stream (asynchronous)."""
+        check(self._L.ps_circuit_run(self._h, 1 if reset else 0))
+
+    PROFILE_KINDS = ("init", "channel_sample", "segment", "measure", "gate", "channel")
+
+    def profile(self, reset: bool = True) -> dict:
+        """Device time per kernel kind of one run (CUDA events around every
+        launch; the plan is enqueued launch by launch)."""
+        class _Prof(C.Structure):
+            _fields_ = [("ms", C.c_double * 6), ("launches", C.c_uint64 * 6)]
+        p = _Prof()
+        check(self._L.ps_circuit_profile(self._h, 1 if reset else 0, C.byref(p)))
+        return {k: {"ms": p.ms[i], "launches": int(p.launches[i])} for i, k in enumerate(self.PROFILE_KINDS)}
+
+    def measure_stats(self, reset: bool = True):
+        """(random_branch, rows_multiplied) per measurement of one run, for
+        the first 64 shots."""
+        nm = int(self.stats["num_measurements"])
+        rnd = np.zeros(max(nm, 1), np.int32)
+        rows = np.zeros(max(nm, 1), np.int32)
+        check(self._L.ps_circuit_measure_stats(self._h, 1 if reset else 0, _ptr(rnd), _ptr(rows)))
+        return rnd[:nm], rows[:nm]
+
+    def measure_bytes(self, reset: bool = True) -> float:
+        """Algorithmic HBM bytes of all measurements of one run, per shot bit:
+        deterministic  n + k'*2n + (2n+1);  random  2n + 2k(2n+1) + 3(2n+1)."""
+        rnd, rows = self.measure_stats(reset)
+        n = self.state.get_num_qubits()
+        B8 = self.state.get_batch_size() / 8.0
+        det_bits = n + rows * 2 * n + (2 * n + 1)
+        rnd_bits = 2 * n + 2 * rows * (2 * n + 1) + 3 * (2 * n + 1)
+        return float(np.where(rnd > 0, rnd_bits, det_bits).sum() * B8)
+
+    def copy_records_words(self, results: Optional[np.ndarray] = None, determined: Optional[np.ndarray] = None):
+        """Copy every record of the circuit to host arrays of shape
+        [num_measurements, words] uint64 (pinned buffers give async speed)."""
+        words = C.c_uint64()
+        check(self._L.ps_circuit_copy_records(self._h, _ptr(results), _ptr(determined), C.byref(words)))
+        return words.value
+
+    def records(self):
+        """(results, determined) int32 arrays [num_measurements, batch]."""
+        self.state.synchronize()
+        first, nm = self.first_record, int(self.stats["num_measurements"])
+        res = np.empty((nm, self.state.get_batch_size()), np.int32)
+        det = np.empty_like(res)
+        for k in range(nm):
+            res[k], det[k] = self.state.record(first + k)
+        return res, det
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and not _lib.exiting():
+            try:
+                self._L.ps_circuit_destroy(h)
+            except Exception:
+                pass
+            self._h = None

@@ -78,7 +78,7 @@ class CliffordState:
 
     def __del__(self):
         h = getattr(self, "_h", None)
-        if h is not None and h.value:
+        if h is not None and h.value and not _lib.exiting():
             try:
                 self._L.ps_destroy(h)
             except Exception:

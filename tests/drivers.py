@@ -12,7 +12,7 @@ def run_ops_gpu(st, ops, params, forced_all=None, first_record=0):
     ops = np.asarray(ops, np.int32).reshape(-1, 4)
     k = 0
     for code, a, b, c in ops.tolist():
-        f = None if forced_all is None else forced_all[k]
+        f = None if forced_all is None or code not in (C.OP_M, C.OP_R) else forced_all[k]
         if code == C.OP_H:
             st.apply_hadamard_gate(a)
         elif code == C.OP_S:

@@ -1,0 +1,131 @@
+"""Compiled circuits (plain and fused forms, with and without CUDA graphs)
+against the CPU oracle, bit-for-bit, through the C ABI."""
+import numpy as np
+import pytest
+
+from drivers import random_mixed_circuit
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(st, o, first, nm):
+    gx, gz, gr = st.device_to_host_numpy()
+    ox, oz, orr = o.tableau()
+    assert np.array_equal(gx, ox), "x differs"
+    assert np.array_equal(gz, oz), "z differs"
+    assert np.array_equal(gr, orr), "r differs"
+    for k in range(nm):
+        gres, gdet = st.record(first + k)
+        ores, odet = o.record(k)
+        assert np.array_equal(gres, ores), f"record {k} results differ"
+        assert np.array_equal(gdet, odet), f"record {k} determined differ"
+
+
+def _circuits():
+    from plaquette_simulator import circuits as C
+    return {
+        "mixed_n9": (random_mixed_circuit(9, 300, seed=31), 130),
+        "mixed_n40": (random_mixed_circuit(40, 500, seed=32), 64),
+        "surface_d3_noisy": (C.surface_code_memory(3, 3, p=0.03), 300),
+        "surface_d5_noisy": (C.surface_code_memory(5, 2, p=0.01), 256),
+        "clifford_n64": (C.random_clifford(64, 400, seed=33), 128),
+    }
+
+
+@pytest.mark.parametrize("name", list(_circuits().keys()))
+@pytest.mark.parametrize("fused,graph", [(False, False), (False, True), (True, False), (True, True)])
+def test_compiled_matches_oracle(ps, O, name, fused, graph):
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ, B = _circuits()[name]
+    st = ps.CliffordState(circ.num_qubits, B, 77, True)
+    cc = CompiledCircuit(circ, st, fused=fused, graph=graph)
+    cc.run()
+    st.synchronize()
+    o = O.Oracle(circ.num_qubits, B, seed=77)
+    o.run(circ.op_array(), circ.param_array())
+    _check(st, o, cc.first_record, circ.num_measurements())
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_forced_draws(ps, O, fused):
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ, B = _circuits()["mixed_n40"]
+    nm = circ.num_measurements()
+    forced = np.random.default_rng(3).integers(0, 256, size=(nm, (B + 7) // 8), dtype=np.uint8)
+    st = ps.CliffordState(circ.num_qubits, B, 5, True)
+    cc = CompiledCircuit(circ, st, fused=fused, graph=True)
+    cc.set_forced(forced)
+    cc.run()
+    o = O.Oracle(circ.num_qubits, B, seed=5)
+    o.run(circ.op_array(), circ.param_array(), forced)
+    _check(st, o, cc.first_record, nm)
+
+
+def test_two_runs_advance_events(ps, O):
+    """A second run of the same compiled graph draws fresh events."""
+    from plaquette_simulator.circuit import CompiledCircuit
+    from plaquette_simulator import circuits as C
+    circ = C.surface_code_memory(3, 2, p=0.05)
+    B = 128
+    st = ps.CliffordState(circ.num_qubits, B, 11, True)
+    cc = CompiledCircuit(circ, st, fused=True, graph=True)
+    cc.run()
+    cc.run()
+    o = O.Oracle(circ.num_qubits, B, seed=11)
+    o.run(circ.op_array(), circ.param_array())
+    o.run(circ.op_array(), circ.param_array())
+    # the records hold the second run; the oracle's second run wrote k + nm
+    nm = circ.num_measurements()
+    st.synchronize()
+    for k in range(nm):
+        assert np.array_equal(st.record(cc.first_record + k)[0], o.record(nm + k)[0])
+    gx, gz, gr = st.device_to_host_numpy()
+    ox, oz, orr = o.tableau()
+    assert np.array_equal(gr, orr) and np.array_equal(gx, ox)
+
+
+def test_reset_run_repeats(ps, O):
+    from plaquette_simulator.circuit import CompiledCircuit
+    from plaquette_simulator import circuits as C
+    circ = C.surface_code_memory(3, 2, p=0.05)
+    B = 64
+    st = ps.CliffordState(circ.num_qubits, B, 12, True)
+    st.apply_hadamard_gate(0)
+    cc = CompiledCircuit(circ, st, fused=True, graph=True)
+    cc.run(reset=True)
+    o = O.Oracle(circ.num_qubits, B, seed=12)
+    o.run(circ.op_array(), circ.param_array())
+    _check(st, o, cc.first_record, circ.num_measurements())
+
+
+@pytest.mark.parametrize("rows,words,threads", [(1, 2, 64), (1, 4, 128), (2, 4, 256), (1, 16, 512), (2, 8, 512)])
+def test_tile_shapes(ps, O, rows, words, threads):
+    from plaquette_simulator.circuit import CompiledCircuit
+    from plaquette_simulator import circuits as C
+    circ = C.surface_code_memory(5, 2, p=0.02)
+    B = 64 * 20 + 7
+    st = ps.CliffordState(circ.num_qubits, B, 21, True)
+    cc = CompiledCircuit(circ, st, fused=True, graph=False, seg_rows=rows, seg_words=words, seg_threads=threads)
+    cc.run()
+    o = O.Oracle(circ.num_qubits, B, seed=21)
+    o.run(circ.op_array(), circ.param_array())
+    _check(st, o, cc.first_record, circ.num_measurements())
+
+
+def test_fused_on_host_loaded_tableau(ps, O):
+    """A tableau loaded from the host is not assumed valid: resets keep their
+    X inside the measurement phase, and results stay exact."""
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ = random_mixed_circuit(6, 200, seed=41)
+    B = 70
+    rng = np.random.default_rng(9)
+    W = 13
+    x = rng.integers(0, 2, size=(B, W, 6), dtype=np.int32)
+    z = rng.integers(0, 2, size=(B, W, 6), dtype=np.int32)
+    r = rng.integers(0, 2, size=(B, W), dtype=np.int32)
+    st = ps.CliffordState.from_host(x, z, r, 6, B, 3)
+    cc = CompiledCircuit(circ, st, fused=True, graph=True)
+    cc.run()
+    o = O.Oracle(6, B, seed=3, host=(x, z, r))
+    o.run(circ.op_array(), circ.param_array())
+    _check(st, o, cc.first_record, circ.num_measurements())

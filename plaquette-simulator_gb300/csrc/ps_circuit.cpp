@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <set>
 #include <string>
@@ -38,10 +39,12 @@ struct Step {
 
 struct SegHost {
     std::vector<SegLayer> layers;
+    std::vector<SegRun> runs;
     std::vector<SegGate> gates;
     std::vector<SegSign> signs;
     std::vector<int32_t> cols;
     std::vector<NoiseSlot> slots;
+    std::vector<int32_t> recsig_rec;  // record of each reset-X slot
     SegmentDev dev{};
     void *dev_block = nullptr;
 };
@@ -97,6 +100,53 @@ bool is_sign(int32_t c) { return c == OP_X || c == OP_Y || c == OP_Z; }
 bool is_meas(int32_t c) { return c == OP_M || c == OP_R; }
 bool is_channel(int32_t c) { return c == OP_PAULI1 || c == OP_PAULI2; }
 
+// Splits gates (all of one code) into groups of 8 lanes whose columns have
+// distinct residues mod 8 -- the shared-memory bank group of a 16-byte tile
+// cell -- for a and, for two-qubit gates, for b.  Each group is a matching in
+// the 8x8 residue graph (Kuhn's augmenting paths).  Returns the groups.
+std::vector<std::vector<SegGate>> bank_groups(const std::vector<SegGate> &gs, bool two) {
+    std::vector<SegGate> bucket[8][8];
+    size_t left = gs.size();
+    for (const SegGate &g : gs) bucket[g.a & 7][two ? (g.b & 7) : 0].push_back(g);
+    std::vector<std::vector<SegGate>> out;
+    while (left) {
+        std::vector<SegGate> grp;
+        if (!two) {
+            for (int ra = 0; ra < 8; ++ra)
+                if (!bucket[ra][0].empty()) {
+                    grp.push_back(bucket[ra][0].back());
+                    bucket[ra][0].pop_back();
+                }
+        } else {
+            int match_b[8];
+            for (int k = 0; k < 8; ++k) match_b[k] = -1;
+            std::function<bool(int, bool *)> try_a = [&](int a, bool *seen) -> bool {
+                for (int b = 0; b < 8; ++b)
+                    if (!bucket[a][b].empty() && !seen[b]) {
+                        seen[b] = true;
+                        if (match_b[b] < 0 || try_a(match_b[b], seen)) {
+                            match_b[b] = a;
+                            return true;
+                        }
+                    }
+                return false;
+            };
+            for (int a = 0; a < 8; ++a) {
+                bool seen[8] = {false, false, false, false, false, false, false, false};
+                try_a(a, seen);
+            }
+            for (int b = 0; b < 8; ++b)
+                if (match_b[b] >= 0) {
+                    grp.push_back(bucket[match_b[b]][b].back());
+                    bucket[match_b[b]][b].pop_back();
+                }
+        }
+        left -= grp.size();
+        out.push_back(std::move(grp));
+    }
+    return out;
+}
+
 // Builds the layered schedule of one segment.  Gates go to the first layer
 // after the last use of their qubits; sign ops (Pauli gates, channel
 // outcomes, reset X) are applied after the gates of the layer where their
@@ -127,7 +177,8 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
     auto ensure = [&](int32_t layer) { while ((int32_t)L.size() <= layer) L.emplace_back(); };
 
     for (auto &pr : pre_signs) {
-        SegSign s{SIGN_REC_X, loc[(int32_t)pr.first], pr.second, 0};
+        SegSign s{(uint16_t)loc[(int32_t)pr.first], (uint16_t)SIGN_REC_X, (int32_t)seg.recsig_rec.size()};
+        seg.recsig_rec.push_back(pr.second);
         L[0].signs.push_back(s);
     }
     for (size_t i = i0; i < i1; ++i) {
@@ -135,22 +186,22 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
         const int32_t a = loc[o.a];
         if (is_gate(o.code)) {
             int32_t layer;
-            SegGate g{o.code, a, 0, -1};
+            SegGate g{(uint16_t)a, 0, o.code};
             if (o.code == OP_CX || o.code == OP_CZ) {
                 const int32_t b = loc[o.b];
                 layer = std::max(lastof(a), lastof(b)) + 1;
-                g.b = b;
+                g.b = (uint16_t)b;
                 last[a] = last[b] = layer;
             } else {
                 layer = lastof(a) + 1;
                 last[a] = layer;
-                if (o.code == OP_H_IF || o.code == OP_S_IF) g.rec = o.c;
+                if (o.code == OP_H_IF || o.code == OP_S_IF) g.code_rec = o.code | (o.c << 4);
             }
             ensure(layer);
             L[layer].gates.push_back(g);
         } else if (is_sign(o.code)) {
             const int32_t layer = lastof(a);
-            SegSign s{o.code == OP_X ? SIGN_X : o.code == OP_Y ? SIGN_Y : SIGN_Z, a, -1, 0};
+            SegSign s{(uint16_t)a, (uint16_t)(o.code == OP_X ? SIGN_X : o.code == OP_Y ? SIGN_Y : SIGN_Z), -1};
             L[layer].signs.push_back(s);
         } else if (is_channel(o.code)) {
             NoiseSlot sl{};
@@ -169,13 +220,106 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
             L[layer].slots.push_back(sl);
         }
     }
+    // Tile positions: a permutation of the columns chosen (identity or one of
+    // a few seeded shuffles) to need the fewest conflict-free lane groups.
+    const int nq = (int)seg.cols.size();
+    const uint16_t dummy = (uint16_t)nq;  // zero column appended to every tile row
+    auto remap = [](const std::vector<SegGate> &gs, const std::vector<int> &perm) {
+        std::vector<SegGate> out(gs);
+        for (SegGate &g : out) {
+            g.a = (uint16_t)perm[g.a];
+            g.b = (uint16_t)perm[g.b];
+        }
+        return out;
+    };
+    auto groups_needed = [&](const std::vector<int> &perm) {
+        size_t total = 0;
+        for (size_t l = 0; l < L.size(); ++l)
+            for (int32_t code : {(int32_t)OP_H, (int32_t)OP_S, (int32_t)OP_CX, (int32_t)OP_CZ}) {
+                std::vector<SegGate> gs;
+                for (const SegGate &g : L[l].gates)
+                    if ((g.code_rec & 15) == code) gs.push_back(g);
+                if (!gs.empty()) total += bank_groups(remap(gs, perm), code == OP_CX || code == OP_CZ).size();
+            }
+        return total;
+    };
+    std::vector<int> best(nq);
+    for (int i = 0; i < nq; ++i) best[i] = i;
+    size_t best_cost = groups_needed(best);
+    for (uint64_t seed = 1; seed <= 12 && nq > 8; ++seed) {
+        std::vector<int> perm(nq);
+        for (int i = 0; i < nq; ++i) perm[i] = i;
+        uint64_t st = seed * 0x9E3779B97F4A7C15ull;
+        for (int i = nq - 1; i > 0; --i) {  // Fisher-Yates with SplitMix64
+            st += 0x9E3779B97F4A7C15ull;
+            uint64_t z = st;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            z ^= z >> 31;
+            std::swap(perm[i], perm[(int)(z % (uint64_t)(i + 1))]);
+        }
+        const size_t cost = groups_needed(perm);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = perm;
+        }
+    }
+    {
+        std::vector<int32_t> cols(nq);
+        for (int i = 0; i < nq; ++i) cols[best[i]] = seg.cols[i];
+        seg.cols = cols;
+    }
     for (size_t l = 0; l < L.size(); ++l) {
-        SegLayer ly;
-        ly.g0 = (int32_t)seg.gates.size();
-        seg.gates.insert(seg.gates.end(), L[l].gates.begin(), L[l].gates.end());
-        ly.g1 = (int32_t)seg.gates.size();
+        L[l].gates = remap(L[l].gates, best);
+        for (SegSign &sg : L[l].signs) sg.a = (uint16_t)best[sg.a];
+        for (NoiseSlot &sl : L[l].slots) {
+            sl.a = best[sl.a];
+            if (sl.b >= 0) sl.b = best[sl.b];
+        }
+    }
+    for (size_t l = 0; l < L.size(); ++l) {
+        SegLayer ly{};
+        ly.r0 = (int32_t)seg.runs.size();
+        for (int32_t code : {(int32_t)OP_H, (int32_t)OP_S, (int32_t)OP_CX, (int32_t)OP_CZ, (int32_t)-1}) {
+            std::vector<SegGate> gs;
+            for (const SegGate &g : L[l].gates) {
+                const int32_t gc = g.code_rec & 15;
+                const bool uniform = gc == OP_H || gc == OP_S || gc == OP_CX || gc == OP_CZ;
+                if ((code >= 0 && gc == code) || (code < 0 && !uniform)) gs.push_back(g);
+            }
+            if (gs.empty()) continue;
+            SegRun run{code, (int32_t)seg.gates.size(), 0, 0};
+            if (code < 0) {
+                seg.gates.insert(seg.gates.end(), gs.begin(), gs.end());
+            } else {
+                // A 16-byte shared-memory access is served 8 lanes at a time
+                // (8 cells x 16 B = one 128-byte bank row): each group of 8
+                // lanes gets distinct residues; short groups are padded with
+                // gates on the zero dummy column.
+                for (auto &grp : bank_groups(gs, code == OP_CX || code == OP_CZ)) {
+                    seg.gates.insert(seg.gates.end(), grp.begin(), grp.end());
+                    for (size_t k = grp.size(); k < 8; ++k) seg.gates.push_back(SegGate{dummy, dummy, code});
+                }
+            }
+            run.g1 = (int32_t)seg.gates.size();
+            seg.runs.push_back(run);
+        }
+        ly.r1 = (int32_t)seg.runs.size();
         ly.s0 = (int32_t)seg.signs.size();
-        seg.signs.insert(seg.signs.end(), L[l].signs.begin(), L[l].signs.end());
+        {
+            // interleave residues so 8 consecutive sign ops read distinct bank groups
+            std::vector<SegSign> byres[8];
+            for (const SegSign &sg : L[l].signs) byres[sg.a & 7].push_back(sg);
+            for (bool more = true; more;) {
+                more = false;
+                for (int r8 = 0; r8 < 8; ++r8)
+                    if (!byres[r8].empty()) {
+                        seg.signs.push_back(byres[r8].back());
+                        byres[r8].pop_back();
+                        more = true;
+                    }
+            }
+        }
         ly.s1 = (int32_t)seg.signs.size();
         seg.layers.push_back(ly);
         seg.slots.insert(seg.slots.end(), L[l].slots.begin(), L[l].slots.end());
@@ -194,7 +338,7 @@ void pick_tile(ps_circuit *c, int nq_max) {
         o.seg_words = bw;
     }
     if (o.seg_rows <= 0) o.seg_rows = 1;
-    if (o.seg_threads <= 0) o.seg_threads = std::min(512, std::max(64, 32 * o.seg_rows * o.seg_words));
+    if (o.seg_threads <= 0) o.seg_threads = std::min(256, std::max(64, 32 * o.seg_rows * o.seg_words));
 }
 
 // Optional per-launch timing: an event pair around every launch, by kind.
@@ -446,19 +590,29 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         for (SegHost &sg : c->segs) {
             SegmentDev d{};
             SegLayer *dl;
+            SegRun *drn;
             SegGate *dg;
             SegSign *ds;
             int32_t *dc;
             NoiseSlot *dsl;
-            if (upload(c->owned, sg.layers, &dl) || upload(c->owned, sg.gates, &dg) || upload(c->owned, sg.signs, &ds) ||
-                upload(c->owned, sg.cols, &dc) || upload(c->owned, sg.slots, &dsl))
+            int32_t *drr;
+            if (upload(c->owned, sg.layers, &dl) || upload(c->owned, sg.runs, &drn) || upload(c->owned, sg.gates, &dg) ||
+                upload(c->owned, sg.signs, &ds) ||
+                upload(c->owned, sg.cols, &dc) || upload(c->owned, sg.slots, &dsl) ||
+                upload(c->owned, sg.recsig_rec, &drr))
                 return bail(E_CUDA);
+            d.recsig_rec = drr;
+            d.nrecsig = (int32_t)sg.recsig_rec.size();
             d.layers = dl;
             d.nlayers = (int32_t)sg.layers.size();
+            d.runs = drn;
+            d.nruns = (int32_t)sg.runs.size();
             d.gates = dg;
             d.signs = ds;
             d.cols = dc;
             d.nq = (int32_t)sg.cols.size();
+            d.ngates = (int32_t)sg.gates.size();
+            d.nsigns = (int32_t)sg.signs.size();
             d.slots = dsl;
             d.nslots = (int32_t)sg.slots.size();
             d.thr = c->d_thr;

@@ -11,14 +11,14 @@ struct RunParams {
     uint64_t event_base;
 };
 
-// A gate inside a fused segment.  a / b are LOCAL column indices (positions
-// in the segment's touched-qubit list); rec indexes the record table for the
-// per-shot conditional gates.
+// A gate inside a fused segment (8 bytes).  a / b are LOCAL column indices
+// (positions in the segment's touched-qubit list); code_rec holds the op code
+// in its low 4 bits and, for the per-shot conditional gates, the record index
+// above them.
 struct SegGate {
-    int32_t code;
-    int32_t a;
-    int32_t b;
-    int32_t rec;
+    uint16_t a;
+    uint16_t b;
+    int32_t code_rec;
 };
 
 // A sign operation r ^= (fx & z_a) ^ (fz & x_a): the Pauli gates (constant
@@ -26,16 +26,23 @@ struct SegGate {
 // (mask = record outcome).
 enum SignKind : int32_t { SIGN_X = 0, SIGN_Y = 1, SIGN_Z = 2, SIGN_REC_X = 3 };
 struct SegSign {
-    int32_t kind;
-    int32_t a;
+    uint16_t a;
+    uint16_t kind;
     int32_t rec;
-    int32_t pad;
 };
 
-// Layer L: gates [g0, g1) act on disjoint columns; afterwards sign ops
-// [s0, s1) and the noise entries tagged with layer L.
+// Layer L: gate runs [r0, r1) (all of its gates act on disjoint columns);
+// afterwards sign ops [s0, s1) and the noise entries tagged with layer L.
 struct SegLayer {
-    int32_t g0, g1, s0, s1;
+    int32_t r0, r1, s0, s1;
+};
+
+// A run of gates [g0, g1) of one code.  For H, S, CX and CZ the run is laid
+// out in batches of 32 (one per warp instruction) whose columns fall evenly on
+// the shared-memory banks, padded with gates on a zero dummy column; code -1
+// marks a run of mixed / conditional gates.
+struct SegRun {
+    int32_t code, g0, g1, pad;
 };
 
 // One Pauli channel of a segment.  thr_off indexes the threshold table
@@ -49,20 +56,31 @@ struct NoiseSlot {
     uint32_t event;
 };
 
-// Sampled channel outcome for one 64-shot word: X/Z components on a and b.
+// Sampled channel outcome for one 64-shot word: X/Z components on local
+// columns a and b (b = 0xFFFF for a one-qubit channel), applied after the
+// gates of `layer`.
 struct NoiseEntry {
     u64 fxa, fza, fxb, fzb;
-    int32_t slot;
     int32_t layer;
+    uint16_t a;
+    uint16_t b;
 };
 
 struct SegmentDev {
     const SegLayer *layers;
     int32_t nlayers;
+    const SegRun *runs;
+    int32_t nruns;
     const SegGate *gates;
     const SegSign *signs;
     const int32_t *cols;     // touched global qubits, nq entries
     int32_t nq;
+    int32_t ngates;
+    int32_t nsigns;
+    // Reset-X sign ops carry a slot number (SegSign.rec); the record behind
+    // slot i is recsig_rec[i].  Their outcome words are staged per tile.
+    const int32_t *recsig_rec;
+    int32_t nrecsig;
     const NoiseSlot *slots;
     int32_t nslots;
     const uint64_t *thr;     // threshold table

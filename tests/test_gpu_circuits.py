@@ -98,7 +98,7 @@ def test_reset_run_repeats(ps, O):
     _check(st, o, cc.first_record, circ.num_measurements())
 
 
-@pytest.mark.parametrize("rows,words,threads", [(1, 2, 64), (1, 4, 128), (2, 4, 256), (1, 16, 512), (2, 8, 512)])
+@pytest.mark.parametrize("rows,words,threads", [(1, 2, 64), (1, 4, 128), (2, 4, 256), (1, 16, 256), (2, 8, 256), (4, 2, 128)])
 def test_tile_shapes(ps, O, rows, words, threads):
     from plaquette_simulator.circuit import CompiledCircuit
     from plaquette_simulator import circuits as C

@@ -146,6 +146,18 @@ ps_status ps_pauli_channel_1(ps_state *h, uint64_t q, const float p[3]);
  * YI YX YY YZ ZI ZX ZY ZZ.  Mirrors E_PAULI2 (CliffordCircuit.hpp:50-55). */
 ps_status ps_pauli_channel_2(ps_state *h, uint64_t a, uint64_t b, const float p[15]);
 
+/* Same channel and random draws as ps_pauli_channel_1, for callers that must
+ * not allocate device memory during the call (a host that has already handed
+ * the whole device to its own memory pool, a process under a strict memory
+ * budget, or code that must not risk the device-wide synchronisation an
+ * allocation can cause).  It has no counterpart in the reference.  Its scratch
+ * is a fixed 258 KiB array inside the library: at most 524,288 shots (8,192
+ * shot-words) per state, larger states get PS_E_ARG.  The first call on a
+ * device looks up that array's address and must not be made while a stream is
+ * being captured; calls on different streams that overlap on the GPU share
+ * the array and race. */
+ps_status ps_pauli_channel_1_noalloc(ps_state *h, uint64_t q, const float p[3]);
+
 /* ------------------------------------------------------------- circuits */
 /* A circuit is an op table (see the PS_OP_* codes) plus a float parameter
  * table.  It replaces the reference's CliffordCircuit driver

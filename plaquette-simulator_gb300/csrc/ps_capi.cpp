@@ -413,6 +413,16 @@ ps_status ps_pauli_channel_1(ps_state *h, uint64_t q, const float p[3]) {
     return launch_pauli_channel(h, (int64_t)q, 0, thr, 3);
 }
 
+ps_status ps_pauli_channel_1_noalloc(ps_state *h, uint64_t q, const float p[3]) {
+    ENTER();
+    CHECK_HANDLE(h);
+    CHECK_QUBIT(h, q);
+    if (!p) return fail(E_ARG, "null probabilities");
+    uint64_t thr[3];
+    channel_thresholds(p, 3, thr);
+    return launch_pauli_channel_noalloc(h, (int64_t)q, thr);
+}
+
 ps_status ps_pauli_channel_2(ps_state *h, uint64_t a, uint64_t b, const float p[15]) {
     ENTER();
     CHECK_HANDLE(h);

@@ -4,6 +4,8 @@
 // parallel_for launches (CliffordState.hpp:348-531) and the baseline the
 // fused circuit form is measured against.
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "ps_internal.h"
 #include "ps_segment.cuh"
@@ -243,6 +245,86 @@ int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thr,
     }
     PS_CUDA(cudaGetLastError());
     PS_CUDA(cudaFreeAsync(dthr, h->stream));
+    return OK;
+}
+
+}  // namespace ps
+
+// ---------------------------------------------------------------------------
+// Pauli channel without device allocation.
+//
+// Some callers cannot allocate device memory while they run: a host that
+// reserved the whole device for its own pool before starting, code that runs
+// under a memory-budget sandbox, or a caller that must not synchronise the
+// device (cudaMalloc / cudaFree can).  ps_pauli_channel_1 asks the stream
+// allocator for its threshold table on every call; this variant keeps that
+// table and the per-word outcome masks in one fixed array linked into the
+// library instead; the thresholds reach it as kernel arguments.
+//
+// Limit: at most NOALLOC_MAX_WORDS shot-words per state (524,288 shots).  The
+// array is a module-scope __device__ variable, so every GPU that loads the
+// library holds it (258 KiB) until the process exits.  All calls share it and
+// it keeps the last call's contents: every word a call reads is written by
+// that same call first (thresholds, then all 4*w mask words), so nothing has
+// to be cleared.  Calls whose work overlaps on the GPU (different streams)
+// race on the array; calls on one stream are ordered.
+namespace ps {
+
+namespace {
+constexpr int64_t NOALLOC_MAX_WORDS = 8192;
+constexpr int NOALLOC_THR = 16;  // threshold slots in front of the masks
+
+static __device__ __align__(256) u64 g_noalloc_scratch[NOALLOC_THR + 4 * NOALLOC_MAX_WORDS];
+
+__global__ void noalloc_set_thresholds(uint64_t *thr, uint64_t t0, uint64_t t1, uint64_t t2) {
+    thr[0] = t0;
+    thr[1] = t1;
+    thr[2] = t2;
+}
+
+// Device address of the array, looked up once per device on the first call
+// made with that device current (so that first call should not happen during
+// stream capture).
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {nullptr};
+
+int noalloc_scratch(int dev, u64 **out) {
+    if (dev < 0 || dev >= 64) return fail(E_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<u64 *>(g_noalloc_ptr[dev]);
+    return OK;
+}
+}  // namespace
+
+int launch_pauli_channel_noalloc(ps_state *h, int64_t q, const uint64_t *thr3) {
+    if (h->w > NOALLOC_MAX_WORDS)
+        return fail(E_ARG, "batch_size " + std::to_string(h->S) + " exceeds the allocation-free limit of " +
+                               std::to_string(NOALLOC_MAX_WORDS * 64) + " shots");
+    int dev = 0;
+    PS_CUDA(cudaGetDevice(&dev));
+    if (dev != h->device) return fail(E_STATE, "the handle belongs to another device than the current one");
+    u64 *scratch = nullptr;
+    int rc = noalloc_scratch(dev, &scratch);
+    if (rc != OK) return rc;
+    uint64_t *thr = reinterpret_cast<uint64_t *>(scratch);
+    u64 *masks = scratch + NOALLOC_THR;
+    const uint64_t event = h->events++;
+    // Thresholds travel as kernel arguments (no host copy, no allocation).
+    noalloc_set_thresholds<<<1, 1, 0, h->stream>>>(thr, thr3[0], thr3[1], thr3[2]);
+    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, h->stream>>>(masks, h->w, (uint64_t)h->seed, event,
+                                                                        nullptr, 3, thr);
+    PS_CUDA(cudaGetLastError());
+    const int64_t work = h->W * (h->w >> 1);
+    if (h->n > 0 && work > 0)
+        sign_flip_kernel<<<blocks_for(work), 256, 0, h->stream>>>(h->X, h->Z, h->R, h->n, h->W, h->w, q, masks,
+                                                                  masks + h->w);
+    PS_CUDA(cudaGetLastError());
     return OK;
 }
 

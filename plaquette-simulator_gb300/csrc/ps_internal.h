@@ -122,3 +122,8 @@ int launch_channel_rp(cudaStream_t stream, ps_state *h, int64_t a, int64_t b, co
                       uint32_t event_off, const RunParams *rp, u64 *dev_masks);
 int launch_gate_on(cudaStream_t stream, ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag);
 } // namespace ps
+
+namespace ps {
+// ps_gates.cu: Pauli channel on q whose scratch lives in a fixed device array.
+int launch_pauli_channel_noalloc(ps_state *h, int64_t q, const uint64_t *thr3);
+}  // namespace ps

@@ -57,6 +57,7 @@ _SIGS = {
     "ps_reset_qubit": (C.c_int, [_vp, _u64, _vp, _pu64]),
     "ps_pauli_channel_1": (C.c_int, [_vp, _u64, _vp]),
     "ps_pauli_channel_2": (C.c_int, [_vp, _u64, _u64, _vp]),
+    "ps_pauli_channel_1_noalloc": (C.c_int, [_vp, _u64, _vp]),
     "ps_circuit_compile": (C.c_int, [_vp, _vp, _u64, _vp, _u64, _vp, _pp]),
     "ps_circuit_set_forced": (C.c_int, [_vp, _vp]),
     "ps_circuit_run": (C.c_int, [_vp, C.c_int]),

@@ -33,6 +33,8 @@ WORKLOADS = {
     # name: (distance, rounds, p, shots)
     "surface_d15": (15, 15, 1e-3, 16384),
     "surface_d5": (5, 5, 1e-3, 4096),
+    # small case for profiler captures: 206 MB tableau, still larger than L2
+    "surface_d15_s2048": (15, 15, 1e-3, 2048),
 }
 
 
@@ -46,6 +48,13 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--cpu-shots", type=int, default=0, help="shots of the CPU sample (0 = auto)")
+    ap.add_argument("--batch-jobs", type=int, default=64,
+                    help="uneven surface-code jobs in the one-launch batch leg (0 = skip)")
+    ap.add_argument("--serve-seconds", type=float, default=1.0,
+                    help="seconds of Poisson arrivals in the serving leg (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="serving leg: arrivals per second")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="serving leg: HBM admission budget")
+    ap.add_argument("--serve-drain-s", type=float, default=180.0, help="serving leg: longest wait for the backlog")
     return ap.parse_args()
 
 
@@ -172,6 +181,102 @@ def run_reference(args):
                 "to the GPU box (no reference checkout there)",
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------- batch and serving
+def batch_leg(args, rank, torch):
+    """64 uneven surface-code jobs (d in 3..21, d rounds, shots log-uniform in
+    [256, 65536], p in {1e-4, 1e-3, 5e-3}) in ONE graph launch per run, tiles
+    chosen by the autotuner; beside it the same compiled jobs run one after
+    another."""
+    from plaquette_simulator.batch import Batch, uneven_surface_jobs
+    from plaquette_simulator.circuit import CompiledCircuit
+    jobs = uneven_surface_jobs(args.batch_jobs, seed=12345 + 7919 * rank)
+    t0 = time.perf_counter()
+    b = Batch(jobs, autotune=True, graph=True)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(b.stream)
+    b.run()
+    b.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = max(1, min(3, args.steps))
+    e0.record(stream)
+    for _ in range(k):
+        b.run()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    sg = b.stats["shot_gates_per_run"]
+    # the same jobs, one after another (each enqueued launch by launch)
+    seq = []
+    for j in range(len(jobs)):
+        c, _ = b._job(j)
+        seq.append(CompiledCircuit._borrowed(c.value, jobs[j].circuit, None))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for cc in seq:
+        cc.run(reset=True)
+        b._L.ps_device_synchronize()
+    seq_ms = (time.perf_counter() - t1) * 1e3
+    shapes = sorted({(jobs[j].distance, *b.job_options(j).values()) for j in range(len(jobs))})
+    out = {"workload": f"{len(jobs)} uneven rotated surface-code memory jobs, d uniform in 3..21 (d rounds), "
+                       "shots log-uniform in [256, 65536], p in {1e-4, 1e-3, 5e-3}, one CUDA graph launch",
+           "value": sg / (ms / 1e3), "unit": "shot-gates/s", "ms_per_run": ms, "runs": k,
+           "shot_gates_per_run": sg, "tableau_gb": b.stats["tableau_bytes"] / 1e9,
+           "launches_per_run": b.stats["launches_per_run"], "setup_s": setup_s,
+           "compile_ms": b.stats["compile_ms"], "tune_ms": b.stats["tune_ms"],
+           "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / ms,
+           "tiles": [{"d": s[0], "seg_rows": s[1], "seg_words": s[2], "seg_threads": s[3], "meas_words": s[4]}
+                     for s in shapes]}
+    del seq
+    b.close()
+    return out
+
+
+def serving_leg(args, rank):
+    """Poisson arrivals of sampling jobs (sizes as the batch leg plus d=25),
+    admitted by tableau bytes against an HBM budget; p50/p99 latency."""
+    from plaquette_simulator.batch import Server, poisson_arrivals, uneven_surface_jobs
+    arrivals = poisson_arrivals(args.serve_rate, args.serve_seconds, seed=12345 + rank)
+    jobs = uneven_surface_jobs(len(arrivals), seed=24680 + rank, distances=tuple(range(3, 22, 2)) + (25,),
+                               job_seed_base=100000)
+    offered = sum(j.shot_gates() for j in jobs)
+    with Server(hbm_budget_bytes=int(args.serve_budget_gb * 1e9), max_active=16, autotune=False) as srv:
+        t0 = srv.now()
+        ids = []
+        for t, j in zip(arrivals, jobs):
+            dt = t0 + t - srv.now()
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(j))
+        submit_end = srv.now() - t0
+        drained = True
+        try:
+            srv.drain(args.serve_drain_s)
+        except Exception:
+            drained = False
+        errors = {}
+        if drained:
+            for i, j in zip(ids, jobs):
+                try:
+                    srv.wait(i, 0.0)
+                except Exception as e:  # a failed job: keep one message per kind
+                    errors.setdefault(str(e).split("Error in Plaquette:")[-1].strip()[:160], []).append(
+                        {"d": j.distance, "shots": j.shots})
+        st = srv.stats()
+    span = max(1e-9, st["last_done_s"] - st["first_submit_s"])
+    return {"workload": f"Poisson arrivals at {args.serve_rate:g} jobs/s for {args.serve_seconds:g} s, "
+                        "rotated surface-code memory jobs d in {3..21, 25} (d rounds), shots log-uniform in "
+                        f"[256, 65536], admission by device bytes against {args.serve_budget_gb:g} GB",
+            "jobs": len(ids), "completed": st["completed"], "failed": st["failed"], "drained": drained,
+            "p50_latency_s": st["p50_latency_s"], "p99_latency_s": st["p99_latency_s"],
+            "mean_latency_s": st["mean_latency_s"], "max_latency_s": st["max_latency_s"],
+            "value": st["shot_gates_completed"] / span, "unit": "shot-gates/s",
+            "offered_shot_gates_per_s": offered / args.serve_seconds,
+            "offered_jobs_per_s": len(ids) / args.serve_seconds,
+            "achieved_jobs_per_s": st["completed"] / span, "submit_span_s": submit_end,
+            "pool_peak_gb": st["pool_peak_bytes"] / 1e9, "max_active": 16,
+            "errors": {k: v[:4] for k, v in errors.items()}}
 
 
 # ---------------------------------------------------------------- ours
@@ -322,6 +427,15 @@ def main():
                          "form": "one kernel launch per op, captured in a CUDA graph"}
         line["speedup_vs_plain"] = pms / ms
         del plain
+
+    del fused, st
+    torch.cuda.synchronize()
+    if args.batch_jobs > 0:
+        line["batch"] = batch_leg(args, rank, torch)
+    if args.serve_seconds > 0:
+        line["serving"] = serving_leg(args, rank)
+        line["p50_latency_s"] = line["serving"]["p50_latency_s"]
+        line["p99_latency_s"] = line["serving"]["p99_latency_s"]
 
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(circ, seed, args.cpu_shots)

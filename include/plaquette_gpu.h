@@ -196,6 +196,7 @@ typedef struct {
     int32_t seg_rows;    /* fused tile: tableau rows per CTA (0 = auto)          */
     int32_t seg_words;   /* fused tile: 64-shot words per CTA (0 = auto)         */
     int32_t seg_threads; /* fused tile: threads per CTA (0 = auto)               */
+    int32_t meas_words;  /* measurement kernel: shot-words per CTA, 1 or 2 (0 = auto) */
 } ps_circuit_options;
 
 typedef struct {
@@ -203,7 +204,7 @@ typedef struct {
     uint64_t num_segments, num_measure_phases, launches_per_run;
     uint64_t first_record;          /* state record id of the first M/R      */
     double segment_bytes;           /* algorithmic HBM bytes of all segments  */
-    int32_t seg_rows, seg_words, seg_threads;
+    int32_t seg_rows, seg_words, seg_threads, meas_words;
 } ps_circuit_stats;
 
 typedef struct ps_circuit ps_circuit;
@@ -242,6 +243,122 @@ ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *rand
  * host memory: num_measurements rows of `words` uint64 each (bit s of word
  * k = shot 64k+s).  Either pointer may be NULL.  Waits for the stream. */
 ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *determined, uint64_t *words);
+
+/* The project's autotuner (no counterpart in the reference): times the
+ * fused-segment tile shapes (rows x shot-words x threads) on the circuit's
+ * first segment and the measurement kernel's shot-words per CTA on its first
+ * measurement phase, on the circuit's own state, and keeps the fastest
+ * (re-capturing the CUDA graphs).  The tableau and records are left holding
+ * valid but meaningless data (runs with reset_state = 1 start over); the
+ * event counter is not advanced.  Results are cached per process by
+ * (qubits, shot-words, touched qubits), so circuits of one shape are timed
+ * once.  *chosen and *tune_ms may be NULL.  Plain circuits are left as they
+ * are. */
+ps_status ps_circuit_autotune(ps_circuit *c, ps_circuit_options *chosen, double *tune_ms);
+
+/* ------------------------------------------------------ batches of jobs */
+/* Many sampling jobs of uneven qubit and shot counts (the reference runs one
+ * CliffordState at a time; this has no counterpart there).  Each job is a
+ * circuit on its own state, compiled in the fused form; one batch run is ONE
+ * CUDA graph launch holding every job as an independent branch, so the
+ * device overlaps the jobs' kernels (the small jobs' launches fill the tails
+ * of the big ones).  Every job starts from |0...0> and draws from its own
+ * seed, exactly as it would alone. */
+typedef struct {
+    const ps_op *ops;
+    uint64_t nops;
+    const float *params;
+    uint64_t nparams;
+    uint64_t num_qubits;
+    uint64_t shots;
+    int64_t seed;
+} ps_job_desc;
+
+typedef struct {
+    int32_t autotune;   /* ps_circuit_autotune every job shape first          */
+    int32_t use_graph;  /* one graph for the whole batch (else stream order)  */
+} ps_batch_options;
+
+typedef struct {
+    uint64_t num_jobs;
+    uint64_t shot_gates_per_run;  /* sum over jobs of gates x shots          */
+    uint64_t tableau_bytes;       /* device bytes of all job tableaux        */
+    uint64_t launches_per_run;    /* kernels in one batch run                 */
+    double compile_ms, tune_ms;
+} ps_batch_stats;
+
+typedef struct ps_batch ps_batch;
+ps_status ps_batch_create(const ps_job_desc *jobs, uint64_t njobs, const ps_batch_options *opts, ps_batch **out);
+/* Enqueues one run of every job (returns without waiting). */
+ps_status ps_batch_run(ps_batch *b);
+ps_status ps_batch_synchronize(ps_batch *b);
+/* The stream batch runs are launched on (as void*). */
+ps_status ps_batch_get_stream(const ps_batch *b, void **stream);
+/* Job j's compiled circuit and state (owned by the batch).  Read records
+ * with ps_circuit_copy_records after ps_batch_synchronize. */
+ps_status ps_batch_job(const ps_batch *b, uint64_t j, ps_circuit **circuit, ps_state **state);
+ps_status ps_batch_get_stats(const ps_batch *b, ps_batch_stats *out);
+ps_status ps_batch_destroy(ps_batch *b);
+
+/* ------------------------------------------------------------- serving */
+/* A request loop for sampling jobs (no counterpart in the reference).
+ * Submitted jobs queue on the host; worker threads admit them while the sum
+ * of admitted jobs' device bytes fits the HBM budget and fewer than
+ * max_active run, so jobs that arrive while others are on the GPU start as
+ * soon as memory and a slot free up, and their kernels overlap on the device
+ * (one stream per active job).  The budget is reserved once at creation as
+ * one device region; job tableaux, records and scratch come from it and go
+ * back to it without device-wide synchronisation.  A job's measurement
+ * records are copied to host memory when it finishes and stay there until
+ * ps_server_release.  Results are the same as the job run alone: every job
+ * starts from |0...0> and draws from its own seed. */
+typedef struct {
+    uint64_t hbm_budget_bytes;  /* device region for all admitted jobs        */
+    int32_t max_active;         /* jobs on the device at once (0 = 16)        */
+    int32_t autotune;           /* tune each new job shape on its first job   */
+    double hol_wait_s;          /* a queued job that waited this long stops
+                                   smaller later jobs from overtaking it      */
+} ps_server_options;
+
+typedef struct {
+    int32_t status;             /* PS_OK, or the job's error code            */
+    int32_t pad;
+    uint64_t num_measurements;
+    uint64_t words;             /* uint64 words per record row                */
+    uint64_t shot_gates;
+    uint64_t device_bytes;      /* bytes the job held while admitted          */
+    double submit_s, admit_s, done_s;  /* server clock (seconds since create) */
+    double latency_s;           /* done_s - submit_s                          */
+} ps_job_result;
+
+typedef struct {
+    uint64_t submitted, completed, failed, queued, active;
+    uint64_t shot_gates_completed;
+    uint64_t pool_bytes, pool_peak_bytes;
+    double p50_latency_s, p99_latency_s, mean_latency_s, max_latency_s;
+    double first_submit_s, last_done_s;
+} ps_server_stats;
+
+typedef struct ps_server ps_server;
+ps_status ps_server_create(const ps_server_options *opts, ps_server **out);
+/* Copies the job description and queues it; never blocks on the device.
+ * A job larger than the whole budget is refused with PS_E_NOMEM. */
+ps_status ps_server_submit(ps_server *s, const ps_job_desc *job, uint64_t *job_id);
+/* Waits up to timeout_s (< 0: no limit) for the job; PS_E_TIMEOUT if it is
+ * not done by then. */
+ps_status ps_server_wait(ps_server *s, uint64_t job_id, double timeout_s, ps_job_result *out);
+/* The finished job's records: num_measurements rows of `words` uint64. */
+ps_status ps_server_copy_records(ps_server *s, uint64_t job_id, uint64_t *results, uint64_t *determined);
+/* Drops the finished job's host records. */
+ps_status ps_server_release(ps_server *s, uint64_t job_id);
+/* Waits until no job is queued or active (timeout_s < 0: no limit). */
+ps_status ps_server_drain(ps_server *s, double timeout_s);
+/* Latency percentiles over every job completed so far. */
+ps_status ps_server_get_stats(ps_server *s, ps_server_stats *out);
+/* Seconds on the server clock. */
+ps_status ps_server_now(const ps_server *s, double *seconds);
+/* Waits for active jobs, drops queued ones, frees the budget region. */
+ps_status ps_server_destroy(ps_server *s);
 
 /* ------------------------------------------------------------ streaming */
 /* Block until all work queued on the handle's stream is done. */

@@ -1,0 +1,705 @@
+// ps_batch.cpp -- many sampling jobs at once: batches (one CUDA graph launch
+// whose branches are the jobs) and the serving loop (continuous admission of
+// jobs against an HBM budget, one stream per active job).  Neither has a
+// counterpart in the reference, which runs one CliffordState at a time
+// (CliffordState.hpp:97-139); every job here is a compiled circuit on its own
+// state and gives the same records as when it runs alone.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <numeric>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/plaquette_gpu.h"
+#include "ps_internal.h"
+#include "ps_segment.cuh"
+
+#define TRY(expr)                     \
+    do {                              \
+        const int _rc = (expr);       \
+        if (_rc != ps::OK) return _rc; \
+    } while (0)
+
+namespace ps {
+
+// ------------------------------------------------------------ DevPool
+void DevPool::reset(void *region, size_t bytes) {
+    std::lock_guard<std::mutex> lk(mu);
+    base = static_cast<char *>(region);
+    cap = bytes;
+    used = peak = 0;
+    free_.clear();
+    taken.clear();
+    if (bytes) free_[0] = bytes;
+}
+
+bool DevPool::alloc(void **p, size_t bytes) {
+    bytes = (bytes + 255) & ~size_t(255);
+    std::lock_guard<std::mutex> lk(mu);
+    auto best = free_.end();
+    for (auto it = free_.begin(); it != free_.end(); ++it)
+        if (it->second >= bytes && (best == free_.end() || it->second < best->second)) best = it;
+    if (best == free_.end()) return false;
+    const size_t off = best->first, sz = best->second;
+    free_.erase(best);
+    if (sz > bytes) free_[off + bytes] = sz - bytes;
+    taken[off] = bytes;
+    used += bytes;
+    peak = std::max(peak, used);
+    *p = base + off;
+    return true;
+}
+
+void DevPool::release(void *p) {
+    std::lock_guard<std::mutex> lk(mu);
+    const size_t off = (size_t)(static_cast<char *>(p) - base);
+    auto t = taken.find(off);
+    if (t == taken.end()) return;
+    size_t start = off, sz = t->second;
+    taken.erase(t);
+    used -= sz;
+    auto nx = free_.lower_bound(off);
+    if (nx != free_.end() && off + sz == nx->first) {
+        sz += nx->second;
+        nx = free_.erase(nx);
+    }
+    if (nx != free_.begin()) {
+        auto pv = std::prev(nx);
+        if (pv->first + pv->second == off) {
+            pv->second += sz;
+            return;
+        }
+    }
+    free_[start] = sz;
+}
+
+namespace {
+
+// Writes each job's run parameters (seed, event base) into its circuit's
+// device slot: the root node of a batch graph.
+__global__ void batch_params_kernel(RunParams *const *__restrict__ dst, const RunParams *__restrict__ src, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) *dst[i] = src[i];
+}
+
+bool is_meas_code(int32_t c) { return c == OP_M || c == OP_R; }
+bool is_channel_code(int32_t c) { return c == OP_PAULI1 || c == OP_PAULI2; }
+
+uint64_t count_gates(const ps_op *ops, uint64_t nops) {
+    uint64_t g = 0;
+    for (uint64_t i = 0; i < nops; ++i) g += ops[i].code <= OP_R ? 1 : 0;
+    return g;
+}
+
+// Upper bound of the device bytes a fused job takes: tableau, records, the
+// channel-outcome scratch of its largest segment, schedule tables.
+size_t job_device_bytes(const ps_job_desc &j) {
+    int64_t w = ((int64_t)j.shots + 63) / 64;
+    w = (w + 1) & ~int64_t(1);
+    if (w == 0) w = 2;
+    size_t nm = 0, nch = 0, seg_ch = 0, max_ch = 0;
+    for (uint64_t i = 0; i < j.nops; ++i) {
+        const int32_t c = j.ops[i].code;
+        if (is_meas_code(c)) {
+            ++nm;
+            seg_ch = 0;
+        } else if (is_channel_code(c)) {
+            ++nch;
+            max_ch = std::max(max_ch, ++seg_ch);
+        }
+    }
+    const size_t W = (size_t)w;
+    size_t b = state_bytes((int64_t)j.num_qubits, (int64_t)j.shots);
+    b += 2 * nm * W * 8;                                             // records
+    b += std::max<size_t>(1, max_ch) * W * (sizeof(NoiseEntry) + 32) + W * 4;  // outcome scratch
+    b += 4 * W * 8 + 64;                                             // masks, params
+    b += (size_t)j.nops * 128 + nch * 15 * 8 + nm * sizeof(MeasOp);  // schedules
+    b += 64 * 256 + (1u << 20);                                      // granules, slack
+    return b;
+}
+
+int check_job(const ps_job_desc &j, uint64_t index) {
+    if (!j.ops && j.nops) return fail(E_ARG, "job " + std::to_string(index) + ": null op table");
+    if (j.num_qubits == 0 || j.shots == 0) return fail(E_ARG, "job " + std::to_string(index) + ": empty job");
+    if (j.num_qubits > 2048) return fail(E_ARG, "job " + std::to_string(index) + ": more than 2048 qubits");
+    return OK;
+}
+
+double seconds_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+}  // namespace ps
+
+using namespace ps;
+
+// ================================================================ batches
+struct ps_batch {
+    ps_batch_options opts{};
+    ps_batch_stats stats{};
+    int device = 0;
+    std::vector<ps_state *> states;
+    std::vector<ps_circuit *> circs;
+    std::vector<size_t> order;  // launch order: most shot-gates first
+    cudaStream_t stream = nullptr;
+    std::vector<cudaStream_t> branches;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+    static constexpr int RING = 4;
+    RunParams *h_vals[RING] = {};
+    cudaEvent_t copied[RING] = {};
+    int ring_pos = 0;
+    RunParams *d_vals = nullptr;
+    RunParams **d_dst = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace ps {
+namespace {
+
+// Root scatter node, then every job on its own branch, joined back.
+int enqueue_batch(ps_batch *b) {
+    const int nj = (int)b->circs.size();
+    batch_params_kernel<<<1, 256, 0, b->stream>>>(b->d_dst, b->d_vals, nj);
+    PS_CUDA(cudaGetLastError());
+    PS_CUDA(cudaEventRecord(b->fork, b->stream));
+    for (size_t k = 0; k < b->order.size(); ++k) {
+        const size_t j = b->order[k];
+        PS_CUDA(cudaStreamWaitEvent(b->branches[k], b->fork, 0));
+        TRY(circuit_enqueue(b->circs[j], b->branches[k], true));
+        PS_CUDA(cudaEventRecord(b->joins[k], b->branches[k]));
+        PS_CUDA(cudaStreamWaitEvent(b->stream, b->joins[k], 0));
+    }
+    return OK;
+}
+
+}  // namespace
+}  // namespace ps
+
+extern "C" {
+
+ps_status ps_batch_destroy(ps_batch *b);
+
+ps_status ps_batch_create(const ps_job_desc *jobs, uint64_t njobs, const ps_batch_options *opts, ps_batch **out) {
+    ps_enter(__func__, __LINE__);
+    if (!out || (!jobs && njobs)) return fail(E_ARG, "null argument");
+    *out = nullptr;
+    if (njobs == 0) return fail(E_ARG, "empty batch");
+    for (uint64_t j = 0; j < njobs; ++j) TRY(check_job(jobs[j], j));
+    auto *b = new ps_batch;
+    if (opts) b->opts = *opts;
+    auto bail = [&](int rc) {
+        const std::string msg = ps_last_error();
+        ps_batch_destroy(b);
+        set_error(msg);  // keep the failing call's message
+        return rc;
+    };
+    PS_CUDA(cudaGetDevice(&b->device));
+    const auto t0 = std::chrono::steady_clock::now();
+    b->states.assign(njobs, nullptr);
+    b->circs.assign(njobs, nullptr);
+    // Jobs compile in parallel on the host (schedules, bank-group search).
+    std::vector<int> rcs(njobs, OK);
+    std::vector<std::string> errs(njobs);
+    {
+        std::atomic<uint64_t> next{0};
+        const unsigned nt = std::max(1u, std::min<unsigned>(16, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (unsigned t = 0; t < std::min<uint64_t>(nt, njobs); ++t)
+            pool.emplace_back([&] {
+                cudaSetDevice(b->device);
+                for (uint64_t j = next++; j < njobs; j = next++) {
+                    const ps_job_desc &jd = jobs[j];
+                    int rc = ps_create(jd.num_qubits, jd.shots, jd.seed, 1, &b->states[j]);
+                    if (rc == OK) {
+                        ps_circuit_options co{};
+                        co.mode = PS_MODE_FUSED;
+                        co.use_graph = 0;
+                        rc = ps_circuit_compile(b->states[j], jd.ops, jd.nops, jd.params, jd.nparams, &co, &b->circs[j]);
+                    }
+                    if (rc != OK) errs[j] = "job " + std::to_string(j) + ": " + ps_last_error();
+                    rcs[j] = rc;
+                }
+            });
+        for (auto &t : pool) t.join();
+    }
+    for (uint64_t j = 0; j < njobs; ++j)
+        if (rcs[j] != OK) {
+            fail(rcs[j], errs[j]);
+            return bail(rcs[j]);
+        }
+    b->stats.compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (b->opts.autotune) {
+        for (uint64_t j = 0; j < njobs; ++j) {
+            double ms = 0.0;
+            int rc = ps_circuit_autotune(b->circs[j], nullptr, &ms);
+            if (rc != OK) return bail(rc);
+            b->stats.tune_ms += ms;
+        }
+    }
+    // ---- stats and launch order
+    std::vector<double> work(njobs);
+    for (uint64_t j = 0; j < njobs; ++j) {
+        ps_circuit_stats cs{};
+        ps_circuit_get_stats(b->circs[j], &cs);
+        b->stats.shot_gates_per_run += cs.num_gates * jobs[j].shots;
+        b->stats.tableau_bytes += state_bytes((int64_t)jobs[j].num_qubits, (int64_t)jobs[j].shots);
+        b->stats.launches_per_run += cs.launches_per_run;  // its parameter update stands for the init launch
+        work[j] = (double)cs.segment_bytes;
+    }
+    b->stats.launches_per_run += 1;  // the parameter scatter
+    b->stats.num_jobs = njobs;
+    b->order.resize(njobs);
+    std::iota(b->order.begin(), b->order.end(), size_t(0));
+    std::stable_sort(b->order.begin(), b->order.end(), [&](size_t x, size_t y) { return work[x] > work[y]; });
+
+    // ---- streams, parameter staging
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+        return bail(cuda_fail(cudaGetLastError(), "stream/event"));
+    b->branches.assign(njobs, nullptr);
+    b->joins.assign(njobs, nullptr);
+    for (uint64_t k = 0; k < njobs; ++k)
+        if (cudaStreamCreateWithFlags(&b->branches[k], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming) != cudaSuccess)
+            return bail(cuda_fail(cudaGetLastError(), "stream/event"));
+    for (int r = 0; r < ps_batch::RING; ++r) {
+        if (cudaMallocHost(&b->h_vals[r], njobs * sizeof(RunParams)) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->copied[r], cudaEventDisableTiming) != cudaSuccess)
+            return bail(cuda_fail(cudaGetLastError(), "pinned staging"));
+    }
+    if (cudaMalloc(&b->d_vals, njobs * sizeof(RunParams)) != cudaSuccess ||
+        cudaMalloc(&b->d_dst, njobs * sizeof(RunParams *)) != cudaSuccess)
+        return bail(cuda_fail(cudaGetLastError(), "cudaMalloc"));
+    {
+        std::vector<RunParams *> dst(njobs);
+        for (uint64_t j = 0; j < njobs; ++j) dst[j] = circuit_params_dev(b->circs[j]);
+        if (cudaMemcpy(b->d_dst, dst.data(), njobs * sizeof(RunParams *), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(cuda_fail(cudaGetLastError(), "cudaMemcpy"));
+    }
+    // ---- one graph for the whole batch
+    if (b->opts.use_graph) {
+        cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+        int rc = e == cudaSuccess ? enqueue_batch(b) : cuda_fail(e, "cudaStreamBeginCapture");
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+        if (rc != OK) {
+            if (g) cudaGraphDestroy(g);
+            return bail(rc);
+        }
+        if (e2 != cudaSuccess) return bail(cuda_fail(e2, "cudaStreamEndCapture"));
+        b->graph = g;
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        if (e != cudaSuccess) return bail(cuda_fail(e, "cudaGraphInstantiate"));
+    }
+    *out = b;
+    return OK;
+}
+
+ps_status ps_batch_run(ps_batch *b) {
+    ps_enter(__func__, __LINE__);
+    if (!b) return fail(E_ARG, "null batch");
+    const int slot = b->ring_pos;
+    b->ring_pos = (b->ring_pos + 1) % ps_batch::RING;
+    PS_CUDA(cudaEventSynchronize(b->copied[slot]));  // the slot's previous copy has been read
+    RunParams *vals = b->h_vals[slot];
+    for (size_t j = 0; j < b->circs.size(); ++j) vals[j] = circuit_begin_run(b->circs[j], true);
+    PS_CUDA(cudaMemcpyAsync(b->d_vals, vals, b->circs.size() * sizeof(RunParams), cudaMemcpyHostToDevice, b->stream));
+    PS_CUDA(cudaEventRecord(b->copied[slot], b->stream));
+    if (b->exec) {
+        PS_CUDA(cudaGraphLaunch(b->exec, b->stream));
+        return OK;
+    }
+    return enqueue_batch(b);
+}
+
+ps_status ps_batch_synchronize(ps_batch *b) {
+    ps_enter(__func__, __LINE__);
+    if (!b) return fail(E_ARG, "null batch");
+    PS_CUDA(cudaStreamSynchronize(b->stream));
+    return OK;
+}
+
+ps_status ps_batch_get_stream(const ps_batch *b, void **stream) {
+    ps_enter(__func__, __LINE__);
+    if (!b || !stream) return fail(E_ARG, "null argument");
+    *stream = (void *)b->stream;
+    return OK;
+}
+
+ps_status ps_batch_job(const ps_batch *b, uint64_t j, ps_circuit **circuit, ps_state **state) {
+    ps_enter(__func__, __LINE__);
+    if (!b) return fail(E_ARG, "null batch");
+    if (j >= b->circs.size()) return fail(E_RANGE, "job index out of range");
+    if (circuit) *circuit = b->circs[j];
+    if (state) *state = b->states[j];
+    return OK;
+}
+
+ps_status ps_batch_get_stats(const ps_batch *b, ps_batch_stats *out) {
+    ps_enter(__func__, __LINE__);
+    if (!b || !out) return fail(E_ARG, "null argument");
+    *out = b->stats;
+    return OK;
+}
+
+ps_status ps_batch_destroy(ps_batch *b) {
+    ps_enter(__func__, __LINE__);
+    if (!b) return OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (ps_circuit *c : b->circs)
+        if (c) ps_circuit_destroy(c);
+    for (ps_state *h : b->states)
+        if (h) ps_destroy(h);
+    for (cudaStream_t s : b->branches)
+        if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t e : b->joins)
+        if (e) cudaEventDestroy(e);
+    for (int r = 0; r < ps_batch::RING; ++r) {
+        if (b->h_vals[r]) cudaFreeHost(b->h_vals[r]);
+        if (b->copied[r]) cudaEventDestroy(b->copied[r]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
+    cudaFree(b->d_vals);
+    cudaFree(b->d_dst);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return OK;
+}
+
+}  // extern "C"
+
+// ================================================================ serving
+namespace ps {
+namespace {
+
+struct SrvJob {
+    uint64_t id = 0;
+    std::vector<ps_op> ops;
+    std::vector<float> params;
+    uint64_t n = 0, shots = 0;
+    int64_t seed = 0;
+    size_t bytes = 0;
+    uint64_t shot_gates = 0;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    uint64_t retry_after = UINT64_MAX;  // re-admit only after this many completions
+    bool done = false;
+    int status = OK;
+    std::string err;
+    uint64_t nm = 0, words = 0;
+    std::vector<uint64_t> res, det;
+};
+
+}  // namespace
+}  // namespace ps
+
+struct ps_server {
+    ps_server_options opts{};
+    int device = 0;
+    ps::DevPool pool;
+    void *region = nullptr;
+    std::chrono::steady_clock::time_point t0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<ps::SrvJob *> queue;
+    std::unordered_map<uint64_t, std::unique_ptr<ps::SrvJob>> jobs;
+    size_t reserved = 0;
+    int active = 0;
+    bool stop = false;
+    uint64_t next_id = 1, submitted = 0, completed = 0, failed = 0, shot_gates = 0;
+    std::vector<double> latencies;
+    double first_submit = -1.0, last_done = 0.0;
+    std::vector<std::thread> workers;
+};
+
+namespace ps {
+namespace {
+
+// First queued job that fits the budget and a free slot, in arrival order;
+// a head job that has waited longer than hol_wait_s is not overtaken.
+SrvJob *pick_job(ps_server *s, double now) {
+    if (s->active >= s->opts.max_active) return nullptr;
+    for (size_t i = 0; i < s->queue.size(); ++i) {
+        SrvJob *j = s->queue[i];
+        const bool waiting_retry = j->retry_after != UINT64_MAX && s->completed <= j->retry_after;
+        if (!waiting_retry && s->reserved + j->bytes <= s->pool.cap) {
+            s->queue.erase(s->queue.begin() + (std::ptrdiff_t)i);
+            return j;
+        }
+        if (i == 0 && s->opts.hol_wait_s >= 0 && now - j->t_submit > s->opts.hol_wait_s) return nullptr;
+    }
+    return nullptr;
+}
+
+// Runs one admitted job on the calling worker thread: state from the pool,
+// fused compile, one run from |0...0>, records to host, everything returned.
+int run_job(ps_server *s, SrvJob *j) {
+    ps_state *h = new ps_state;
+    ps_circuit *c = nullptr;
+    int rc = state_alloc(h, (int64_t)j->n, (int64_t)j->shots, j->seed, &s->pool);
+    if (rc == OK) {
+        h->valid = true;
+        ps_circuit_options co{};
+        co.mode = PS_MODE_FUSED;
+        co.use_graph = 0;
+        rc = ps_circuit_compile(h, j->ops.data(), j->ops.size(), j->params.data(), j->params.size(), &co, &c);
+    }
+    if (rc == OK && s->opts.autotune) rc = ps_circuit_autotune(c, nullptr, nullptr);
+    if (rc == OK) rc = ps_circuit_run(c, 1);
+    if (rc == OK) {
+        ps_circuit_stats cs{};
+        ps_circuit_get_stats(c, &cs);
+        j->nm = cs.num_measurements;
+        j->words = (uint64_t)h->w;
+        j->res.assign(j->nm * j->words, 0);
+        j->det.assign(j->nm * j->words, 0);
+        uint64_t wds = 0;
+        rc = ps_circuit_copy_records(c, j->res.data(), j->det.data(), &wds);
+    }
+    if (rc != OK) j->err = ps_last_error();
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (c) ps_circuit_destroy(c);
+    state_free(h);
+    delete h;
+    return rc;
+}
+
+void worker_main(ps_server *s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        SrvJob *j = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_work.wait(lk, [&] { return s->stop || (j = pick_job(s, seconds_since(s->t0))) != nullptr; });
+            if (!j) return;  // stopping
+            s->reserved += j->bytes;
+            s->active++;
+            j->t_admit = seconds_since(s->t0);
+        }
+        const int rc = run_job(s, j);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->reserved -= j->bytes;
+            s->active--;
+            if (rc == E_NOMEM && s->active > 0) {
+                // The pool is fragmented right now: wait for another job to finish.
+                j->retry_after = s->completed;
+                j->err.clear();
+                s->queue.push_front(j);
+            } else {
+                j->status = rc;
+                j->t_done = seconds_since(s->t0);
+                j->done = true;
+                if (rc == OK) {
+                    s->completed++;
+                    s->shot_gates += j->shot_gates;
+                    s->latencies.push_back(j->t_done - j->t_submit);
+                    s->last_done = std::max(s->last_done, j->t_done);
+                } else {
+                    s->failed++;
+                    s->completed++;
+                }
+            }
+        }
+        s->cv_work.notify_all();
+        s->cv_done.notify_all();
+    }
+}
+
+double percentile(std::vector<double> v, double q) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double pos = q * (double)(v.size() - 1);
+    const size_t i = (size_t)pos;
+    const double f = pos - (double)i;
+    return i + 1 < v.size() ? v[i] * (1.0 - f) + v[i + 1] * f : v[i];
+}
+
+}  // namespace
+}  // namespace ps
+
+extern "C" {
+
+ps_status ps_server_create(const ps_server_options *opts, ps_server **out) {
+    ps_enter(__func__, __LINE__);
+    if (!opts || !out) return fail(E_ARG, "null argument");
+    *out = nullptr;
+    if (opts->hbm_budget_bytes < (1u << 20)) return fail(E_ARG, "HBM budget below 1 MiB");
+    auto *s = new ps_server;
+    s->opts = *opts;
+    if (s->opts.max_active <= 0) s->opts.max_active = 16;
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e == cudaSuccess) e = cudaMalloc(&s->region, opts->hbm_budget_bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete s;
+        return fail(E_NOMEM, std::string("cannot reserve the HBM budget: ") + cudaGetErrorString(e));
+    }
+    s->pool.reset(s->region, opts->hbm_budget_bytes);
+    s->t0 = std::chrono::steady_clock::now();
+    for (int i = 0; i < s->opts.max_active; ++i) s->workers.emplace_back(worker_main, s);
+    *out = s;
+    return OK;
+}
+
+ps_status ps_server_submit(ps_server *s, const ps_job_desc *job, uint64_t *job_id) {
+    ps_enter(__func__, __LINE__);
+    if (!s || !job) return fail(E_ARG, "null argument");
+    TRY(check_job(*job, 0));
+    auto j = std::make_unique<SrvJob>();
+    j->ops.assign(job->ops, job->ops + job->nops);
+    if (job->params && job->nparams) j->params.assign(job->params, job->params + job->nparams);
+    j->n = job->num_qubits;
+    j->shots = job->shots;
+    j->seed = job->seed;
+    j->bytes = job_device_bytes(*job);
+    j->shot_gates = count_gates(job->ops, job->nops) * job->shots;
+    if (j->bytes > s->pool.cap)
+        return fail(E_NOMEM, "job needs " + std::to_string(j->bytes >> 20) + " MiB, more than the whole HBM budget");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->stop) return fail(E_STATE, "server is shutting down");
+        j->id = s->next_id++;
+        j->t_submit = seconds_since(s->t0);
+        if (s->first_submit < 0) s->first_submit = j->t_submit;
+        s->submitted++;
+        if (job_id) *job_id = j->id;
+        s->queue.push_back(j.get());
+        s->jobs.emplace(j->id, std::move(j));
+    }
+    s->cv_work.notify_one();
+    return OK;
+}
+
+ps_status ps_server_wait(ps_server *s, uint64_t job_id, double timeout_s, ps_job_result *out) {
+    ps_enter(__func__, __LINE__);
+    if (!s) return fail(E_ARG, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job_id);
+    if (it == s->jobs.end()) return fail(E_RANGE, "unknown job id");
+    SrvJob *j = it->second.get();
+    auto ready = [&] { return j->done; };
+    if (timeout_s < 0)
+        s->cv_done.wait(lk, ready);
+    else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready))
+        return fail(E_TIMEOUT, "job not finished within the timeout");
+    if (out) {
+        std::memset(out, 0, sizeof(*out));
+        out->status = j->status;
+        out->num_measurements = j->nm;
+        out->words = j->words;
+        out->shot_gates = j->shot_gates;
+        out->device_bytes = j->bytes;
+        out->submit_s = j->t_submit;
+        out->admit_s = j->t_admit;
+        out->done_s = j->t_done;
+        out->latency_s = j->t_done - j->t_submit;
+    }
+    if (j->status != OK) return fail(j->status, "job " + std::to_string(job_id) + " failed: " + j->err);
+    return OK;
+}
+
+ps_status ps_server_copy_records(ps_server *s, uint64_t job_id, uint64_t *results, uint64_t *determined) {
+    ps_enter(__func__, __LINE__);
+    if (!s) return fail(E_ARG, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job_id);
+    if (it == s->jobs.end()) return fail(E_RANGE, "unknown job id");
+    SrvJob *j = it->second.get();
+    if (!j->done) return fail(E_STATE, "job not finished");
+    if (j->status != OK) return fail(j->status, "job failed: " + j->err);
+    if (results) std::memcpy(results, j->res.data(), j->res.size() * sizeof(uint64_t));
+    if (determined) std::memcpy(determined, j->det.data(), j->det.size() * sizeof(uint64_t));
+    return OK;
+}
+
+ps_status ps_server_release(ps_server *s, uint64_t job_id) {
+    ps_enter(__func__, __LINE__);
+    if (!s) return fail(E_ARG, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job_id);
+    if (it == s->jobs.end()) return fail(E_RANGE, "unknown job id");
+    if (!it->second->done) return fail(E_STATE, "job not finished");
+    s->jobs.erase(it);
+    return OK;
+}
+
+ps_status ps_server_drain(ps_server *s, double timeout_s) {
+    ps_enter(__func__, __LINE__);
+    if (!s) return fail(E_ARG, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto idle = [&] { return s->queue.empty() && s->active == 0; };
+    if (timeout_s < 0)
+        s->cv_done.wait(lk, idle);
+    else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), idle))
+        return fail(E_TIMEOUT, "jobs still queued or active");
+    return OK;
+}
+
+ps_status ps_server_get_stats(ps_server *s, ps_server_stats *out) {
+    ps_enter(__func__, __LINE__);
+    if (!s || !out) return fail(E_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->submitted = s->submitted;
+    out->completed = s->completed;
+    out->failed = s->failed;
+    out->queued = s->queue.size();
+    out->active = (uint64_t)s->active;
+    out->shot_gates_completed = s->shot_gates;
+    {
+        std::lock_guard<std::mutex> pk(s->pool.mu);
+        out->pool_bytes = s->pool.cap;
+        out->pool_peak_bytes = s->pool.peak;
+    }
+    out->p50_latency_s = percentile(s->latencies, 0.50);
+    out->p99_latency_s = percentile(s->latencies, 0.99);
+    if (!s->latencies.empty()) {
+        out->mean_latency_s = std::accumulate(s->latencies.begin(), s->latencies.end(), 0.0) / s->latencies.size();
+        out->max_latency_s = *std::max_element(s->latencies.begin(), s->latencies.end());
+    }
+    out->first_submit_s = s->first_submit;
+    out->last_done_s = s->last_done;
+    return OK;
+}
+
+ps_status ps_server_now(const ps_server *s, double *seconds) {
+    ps_enter(__func__, __LINE__);
+    if (!s || !seconds) return fail(E_ARG, "null argument");
+    *seconds = seconds_since(s->t0);
+    return OK;
+}
+
+ps_status ps_server_destroy(ps_server *s) {
+    ps_enter(__func__, __LINE__);
+    if (!s) return OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        for (SrvJob *j : s->queue) {  // never admitted
+            j->done = true;
+            j->status = E_STATE;
+            j->err = "server destroyed before the job was admitted";
+        }
+        s->queue.clear();
+    }
+    s->cv_work.notify_all();
+    for (auto &t : s->workers) t.join();
+    s->cv_done.notify_all();
+    cudaFree(s->region);
+    delete s;
+    return OK;
+}
+
+}  // extern "C"

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -67,12 +68,11 @@ namespace {
 void drain_at_exit() { cudaDeviceSynchronize(); }
 
 ps_status create_common(uint64_t n, uint64_t S, int64_t seed, ps_state **out) {
-    static bool exit_hook = false;
-    if (!exit_hook) {
+    static std::once_flag exit_hook;
+    std::call_once(exit_hook, [] {
         cudaFree(nullptr);  // initialise the runtime first
         std::atexit(drain_at_exit);
-        exit_hook = true;
-    }
+    });
     if (!out) return fail(E_ARG, "null output pointer");
     *out = nullptr;
     if (n > (uint64_t)1 << 20 || S > (uint64_t)1 << 36) return fail(E_ARG, "num_qubits or batch_size too large");
@@ -134,7 +134,8 @@ ps_status ps_device_synchronize(void) {
 
 const char *ps_backend_name(void) {
     static std::string name;
-    if (name.empty()) {
+    static std::once_flag once;
+    std::call_once(once, [] {
         cudaDeviceProp prop;
         int dev = 0;
         if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess)
@@ -142,7 +143,7 @@ const char *ps_backend_name(void) {
                    prop.name + ")";
         else
             name = "CUDA sm_103a (no device)";
-    }
+    });
     return name.c_str();
 }
 

@@ -5,9 +5,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <functional>
 #include <map>
+#include <mutex>
 #include <set>
 #include <string>
 #include <vector>
@@ -49,13 +51,15 @@ struct SegHost {
     void *dev_block = nullptr;
 };
 
-template <class T> int upload(std::vector<void *> &owned, const std::vector<T> &v, T **out) {
+// Device copy of a host table, owned by the circuit.  The copy is ordered on
+// the state's stream (pageable source: staged before the call returns).
+template <class T> int upload(ps_state *h, std::vector<void *> &owned, const std::vector<T> &v, T **out) {
     *out = nullptr;
     if (v.empty()) return OK;
     void *p = nullptr;
-    PS_CUDA(cudaMalloc(&p, v.size() * sizeof(T)));
+    if (dev_alloc(h, &p, v.size() * sizeof(T)) != OK) return E_NOMEM;
     owned.push_back(p);
-    PS_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    PS_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
     *out = static_cast<T *>(p);
     return OK;
 }
@@ -329,16 +333,26 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
     return OK;
 }
 
-void pick_tile(ps_circuit *c, int nq_max) {
+// Largest shared-memory footprint of any segment launch for a tile shape.
+size_t max_seg_smem(const ps_circuit *c, int rows, int bw) {
+    size_t m = 0;
+    for (const SegHost &sg : c->segs)
+        m = std::max(m, segment_launch_smem((int)sg.layers.size(), (int)sg.runs.size(), (int)sg.gates.size(),
+                                            (int)sg.signs.size(), (int)sg.cols.size(), (int)sg.recsig_rec.size(),
+                                            rows, bw));
+    return m;
+}
+
+void pick_tile(ps_circuit *c) {
     ps_circuit_options &o = c->opts;
     const ps_state *h = c->h;
+    if (o.seg_rows <= 0) o.seg_rows = 1;
     if (o.seg_words <= 0) {
         int bw = 8;
-        while (bw > 2 && (segment_smem_bytes(nq_max, 1, bw) > 200 * 1024 || bw > h->w)) bw >>= 1;
+        while (bw > 1 && (max_seg_smem(c, o.seg_rows, bw) > 200 * 1024 || bw > h->w)) bw >>= 1;
         o.seg_words = bw;
     }
-    if (o.seg_rows <= 0) o.seg_rows = 1;
-    if (o.seg_threads <= 0) o.seg_threads = std::min(256, std::max(64, 32 * o.seg_rows * o.seg_words));
+    if (o.seg_threads <= 0) o.seg_threads = std::min(256, std::max(32, 32 * o.seg_rows * o.seg_words));
 }
 
 // Optional per-launch timing: an event pair around every launch, by kind.
@@ -367,7 +381,8 @@ struct Profiler {
 
 enum ProfKind { P_INIT = 0, P_SAMPLE = 1, P_SEGMENT = 2, P_MEASURE = 3, P_GATE = 4, P_CHANNEL = 5 };
 
-int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nullptr) {
+// Enqueues plan steps [from, to) on `st`.
+int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profiler *prof = nullptr) {
     ps_state *h = c->h;
     auto timed = [&](int kind, auto &&launch) -> int {
         if (prof && prof->begin(kind) != OK) return E_CUDA;
@@ -375,11 +390,8 @@ int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nu
         if (prof && rc == OK && prof->end() != OK) return E_CUDA;
         return rc;
     };
-    if (reset) {
-        int rc = timed(P_INIT, [&] { return launch_init_zero_on(st, h); });
-        if (rc != OK) return rc;
-    }
-    for (const Step &s : c->steps) {
+    for (size_t i = from; i < to && i < c->steps.size(); ++i) {
+        const Step &s = c->steps[i];
         int rc = OK;
         switch (s.kind) {
         case K_GATE:
@@ -397,7 +409,7 @@ int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nu
         case K_MEAS:
             rc = timed(P_MEASURE, [&] {
                 return launch_measure_list(st, h->X, h->Z, h->R, h->n, h->w, c->d_meas + s.first, s.count,
-                                           (uint64_t)h->seed, 0, c->d_params);
+                                           (uint64_t)h->seed, 0, c->d_params, c->opts.meas_words);
             });
             break;
         case K_SEGMENT: {
@@ -414,6 +426,186 @@ int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nu
         }
         if (rc != OK) return rc;
     }
+    return OK;
+}
+
+int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nullptr) {
+    if (reset) {
+        if (prof && prof->begin(P_INIT) != OK) return E_CUDA;
+        int rc = launch_init_zero_on(st, c->h);
+        if (rc != OK) return rc;
+        if (prof && prof->end() != OK) return E_CUDA;
+    }
+    return enqueue_steps(c, st, 0, c->steps.size(), prof);
+}
+
+// Captures the plan into the two CUDA graphs (without / with the reset).
+int capture_graphs(ps_circuit *c) {
+    for (int reset = 0; reset < 2; ++reset) {
+        if (c->exec[reset]) cudaGraphExecDestroy(c->exec[reset]);
+        if (c->graph[reset]) cudaGraphDestroy(c->graph[reset]);
+        c->exec[reset] = nullptr;
+        c->graph[reset] = nullptr;
+        cudaStream_t cs;
+        PS_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        int rc = e == cudaSuccess ? enqueue_plan(c, cs, reset != 0) : cuda_fail(e, "cudaStreamBeginCapture");
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+        cudaStreamDestroy(cs);
+        if (rc != OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+        c->graph[reset] = g;
+        e = cudaGraphInstantiate(&c->exec[reset], g, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    return OK;
+}
+
+// Host bookkeeping of one run: records go stale, the event counter advances;
+// returns the run's parameters.
+RunParams begin_run(ps_circuit *c, bool reset) {
+    ps_state *h = c->h;
+    for (int64_t id : c->rec_ids) h->recs[(size_t)id].host_valid = false;
+    RunParams p;
+    p.seed = (uint64_t)h->seed;
+    p.event_base = h->events;
+    h->events += c->num_events;
+    if (reset) h->valid = true;
+    return p;
+}
+
+// ---- autotuner ---------------------------------------------------------
+struct TuneKey {
+    int64_t n, w;
+    int nq;
+    bool operator<(const TuneKey &o) const {
+        return n != o.n ? n < o.n : (w != o.w ? w < o.w : nq < o.nq);
+    }
+};
+struct TuneChoice {
+    int rows, words, threads, meas_words;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneChoice> g_tune_cache;
+
+struct EventTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventTimer() {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    }
+    ~EventTimer() {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
+
+int autotune(ps_circuit *c, double *tune_ms) {
+    ps_state *h = c->h;
+    const auto t0 = std::chrono::steady_clock::now();
+    size_t s0 = c->steps.size(), m0 = c->steps.size();
+    int nq = 1;
+    for (size_t i = 0; i < c->steps.size(); ++i) {
+        if (c->steps[i].kind == K_SEGMENT) {
+            nq = std::max(nq, (int)c->segs[(size_t)c->steps[i].first].cols.size());
+            if (s0 == c->steps.size()) s0 = i;
+        }
+        if (c->steps[i].kind == K_MEAS && s0 < c->steps.size() && m0 == c->steps.size() && c->steps[i].count > 1) m0 = i;
+    }
+    if (s0 == c->steps.size()) return OK;
+    const TuneKey key{h->n, h->w, nq};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            c->opts.seg_rows = it->second.rows;
+            c->opts.seg_words = it->second.words;
+            c->opts.seg_threads = it->second.threads;
+            c->opts.meas_words = it->second.meas_words;
+            if (tune_ms) *tune_ms = 0.0;
+            return OK;
+        }
+    }
+    const cudaStream_t st = h->stream;
+    set_params_kernel<<<1, 1, 0, st>>>(c->d_params, (uint64_t)h->seed, h->events);
+    PS_CUDA(cudaGetLastError());
+    auto prefix = [&](size_t upto) -> int {  // |0...0>, then steps [0, upto)
+        int rc = launch_init_zero_on(st, h);
+        if (rc == OK) rc = enqueue_steps(c, st, 0, upto);
+        return rc;
+    };
+    EventTimer ev;
+    auto time_it = [&](auto &&fn, float *ms) -> int {
+        PS_CUDA(cudaEventRecord(ev.a, st));
+        int rc = fn();
+        if (rc != OK) return rc;
+        PS_CUDA(cudaEventRecord(ev.b, st));
+        PS_CUDA(cudaEventSynchronize(ev.b));
+        PS_CUDA(cudaEventElapsedTime(ms, ev.a, ev.b));
+        return OK;
+    };
+    // Segment tiles: rows x shot-words x threads.
+    const SegHost &sg = c->segs[(size_t)c->steps[s0].first];
+    const int cand[][3] = {{1, 2, 64}, {1, 4, 128}, {1, 8, 256}, {2, 4, 256}, {1, 16, 256}, {2, 8, 256}, {4, 2, 256}};
+    int rc = prefix(s0);
+    if (rc == OK && !sg.slots.empty()) rc = launch_noise_sample(st, sg.dev, h->w, c->d_params);
+    if (rc != OK) return rc;
+    float best = 3.0e38f;
+    TuneChoice pick{c->opts.seg_rows, c->opts.seg_words, c->opts.seg_threads, c->opts.meas_words};
+    for (const auto &cd : cand) {
+        const int rows = cd[0], bw = cd[1], threads = cd[2];
+        if (bw > std::max<int64_t>(2, h->w)) continue;
+        if (max_seg_smem(c, rows, bw) > kSegSmemMax) continue;
+        auto go = [&] {
+            return launch_segment(st, h->X, h->Z, h->R, h->n, h->w, sg.dev, rows, bw, threads, c->d_recs);
+        };
+        float ms = 0.f, ms2 = 0.f;
+        if (time_it(go, &ms) != OK || time_it(go, &ms2) != OK) {  // the first launch also warms up
+            cudaGetLastError();
+            continue;
+        }
+        ms = std::min(ms, ms2);
+        if (ms < best) {
+            best = ms;
+            pick.rows = rows;
+            pick.words = bw;
+            pick.threads = threads;
+        }
+    }
+    c->opts.seg_rows = pick.rows;
+    c->opts.seg_words = pick.words;
+    c->opts.seg_threads = pick.threads;
+    // Measurement kernel: shot-words per CTA, on the first measurement phase.
+    if (m0 < c->steps.size()) {
+        float bestm = 3.0e38f;
+        for (int B = 1; B <= 2; ++B) {
+            if (B == 2 && h->w % 2) continue;
+            c->opts.meas_words = B;
+            float ms = 0.f;
+            for (int rep = 0; rep < 2; ++rep) {
+                rc = prefix(m0);
+                if (rc != OK) return rc;
+                rc = time_it([&] { return enqueue_steps(c, st, m0, m0 + 1); }, &ms);
+                if (rc != OK) return rc;
+            }
+            if (ms < bestm) {
+                bestm = ms;
+                pick.meas_words = B;
+            }
+        }
+        c->opts.meas_words = pick.meas_words;
+    }
+    PS_CUDA(cudaStreamSynchronize(st));
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = pick;
+    }
+    if (tune_ms)
+        *tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return OK;
 }
 
@@ -481,16 +673,15 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     }
     std::vector<u64 *> rec_ptrs;
     for (int64_t id : c->rec_ids) rec_ptrs.push_back(h->recs[(size_t)id].res);
-    if (upload(c->owned, rec_ptrs, &c->d_recs) != OK) return bail(E_CUDA);
+    if (upload(h, c->owned, rec_ptrs, &c->d_recs) != OK) return bail(E_CUDA);
     if (thr.empty()) thr.push_back(0);
-    if (upload(c->owned, thr, &c->d_thr) != OK) return bail(E_CUDA);
+    if (upload(h, c->owned, thr, &c->d_thr) != OK) return bail(E_CUDA);
     {
         void *p = nullptr;
-        if (cudaMalloc(&p, sizeof(RunParams)) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "cudaMalloc"));
+        if (dev_alloc(h, &p, sizeof(RunParams)) != OK) return bail(E_NOMEM);
         c->owned.push_back(p);
         c->d_params = (RunParams *)p;
-        if (cudaMalloc(&p, 4 * (size_t)h->w * sizeof(u64)) != cudaSuccess)
-            return bail(cuda_fail(cudaGetLastError(), "cudaMalloc"));
+        if (dev_alloc(h, &p, 4 * (size_t)h->w * sizeof(u64)) != OK) return bail(E_NOMEM);
         c->owned.push_back(p);
         c->d_masks = (u64 *)p;
     }
@@ -509,7 +700,6 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         c->meas.push_back(m);
     };
     size_t max_slots = 0;
-    int nq_max = 1;
     if (!fused) {
         for (size_t i = 0; i < ops.size(); ++i) {
             const ps_op &o = ops[i];
@@ -560,7 +750,6 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 SegHost seg;
                 build_segment(c, ops, i, j, event_of, rec_of, thr_off, pending, seg);
                 pending.clear();
-                nq_max = std::max(nq_max, (int)seg.cols.size());
                 max_slots = std::max(max_slots, seg.slots.size());
                 Step s{};
                 s.kind = K_SEGMENT;
@@ -571,19 +760,18 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             i = j;
         }
     }
-    pick_tile(c, nq_max);
+    pick_tile(c);
     if (fused) {
         c->entry_cap = (int32_t)std::max<size_t>(1, max_slots);
         void *p = nullptr;
-        if (cudaMalloc(&p, (size_t)c->entry_cap * h->w * sizeof(NoiseEntry)) != cudaSuccess)
+        if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * sizeof(NoiseEntry)) != OK)
             return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
         c->owned.push_back(p);
         c->d_entries = (NoiseEntry *)p;
-        if (cudaMalloc(&p, (size_t)h->w * sizeof(int32_t)) != cudaSuccess)
-            return bail(fail(E_NOMEM, "device allocation failed"));
+        if (dev_alloc(h, &p, (size_t)h->w * sizeof(int32_t)) != OK) return bail(E_NOMEM);
         c->owned.push_back(p);
         c->d_entry_count = (int32_t *)p;
-        if (cudaMalloc(&p, (size_t)c->entry_cap * h->w * 4 * sizeof(u64)) != cudaSuccess)
+        if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * 4 * sizeof(u64)) != OK)
             return bail(fail(E_NOMEM, "device allocation of channel sampling scratch failed"));
         c->owned.push_back(p);
         c->d_dense = (u64 *)p;
@@ -596,10 +784,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             int32_t *dc;
             NoiseSlot *dsl;
             int32_t *drr;
-            if (upload(c->owned, sg.layers, &dl) || upload(c->owned, sg.runs, &drn) || upload(c->owned, sg.gates, &dg) ||
-                upload(c->owned, sg.signs, &ds) ||
-                upload(c->owned, sg.cols, &dc) || upload(c->owned, sg.slots, &dsl) ||
-                upload(c->owned, sg.recsig_rec, &drr))
+            if (upload(h, c->owned, sg.layers, &dl) || upload(h, c->owned, sg.runs, &drn) || upload(h, c->owned, sg.gates, &dg) ||
+                upload(h, c->owned, sg.signs, &ds) ||
+                upload(h, c->owned, sg.cols, &dc) || upload(h, c->owned, sg.slots, &dsl) ||
+                upload(h, c->owned, sg.recsig_rec, &drr))
                 return bail(E_CUDA);
             d.recsig_rec = drr;
             d.nrecsig = (int32_t)sg.recsig_rec.size();
@@ -623,11 +811,12 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             sg.dev = d;
             const double W = (double)h->W, B8 = (double)h->S / 8.0;
             c->stats.segment_bytes += 2.0 * (2.0 * (double)sg.cols.size() + 1.0) * W * B8;
-            if (segment_smem_bytes(d.nq, c->opts.seg_rows, c->opts.seg_words) > 227 * 1024)
-                return bail(fail(E_ARG, "too many touched qubits for one fused tile"));
+            if (segment_launch_smem(d.nlayers, d.nruns, d.ngates, d.nsigns, d.nq, d.nrecsig, c->opts.seg_rows,
+                                    c->opts.seg_words) > kSegSmemMax)
+                return bail(fail(E_ARG, "segment schedule and tile do not fit in shared memory"));
         }
     }
-    if (upload(c->owned, c->meas, &c->d_meas) != OK) return bail(E_CUDA);
+    if (upload(h, c->owned, c->meas, &c->d_meas) != OK) return bail(E_CUDA);
 
     // ---- stats
     ps_circuit_stats &st = c->stats;
@@ -655,27 +844,16 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     st.seg_rows = c->opts.seg_rows;
     st.seg_words = c->opts.seg_words;
     st.seg_threads = c->opts.seg_threads;
+    st.meas_words = c->opts.meas_words;
+
+    // The tables above were copied on the state's stream; runs may be
+    // launched on other streams (graphs, batches).
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "upload"));
 
     // ---- graph capture
     if (c->opts.use_graph) {
-        for (int reset = 0; reset < 2; ++reset) {
-            cudaStream_t cs;
-            if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
-                return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
-            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-            int rc = e == cudaSuccess ? enqueue_plan(c, cs, reset != 0) : cuda_fail(e, "cudaStreamBeginCapture");
-            cudaGraph_t g = nullptr;
-            cudaError_t e2 = cudaStreamEndCapture(cs, &g);
-            cudaStreamDestroy(cs);
-            if (rc != OK) {
-                if (g) cudaGraphDestroy(g);
-                return bail(rc);
-            }
-            if (e2 != cudaSuccess) return bail(cuda_fail(e2, "cudaStreamEndCapture"));
-            c->graph[reset] = g;
-            e = cudaGraphInstantiate(&c->exec[reset], g, 0);
-            if (e != cudaSuccess) return bail(cuda_fail(e, "cudaGraphInstantiate"));
-        }
+        int rc = capture_graphs(c);
+        if (rc != OK) return bail(rc);
     }
     *out = c;
     return OK;
@@ -688,8 +866,10 @@ ps_status ps_circuit_set_forced(ps_circuit *c, const uint8_t *forced_all) {
     const size_t nm = c->meas.size();
     if (forced_all && nm) {
         if (!c->d_forced) {
-            if (cudaMalloc(&c->d_forced, nm * (size_t)h->w * sizeof(u64)) != cudaSuccess)
+            void *p = nullptr;
+            if (dev_alloc(h, &p, nm * (size_t)h->w * sizeof(u64)) != OK)
                 return fail(E_NOMEM, "device allocation of forced draws failed");
+            c->d_forced = (u64 *)p;
         }
         std::vector<u64> buf(nm * (size_t)h->w, 0ull);
         const size_t nb = (size_t)(h->S + 7) / 8;
@@ -712,11 +892,9 @@ ps_status ps_circuit_run(ps_circuit *c, int reset_state) {
     ps_enter(__func__, __LINE__);
     if (!c) return fail(E_ARG, "null circuit");
     ps_state *h = c->h;
-    for (int64_t id : c->rec_ids) h->recs[(size_t)id].host_valid = false;
-    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, (uint64_t)h->seed, h->events);
+    const RunParams p = begin_run(c, reset_state != 0);
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base);
     PS_CUDA(cudaGetLastError());
-    h->events += c->num_events;
-    if (reset_state) h->valid = true;
     if (c->exec[reset_state ? 1 : 0]) {
         PS_CUDA(cudaGraphLaunch(c->exec[reset_state ? 1 : 0], h->stream));
         return OK;
@@ -729,11 +907,9 @@ ps_status ps_circuit_profile(ps_circuit *c, int reset_state, ps_circuit_profile_
     if (!c || !out) return fail(E_ARG, "null argument");
     ps_state *h = c->h;
     std::memset(out, 0, sizeof(*out));
-    for (int64_t id : c->rec_ids) h->recs[(size_t)id].host_valid = false;
-    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, (uint64_t)h->seed, h->events);
+    const RunParams p = begin_run(c, reset_state != 0);
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base);
     PS_CUDA(cudaGetLastError());
-    h->events += c->num_events;
-    if (reset_state) h->valid = true;
     Profiler prof;
     prof.st = h->stream;
     int rc = enqueue_plan(c, h->stream, reset_state != 0, &prof);
@@ -760,10 +936,8 @@ ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *rand
     for (size_t k = 0; k < nm; ++k) m[k].kstat = d + 2 * k;
     PS_CUDA(cudaStreamSynchronize(h->stream));
     PS_CUDA(cudaMemcpy(c->d_meas, m.data(), nm * sizeof(MeasOp), cudaMemcpyHostToDevice));
-    for (int64_t id : c->rec_ids) h->recs[(size_t)id].host_valid = false;
-    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, (uint64_t)h->seed, h->events);
-    h->events += c->num_events;
-    if (reset_state) h->valid = true;
+    const RunParams p = begin_run(c, reset_state != 0);
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base);
     int rc = enqueue_plan(c, h->stream, reset_state != 0);
     cudaError_t e = cudaStreamSynchronize(h->stream);
     std::vector<int32_t> host(nm * 2);
@@ -793,6 +967,26 @@ ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *de
     return OK;
 }
 
+ps_status ps_circuit_autotune(ps_circuit *c, ps_circuit_options *chosen, double *tune_ms) {
+    ps_enter(__func__, __LINE__);
+    if (!c) return fail(E_ARG, "null circuit");
+    if (tune_ms) *tune_ms = 0.0;
+    if (c->opts.mode == PS_MODE_FUSED) {
+        int rc = autotune(c, tune_ms);
+        if (rc != OK) return rc;
+        c->stats.seg_rows = c->opts.seg_rows;
+        c->stats.seg_words = c->opts.seg_words;
+        c->stats.seg_threads = c->opts.seg_threads;
+        c->stats.meas_words = c->opts.meas_words;
+        if (c->opts.use_graph) {
+            rc = capture_graphs(c);
+            if (rc != OK) return rc;
+        }
+    }
+    if (chosen) *chosen = c->opts;
+    return OK;
+}
+
 ps_status ps_circuit_get_stats(const ps_circuit *c, ps_circuit_stats *out) {
     ps_enter(__func__, __LINE__);
     if (!c || !out) return fail(E_ARG, "null argument");
@@ -808,10 +1002,17 @@ ps_status ps_circuit_destroy(ps_circuit *c) {
         if (c->exec[k]) cudaGraphExecDestroy(c->exec[k]);
         if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
     }
-    for (void *p : c->owned) cudaFree(p);
-    cudaFree(c->d_forced);
+    for (void *p : c->owned) dev_free(c->h, p);
+    dev_free(c->h, c->d_forced);
     delete c;
     return OK;
 }
 
 }  // extern "C"
+
+namespace ps {
+int circuit_enqueue(ps_circuit *c, cudaStream_t st, bool reset) { return enqueue_plan(c, st, reset); }
+RunParams circuit_begin_run(ps_circuit *c, bool reset) { return begin_run(c, reset); }
+RunParams *circuit_params_dev(ps_circuit *c) { return c->d_params; }
+ps_state *circuit_state(ps_circuit *c) { return c->h; }
+}  // namespace ps

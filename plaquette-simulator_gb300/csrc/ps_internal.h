@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -52,6 +54,21 @@ struct MeasOp {
     int32_t pad;
 };
 
+// Sub-allocator over one device region reserved up front (the serving
+// loop's HBM budget).  Bookkeeping is on the host only, so returning memory
+// never synchronises the device; callers return a region only after the
+// work that used it has finished.
+struct DevPool {
+    std::mutex mu;
+    char *base = nullptr;
+    size_t cap = 0, used = 0, peak = 0;
+    std::map<size_t, size_t> free_;  // offset -> bytes, coalesced
+    std::map<size_t, size_t> taken;  // offset -> bytes
+    void reset(void *region, size_t bytes);
+    bool alloc(void **p, size_t bytes);  // best fit, 256-byte granules
+    void release(void *p);
+};
+
 } // namespace ps
 
 struct ps_state {
@@ -76,6 +93,8 @@ struct ps_state {
     // the host may not be; compiled circuits then keep every reset's X
     // inside its measurement phase instead of deferring it.
     bool valid = false;
+    // Device memory source: nullptr = cudaMalloc / cudaFree, else a pool.
+    ps::DevPool *pool = nullptr;
 };
 
 namespace ps {
@@ -83,7 +102,15 @@ namespace ps {
 void ps_enter(const char *method, int line);
 
 // ps_state.cu
-int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed);
+// Device memory of a state and of everything compiled for it.
+int dev_alloc(ps_state *h, void **p, size_t bytes);
+void dev_free(ps_state *h, void *p);
+int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed, DevPool *pool = nullptr);
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum, once per (kernel, device).  The limit is a process-wide property
+// of the kernel, so it is only ever raised: launches from other host threads
+// that asked for less are never invalidated between their check and launch.
+int allow_max_smem(const void *kernel);
 void state_free(ps_state *h);
 int launch_init_zero(ps_state *h);
 int launch_init_zero_on(cudaStream_t stream, ps_state *h);
@@ -107,12 +134,16 @@ void channel_thresholds(const float *p, int count, uint64_t *thr);
 // ps_measure.cu
 struct RunParams;
 int launch_measure(ps_state *h, const MeasOp *ops_host, int nops);
+// words_per_cta: 1 or 2 shot-words per CTA, 0 = automatic.
 int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops,
-                        int nops, uint64_t seed, uint64_t word_base, const RunParams *rp);
+                        int nops, uint64_t seed, uint64_t word_base, const RunParams *rp, int words_per_cta = 0);
 
 // ps_segment.cu
 struct SegmentDev;
 size_t segment_smem_bytes(int nq, int rows, int bw);
+// Shared memory of one segment launch: the tile plus the staged schedule.
+size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int nq, int nrecsig, int rows, int bw);
+constexpr size_t kSegSmemMax = 227 * 1024;
 int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp);
 int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
                    int rows, int bw, int threads, const u64 *const *recs);
@@ -122,6 +153,17 @@ int launch_channel_rp(cudaStream_t stream, ps_state *h, int64_t a, int64_t b, co
                       uint32_t event_off, const RunParams *rp, u64 *dev_masks);
 int launch_gate_on(cudaStream_t stream, ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag);
 } // namespace ps
+
+struct ps_circuit;
+namespace ps {
+// ps_circuit.cpp: the pieces of a compiled circuit that batches drive.
+int circuit_enqueue(ps_circuit *c, cudaStream_t st, bool reset);  // the plan, on any stream
+RunParams circuit_begin_run(ps_circuit *c, bool reset);           // host bookkeeping of one run
+RunParams *circuit_params_dev(ps_circuit *c);                     // device run parameters
+ps_state *circuit_state(ps_circuit *c);
+// ps_state.cu: device bytes state_alloc takes.
+size_t state_bytes(int64_t n, int64_t S);
+}  // namespace ps
 
 namespace ps {
 // ps_gates.cu: Pauli channel on q whose scratch lives in a fixed device array.

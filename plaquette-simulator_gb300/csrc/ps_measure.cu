@@ -61,6 +61,10 @@ struct Ctl {
     int uniform;
     int rows_done;
 };
+// Dynamic shared memory a measurement launch may take: the opt-in maximum
+// less the kernel's static control block.
+constexpr size_t kMeasSmemMax = 227 * 1024 - sizeof(Ctl) - 256;
+
 
 struct Smem {
     u64 *col;      // [2n][B]
@@ -787,8 +791,10 @@ template <int B>
 int launch_b(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops, int nops,
              uint64_t seed, const RunParams *rp, int window) {
     const size_t smem = smem_bytes(n, B);
-    if (smem > 48 * 1024)
-        PS_CUDA(cudaFuncSetAttribute(measure_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > 48 * 1024) {
+        const int rc = allow_max_smem((const void *)measure_kernel<B>);
+        if (rc != OK) return rc;
+    }
     measure_kernel<B><<<(unsigned)(w / B), NW * 32, smem, stream>>>(X, Z, R, n, w, dev_ops, nops, seed, rp, window);
     PS_CUDA(cudaGetLastError());
     return OK;
@@ -803,14 +809,16 @@ int measure_words_per_cta(int64_t n, int64_t w) {
 }
 
 int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops,
-                        int nops, uint64_t seed, uint64_t word_base, const RunParams *rp) {
+                        int nops, uint64_t seed, uint64_t word_base, const RunParams *rp, int words_per_cta) {
     (void)word_base;
     if (nops <= 0) return OK;
     if (n > (int64_t)NW * 32 * MAXC) return fail(E_ARG, "too many qubits for the measurement kernel (max 2048)");
     // A single measurement has no window to overlap: spread it over the most
     // CTAs (one word each).
-    const int B = nops == 1 ? 1 : measure_words_per_cta(n, w);
-    if (smem_bytes(n, B) > 227 * 1024) return fail(E_ARG, "measurement tile does not fit in shared memory");
+    int B = nops == 1 ? 1 : measure_words_per_cta(n, w);
+    if (nops > 1 && words_per_cta == 1) B = 1;
+    if (nops > 1 && words_per_cta == 2 && w % 2 == 0 && smem_bytes(n, 2) <= kMeasSmemMax) B = 2;
+    if (smem_bytes(n, B) > kMeasSmemMax) return fail(E_ARG, "measurement tile does not fit in shared memory");
     const int window = nops == 1 ? 0 : NW;
     if (B == 2) return launch_b<2>(stream, X, Z, R, n, w, dev_ops, nops, seed, rp, window);
     return launch_b<1>(stream, X, Z, R, n, w, dev_ops, nops, seed, rp, window);
@@ -818,10 +826,15 @@ int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, 
 
 int launch_measure(ps_state *h, const MeasOp *ops_host, int nops) {
     if ((size_t)nops > h->meas_cap) {
-        cudaFree(h->meas_buf);
+        // A pooled buffer is reused as soon as it is returned: let the
+        // launches that read the old one finish first.
+        if (h->pool && h->meas_buf) PS_CUDA(cudaStreamSynchronize(h->stream));
+        dev_free(h, h->meas_buf);
         h->meas_buf = nullptr;
         h->meas_cap = 0;
-        PS_CUDA(cudaMalloc(&h->meas_buf, (size_t)nops * sizeof(MeasOp)));
+        void *p = nullptr;
+        if (dev_alloc(h, &p, (size_t)nops * sizeof(MeasOp)) != OK) return E_NOMEM;
+        h->meas_buf = (MeasOp *)p;
         h->meas_cap = (size_t)nops;
     }
     PS_CUDA(cudaMemcpyAsync(h->meas_buf, ops_host, (size_t)nops * sizeof(MeasOp), cudaMemcpyHostToDevice, h->stream));

@@ -400,11 +400,12 @@ int g_num_sms = 0;
 
 size_t segment_smem_bytes(int nq, int rows, int bw) { return (size_t)rows * bw * (2 * ((size_t)(nq + 1) | 1) + 1) * sizeof(u64); }
 
-static size_t schedule_bytes(const SegmentDev &seg, int rows, int bw) {
-    return ((size_t)seg.nlayers * sizeof(SegLayer) + (size_t)seg.nruns * sizeof(SegRun) +
-            (size_t)seg.ngates * sizeof(SegGate) + (size_t)seg.nsigns * sizeof(SegSign) +
-            (size_t)seg.nq * sizeof(int32_t) + 15) / 16 * 16 +
-           (size_t)(seg.nrecsig + 1) / 2 * 16 + (size_t)seg.nrecsig * bw * 8 + (size_t)rows * bw * 8;
+size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int nq, int nrecsig, int rows, int bw) {
+    const size_t sched = ((size_t)nlayers * sizeof(SegLayer) + (size_t)nruns * sizeof(SegRun) +
+                          (size_t)ngates * sizeof(SegGate) + (size_t)nsigns * sizeof(SegSign) +
+                          (size_t)nq * sizeof(int32_t) + 15) / 16 * 16 +
+                         (size_t)(nrecsig + 1) / 2 * 16 + (size_t)nrecsig * bw * 8 + (size_t)rows * bw * 8;
+    return segment_smem_bytes(nq, rows, bw) + sched;
 }
 
 int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp) {
@@ -423,11 +424,15 @@ int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64
     const int64_t W = 2 * n + 1;
     const int64_t nchunks = (w + bw - 1) / bw;
     const int64_t tiles = ((W + rows - 1) / rows) * nchunks;
-    const size_t smem = segment_smem_bytes(seg.nq, rows, bw) + schedule_bytes(seg, rows, bw);
-    if (smem > 227 * 1024) return fail(E_ARG, "segment tile does not fit in shared memory");
+    const size_t smem =
+        segment_launch_smem(seg.nlayers, seg.nruns, seg.ngates, seg.nsigns, seg.nq, seg.nrecsig, rows, bw);
+    if (smem > kSegSmemMax) return fail(E_ARG, "segment tile does not fit in shared memory");
     if (threads % 32 != 0 || threads > 256 || bw > 32 || 32 % bw != 0)
         return fail(E_ARG, "segment tile: threads a multiple of 32 (at most 256), words a divisor of 32");
-    PS_CUDA(cudaFuncSetAttribute(segment_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    {
+        const int rc = allow_max_smem((const void *)segment_kernel);
+        if (rc != OK) return rc;
+    }
     if (g_num_sms == 0) {
         int dev = 0;
         PS_CUDA(cudaGetDevice(&dev));

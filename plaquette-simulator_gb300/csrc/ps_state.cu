@@ -2,6 +2,8 @@
 // import/export, checksum and measurement-record storage.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <set>
 #include <vector>
 
 #include "ps_internal.h"
@@ -107,10 +109,53 @@ int grid_for(int64_t work, int threads = 256) {
 
 }  // namespace
 
-int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed) {
+int allow_max_smem(const void *kernel) {
+    static std::mutex mu;
+    static std::set<std::pair<const void *, int>> done;
+    int dev = 0;
+    PS_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({kernel, dev})) return OK;
+    int optin = 0;
+    PS_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    PS_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    const int dyn = optin - (int)fa.sharedSizeBytes;  // static shared memory counts against the limit
+    PS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+    done.insert({kernel, dev});
+    return OK;
+}
+
+int dev_alloc(ps_state *h, void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    if (h->pool) {
+        if (!h->pool->alloc(p, bytes)) return fail(E_NOMEM, "device pool exhausted (" + std::to_string(bytes >> 20) + " MiB requested)");
+        return OK;
+    }
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(E_NOMEM, "device allocation failed (" + std::to_string(bytes >> 20) + " MiB): " +
+                                 cudaGetErrorString(e));
+    }
+    return OK;
+}
+
+void dev_free(ps_state *h, void *p) {
+    if (!p) return;
+    if (h->pool)
+        h->pool->release(p);
+    else
+        cudaFree(p);
+}
+
+int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed, DevPool *pool) {
     h->n = n;
     h->S = S;
     h->W = 2 * n + 1;
+    h->pool = pool;
     int64_t w = (S + 63) / 64;
     w = (w + 1) & ~int64_t(1);  // even: every column starts 16-byte aligned
     if (w == 0) w = 2;
@@ -119,31 +164,50 @@ int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed) {
     PS_CUDA(cudaGetDevice(&h->device));
     PS_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t plane = (size_t)h->W * (size_t)(n > 0 ? n : 1) * (size_t)w * sizeof(u64);
-    if (cudaMalloc(&h->X, plane) != cudaSuccess || cudaMalloc(&h->Z, plane) != cudaSuccess ||
-        cudaMalloc(&h->R, (size_t)h->W * w * sizeof(u64)) != cudaSuccess) {
-        cudaGetLastError();
+    void *px = nullptr, *pz = nullptr, *pr = nullptr;
+    if (dev_alloc(h, &px, plane) != OK || dev_alloc(h, &pz, plane) != OK ||
+        dev_alloc(h, &pr, (size_t)h->W * w * sizeof(u64)) != OK) {
+        dev_free(h, px);
+        dev_free(h, pz);
         return fail(E_NOMEM, "device allocation of the tableau failed (" + std::to_string(3 * plane >> 20) + " MiB)");
     }
-    PS_CUDA(cudaMalloc(&h->forced_buf, (size_t)w * sizeof(u64)));
-    PS_CUDA(cudaMalloc(&h->mask_buf, (size_t)4 * w * sizeof(u64)));
+    h->X = (u64 *)px;
+    h->Z = (u64 *)pz;
+    h->R = (u64 *)pr;
+    void *pf = nullptr, *pm = nullptr;
+    if (dev_alloc(h, &pf, (size_t)w * sizeof(u64)) != OK) return E_NOMEM;
+    h->forced_buf = (u64 *)pf;
+    if (dev_alloc(h, &pm, (size_t)4 * w * sizeof(u64)) != OK) return E_NOMEM;
+    h->mask_buf = (u64 *)pm;
     h->arena.words = (size_t)w;
     return OK;
 }
 
+// Bytes state_alloc takes for a state of n qubits and S shots.
+size_t state_bytes(int64_t n, int64_t S) {
+    int64_t w = (S + 63) / 64;
+    w = (w + 1) & ~int64_t(1);
+    if (w == 0) w = 2;
+    const size_t W = 2 * (size_t)n + 1;
+    return 2 * W * (size_t)(n > 0 ? n : 1) * (size_t)w * 8 + W * (size_t)w * 8 + 5 * (size_t)w * 8;
+}
+
 void state_free(ps_state *h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
-    cudaFree(h->X);
-    cudaFree(h->Z);
-    cudaFree(h->R);
-    cudaFree(h->forced_buf);
-    cudaFree(h->mask_buf);
-    cudaFree(h->meas_buf);
-    for (u64 *c : h->arena.chunks) cudaFree(c);
-    for (u64 *c : h->arena.blocks) cudaFree(c);
+    dev_free(h, h->X);
+    dev_free(h, h->Z);
+    dev_free(h, h->R);
+    dev_free(h, h->forced_buf);
+    dev_free(h, h->mask_buf);
+    dev_free(h, h->meas_buf);
+    for (u64 *c : h->arena.chunks) dev_free(h, c);
+    for (u64 *c : h->arena.blocks) dev_free(h, c);
     h->arena.chunks.clear();
     h->arena.blocks.clear();
     if (h->stream) cudaStreamDestroy(h->stream);
     h->X = h->Z = h->R = nullptr;
+    h->forced_buf = h->mask_buf = nullptr;
+    h->meas_buf = nullptr;
 }
 
 int launch_init_zero_on(cudaStream_t stream, ps_state *h) {
@@ -158,12 +222,10 @@ int launch_init_zero(ps_state *h) { return launch_init_zero_on(h->stream, h); }
 int record_new(ps_state *h, int64_t q, int64_t *id) {
     RecordArena &a = h->arena;
     if (a.chunks.empty() || a.used_in_last == a.per_chunk) {
-        u64 *chunk = nullptr;
-        if (cudaMalloc(&chunk, a.per_chunk * 2 * a.words * sizeof(u64)) != cudaSuccess) {
-            cudaGetLastError();
+        void *chunk = nullptr;
+        if (dev_alloc(h, &chunk, a.per_chunk * 2 * a.words * sizeof(u64)) != OK)
             return fail(E_NOMEM, "device allocation of measurement records failed");
-        }
-        a.chunks.push_back(chunk);
+        a.chunks.push_back((u64 *)chunk);
         a.used_in_last = 0;
     }
     Record rec;
@@ -183,11 +245,10 @@ int record_block(ps_state *h, const std::vector<int64_t> &qubits, std::vector<in
     ids.clear();
     *res_block = *det_block = nullptr;
     if (nm == 0) return OK;
-    u64 *blk = nullptr;
-    if (cudaMalloc(&blk, 2 * nm * wds * sizeof(u64)) != cudaSuccess) {
-        cudaGetLastError();
+    void *pblk = nullptr;
+    if (dev_alloc(h, &pblk, 2 * nm * wds * sizeof(u64)) != OK)
         return fail(E_NOMEM, "device allocation of measurement records failed");
-    }
+    u64 *blk = (u64 *)pblk;
     PS_CUDA(cudaMemsetAsync(blk, 0, 2 * nm * wds * sizeof(u64), h->stream));
     // The state owns the block (freed with the state), like its other records.
     h->arena.blocks.push_back(blk);

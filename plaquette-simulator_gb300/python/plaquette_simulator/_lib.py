@@ -66,6 +66,23 @@ _SIGS = {
     "ps_circuit_profile": (C.c_int, [_vp, C.c_int, _vp]),
     "ps_circuit_copy_records": (C.c_int, [_vp, _vp, _vp, _pu64]),
     "ps_circuit_measure_stats": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "ps_circuit_autotune": (C.c_int, [_vp, _vp, C.POINTER(C.c_double)]),
+    "ps_batch_create": (C.c_int, [_vp, _u64, _vp, _pp]),
+    "ps_batch_run": (C.c_int, [_vp]),
+    "ps_batch_synchronize": (C.c_int, [_vp]),
+    "ps_batch_get_stream": (C.c_int, [_vp, _pp]),
+    "ps_batch_job": (C.c_int, [_vp, _u64, _pp, _pp]),
+    "ps_batch_get_stats": (C.c_int, [_vp, _vp]),
+    "ps_batch_destroy": (C.c_int, [_vp]),
+    "ps_server_create": (C.c_int, [_vp, _pp]),
+    "ps_server_submit": (C.c_int, [_vp, _vp, _pu64]),
+    "ps_server_wait": (C.c_int, [_vp, _u64, C.c_double, _vp]),
+    "ps_server_copy_records": (C.c_int, [_vp, _u64, _vp, _vp]),
+    "ps_server_release": (C.c_int, [_vp, _u64]),
+    "ps_server_drain": (C.c_int, [_vp, C.c_double]),
+    "ps_server_get_stats": (C.c_int, [_vp, _vp]),
+    "ps_server_now": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "ps_server_destroy": (C.c_int, [_vp]),
     "ps_synchronize": (C.c_int, [_vp]),
     "ps_get_stream": (C.c_int, [_vp, _pp]),
     "ps_get_device_tableau": (C.c_int, [_vp, _pp, _pp, _pp, _pu64]),

@@ -22,7 +22,7 @@ from .simulator import CliffordState, _ptr
 
 class CircuitOptions(C.Structure):
     _fields_ = [("mode", C.c_int32), ("use_graph", C.c_int32), ("seg_rows", C.c_int32),
-                ("seg_words", C.c_int32), ("seg_threads", C.c_int32)]
+                ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32)]
 
 
 class CircuitStats(C.Structure):
@@ -30,7 +30,7 @@ class CircuitStats(C.Structure):
                 ("num_channels", C.c_uint64), ("num_events", C.c_uint64), ("num_segments", C.c_uint64),
                 ("num_measure_phases", C.c_uint64), ("launches_per_run", C.c_uint64),
                 ("first_record", C.c_uint64), ("segment_bytes", C.c_double), ("seg_rows", C.c_int32),
-                ("seg_words", C.c_int32), ("seg_threads", C.c_int32)]
+                ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -38,7 +38,7 @@ class CircuitStats(C.Structure):
 
 class CompiledCircuit:
     def __init__(self, circuit: Circuit, state: CliffordState, fused: bool = True, graph: bool = True,
-                 seg_rows: int = 0, seg_words: int = 0, seg_threads: int = 0):
+                 seg_rows: int = 0, seg_words: int = 0, seg_threads: int = 0, meas_words: int = 0):
         if circuit.num_qubits != state.get_num_qubits():
             raise ValueError("circuit and state have different qubit counts")
         self._L = _lib.load()
@@ -46,16 +46,41 @@ class CompiledCircuit:
         self.circuit = circuit
         self._ops = np.ascontiguousarray(circuit.op_array(), dtype=np.int32)
         self._params = np.ascontiguousarray(circuit.param_array(), dtype=np.float32)
-        opts = CircuitOptions(1 if fused else 0, 1 if graph else 0, seg_rows, seg_words, seg_threads)
+        opts = CircuitOptions(1 if fused else 0, 1 if graph else 0, seg_rows, seg_words, seg_threads, meas_words)
         h = C.c_void_p()
         check(self._L.ps_circuit_compile(state.handle, _ptr(self._ops), len(self._ops), _ptr(self._params),
                                          len(self._params), C.byref(opts), C.byref(h)))
         self._h = h
         self.stats = self.get_stats()
 
+    @classmethod
+    def _borrowed(cls, handle, circuit: Circuit, state: CliffordState) -> "CompiledCircuit":
+        """A view of a circuit owned by someone else (a batch job)."""
+        self = cls.__new__(cls)
+        self._L = _lib.load()
+        self.state, self.circuit = state, circuit
+        self._h = None
+        self._view = C.c_void_p(handle)
+        self.stats = self.get_stats()
+        return self
+
+    @property
+    def _handle(self):
+        return self._h if self._h is not None else self._view
+
+    def autotune(self) -> dict:
+        """Time tile shapes on this circuit's state and keep the fastest
+        (ps_circuit_autotune); returns the chosen options and the tuning time."""
+        o = CircuitOptions()
+        ms = C.c_double()
+        check(self._L.ps_circuit_autotune(self._handle, C.byref(o), C.byref(ms)))
+        self.stats = self.get_stats()
+        return {"seg_rows": o.seg_rows, "seg_words": o.seg_words, "seg_threads": o.seg_threads,
+                "meas_words": o.meas_words, "tune_ms": ms.value}
+
     def get_stats(self) -> dict:
         st = CircuitStats()
-        check(self._L.ps_circuit_get_stats(self._h, C.byref(st)))
+        check(self._L.ps_circuit_get_stats(self._handle, C.byref(st)))
         return st.as_dict()
 
     @property
@@ -65,17 +90,17 @@ class CompiledCircuit:
     def set_forced(self, forced_all: Optional[np.ndarray]) -> None:
         """Forced draws: one row of ceil(batch/8) packed bytes per M / R."""
         if forced_all is None:
-            check(self._L.ps_circuit_set_forced(self._h, None))
+            check(self._L.ps_circuit_set_forced(self._handle, None))
             return
         f = np.ascontiguousarray(forced_all, dtype=np.uint8)
         nb = (self.state.get_batch_size() + 7) // 8
         if f.shape != (self.stats["num_measurements"], nb):
             raise ValueError(f"forced draws must have shape ({self.stats['num_measurements']}, {nb})")
-        check(self._L.ps_circuit_set_forced(self._h, _ptr(f)))
+        check(self._L.ps_circuit_set_forced(self._handle, _ptr(f)))
 
     def run(self, reset: bool = False) -> None:
         """Enqueue one run on the state's stream (asynchronous)."""
-        check(self._L.ps_circuit_run(self._h, 1 if reset else 0))
+        check(self._L.ps_circuit_run(self._handle, 1 if reset else 0))
 
     PROFILE_KINDS = ("init", "channel_sample", "segment", "measure", "gate", "channel")
 
@@ -85,7 +110,7 @@ class CompiledCircuit:
         class _Prof(C.Structure):
             _fields_ = [("ms", C.c_double * 6), ("launches", C.c_uint64 * 6)]
         p = _Prof()
-        check(self._L.ps_circuit_profile(self._h, 1 if reset else 0, C.byref(p)))
+        check(self._L.ps_circuit_profile(self._handle, 1 if reset else 0, C.byref(p)))
         return {k: {"ms": p.ms[i], "launches": int(p.launches[i])} for i, k in enumerate(self.PROFILE_KINDS)}
 
     def measure_stats(self, reset: bool = True):
@@ -94,7 +119,7 @@ class CompiledCircuit:
         nm = int(self.stats["num_measurements"])
         rnd = np.zeros(max(nm, 1), np.int32)
         rows = np.zeros(max(nm, 1), np.int32)
-        check(self._L.ps_circuit_measure_stats(self._h, 1 if reset else 0, _ptr(rnd), _ptr(rows)))
+        check(self._L.ps_circuit_measure_stats(self._handle, 1 if reset else 0, _ptr(rnd), _ptr(rows)))
         return rnd[:nm], rows[:nm]
 
     def measure_bytes(self, reset: bool = True) -> float:
@@ -111,7 +136,7 @@ class CompiledCircuit:
         """Copy every record of the circuit to host arrays of shape
         [num_measurements, words] uint64 (pinned buffers give async speed)."""
         words = C.c_uint64()
-        check(self._L.ps_circuit_copy_records(self._h, _ptr(results), _ptr(determined), C.byref(words)))
+        check(self._L.ps_circuit_copy_records(self._handle, _ptr(results), _ptr(determined), C.byref(words)))
         return words.value
 
     def records(self):

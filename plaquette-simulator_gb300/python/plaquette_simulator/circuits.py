@@ -116,6 +116,16 @@ class Circuit:
     def param_array(self) -> np.ndarray:
         return np.asarray(self.params if self.params else [0.0], dtype=np.float32)
 
+    def arrays(self):
+        """(op_array, param_array), converted once and reused while the
+        circuit is unchanged (job submission hot path)."""
+        key = (len(self.ops), len(self.params))
+        cached = getattr(self, "_arrays", None)
+        if cached is None or cached[0] != key:
+            cached = (key, np.ascontiguousarray(self.op_array()), np.ascontiguousarray(self.param_array()))
+            self._arrays = cached
+        return cached[1], cached[2]
+
     def num_gates(self) -> int:
         """Gate applications per shot: H S X Y Z CX CZ M R (noise excluded)."""
         return sum(1 for o in self.ops if o[0] in GATE_CODES)

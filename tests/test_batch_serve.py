@@ -1,0 +1,158 @@
+"""Batches of uneven jobs in one graph launch (ps_batch_*) and the serving
+loop (ps_server_*): each job's measurement records are bit-identical to the
+same job run alone on a fresh state, and to the CPU oracle."""
+import math
+
+import numpy as np
+import pytest
+
+
+def _bits(words, shots):
+    """[nm, w] uint64 record words -> [nm, shots] 0/1 (bit s of word k = shot 64k+s)."""
+    b = np.unpackbits(np.ascontiguousarray(words).view(np.uint8), axis=1, bitorder="little")
+    return b[:, :shots].astype(np.int32)
+
+
+# ------------------------------------------------------------------ CPU
+def test_uneven_jobs_follow_the_mix():
+    from plaquette_simulator.batch import uneven_surface_jobs, PS_NOISE
+    jobs = uneven_surface_jobs(64, seed=12345)
+    assert len(jobs) == 64
+    assert {j.distance for j in jobs} <= set(range(3, 22, 2))
+    assert all(256 <= j.shots <= 65536 and j.shots % 64 == 0 for j in jobs)
+    assert {j.p for j in jobs} <= set(PS_NOISE)
+    assert [j.seed for j in jobs] == list(range(12345, 12345 + 64))
+    assert all(j.num_qubits == 2 * j.distance ** 2 - 1 for j in jobs)
+    # seeded: the same mix every time
+    again = uneven_surface_jobs(64, seed=12345)
+    assert [(j.distance, j.shots, j.p) for j in jobs] == [(j.distance, j.shots, j.p) for j in again]
+    # log-uniform shots: about half the jobs below the geometric midpoint 4096
+    below = sum(j.shots <= 4096 for j in uneven_surface_jobs(2000, seed=7))
+    assert 850 < below < 1150
+
+
+def test_poisson_arrivals_rate():
+    from plaquette_simulator.batch import poisson_arrivals
+    t = poisson_arrivals(200.0, 60.0, seed=12345)
+    assert all(0 < a < 60.0 for a in t) and t == sorted(t)
+    assert abs(len(t) - 12000) < 4 * math.sqrt(12000)
+    gaps = np.diff(t)
+    assert abs(gaps.mean() - 1 / 200.0) < 0.05 / 200.0 * 4
+
+
+# ------------------------------------------------------------------ GPU
+def _small_jobs():
+    from plaquette_simulator.batch import Job
+    from plaquette_simulator import circuits as C
+    spec = [(3, 320, 0.03, 11), (5, 1000, 5e-3, 12), (3, 64, 1e-3, 13), (7, 700, 1e-3, 14),
+            (5, 4096, 1e-2, 15), (3, 2000, 5e-3, 16)]
+    return [Job(C.surface_code_memory(d, d, p=p), s, seed, d, p) for d, s, p, seed in spec]
+
+
+def _alone(ps, job, runs=1):
+    from plaquette_simulator.circuit import CompiledCircuit
+    st = ps.CliffordState(job.num_qubits, job.shots, job.seed, True)
+    cc = CompiledCircuit(job.circuit, st, fused=True, graph=True)
+    nm = job.circuit.num_measurements()
+    w = ((job.shots + 63) // 64 + 1) & ~1
+    out = []
+    for _ in range(runs):
+        cc.run(reset=True)
+        res = np.zeros((nm, w), np.uint64)
+        det = np.zeros_like(res)
+        cc.copy_records_words(res, det)
+        out.append((res, det))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("autotune,graph", [(False, True), (True, True), (False, False)])
+def test_batch_jobs_match_alone(ps, autotune, graph):
+    from plaquette_simulator.batch import Batch
+    jobs = _small_jobs()
+    b = Batch(jobs, autotune=autotune, graph=graph)
+    assert b.stats["num_jobs"] == len(jobs)
+    assert b.stats["shot_gates_per_run"] == sum(j.shot_gates() for j in jobs)
+    b.run()
+    first = [b.records(j) for j in range(len(jobs))]
+    b.run()  # a second run draws fresh outcomes, exactly like a second run alone
+    second = [b.records(j) for j in range(len(jobs))]
+    for j, job in enumerate(jobs):
+        alone = _alone(ps, job, runs=2)
+        for k, got in enumerate((first[j], second[j])):
+            assert np.array_equal(got[0], alone[k][0]), f"job {j} run {k}: results differ"
+            assert np.array_equal(got[1], alone[k][1]), f"job {j} run {k}: determined differ"
+        if autotune:
+            o = b.job_options(j)
+            assert o["seg_words"] in (2, 4, 8, 16) and o["meas_words"] in (0, 1, 2)
+    b.close()
+
+
+@pytest.mark.gpu
+def test_batch_job_matches_oracle(ps, O):
+    from plaquette_simulator.batch import Batch
+    jobs = _small_jobs()[:3]
+    b = Batch(jobs, autotune=True)
+    b.run()
+    for j, job in enumerate(jobs):
+        res, det = b.records(j)
+        o = O.Oracle(job.num_qubits, job.shots, seed=job.seed)
+        o.run(job.circuit.op_array(), job.circuit.param_array())
+        gres, gdet = _bits(res, job.shots), _bits(det, job.shots)
+        for k in range(job.circuit.num_measurements()):
+            ores, odet = o.record(k)
+            assert np.array_equal(gres[k], ores), f"job {j} record {k}"
+            assert np.array_equal(gdet[k], odet), f"job {j} record {k}"
+    b.close()
+
+
+@pytest.mark.gpu
+def test_server_mix_matches_alone(ps):
+    from plaquette_simulator.batch import Server
+    jobs = _small_jobs() * 2
+    biggest = max(j.device_bytes() for j in jobs)
+    # A budget of a few jobs: later arrivals queue and are admitted as
+    # earlier ones finish, while up to 4 run at once.
+    with Server(hbm_budget_bytes=3 * biggest + (64 << 20), max_active=4) as srv:
+        ids = [srv.submit(j) for j in jobs]
+        got = [srv.records(i) for i in ids]
+        infos = [srv.wait(i) for i in ids]
+        st = srv.stats()
+    assert st["completed"] == len(jobs) and st["failed"] == 0
+    assert 0 < st["p50_latency_s"] <= st["p99_latency_s"] <= st["max_latency_s"]
+    assert st["pool_peak_bytes"] <= st["pool_bytes"]
+    assert all(r["latency_s"] >= 0 and r["admit_s"] >= r["submit_s"] for r in infos)
+    for j, job in enumerate(jobs):
+        alone = _alone(ps, job)[0]
+        assert np.array_equal(got[j][0], alone[0]), f"job {j}: results differ in the mix"
+        assert np.array_equal(got[j][1], alone[1]), f"job {j}: determined differ in the mix"
+
+
+@pytest.mark.gpu
+def test_server_refuses_job_over_budget(ps):
+    from plaquette_simulator import _lib
+    from plaquette_simulator.batch import Server
+    job = _small_jobs()[4]
+    with Server(hbm_budget_bytes=4 << 20, max_active=2) as srv:
+        with pytest.raises(_lib.PlaquetteError) as e:
+            srv.submit(job)
+        assert e.value.status == _lib.PS_E_NOMEM
+
+
+@pytest.mark.gpu
+def test_server_d25_job_matches_oracle(ps, O):
+    """The largest serving size (d=25, 1249 qubits): its schedule and tile
+    must share one CTA's shared memory; one round, 64 shots, against the
+    oracle."""
+    from plaquette_simulator.batch import Job, Server
+    from plaquette_simulator import circuits as C
+    job = Job(C.surface_code_memory(25, 1, p=1e-3), 64, 4321, 25, 1e-3)
+    with Server(hbm_budget_bytes=2 << 30, max_active=2) as srv:
+        res, det = srv.records(srv.submit(job))
+    o = O.Oracle(job.num_qubits, job.shots, seed=job.seed)
+    o.run(job.circuit.op_array(), job.circuit.param_array())
+    gres, gdet = _bits(res, job.shots), _bits(det, job.shots)
+    for k in range(job.circuit.num_measurements()):
+        ores, odet = o.record(k)
+        assert np.array_equal(gres[k], ores), f"record {k}"
+        assert np.array_equal(gdet[k], odet), f"record {k}"

@@ -197,6 +197,10 @@ typedef struct {
     int32_t seg_words;   /* fused tile: 64-shot words per CTA (0 = auto)         */
     int32_t seg_threads; /* fused tile: threads per CTA (0 = auto)               */
     int32_t meas_words;  /* measurement kernel: shot-words per CTA, 1 or 2 (0 = auto) */
+    int32_t seg_resident; /* fused segments: 1 = keep gate-dense columns in registers
+                             where possible (channel outcomes and sign ops then
+                             act after the last layer through propagated
+                             Paulis), 0 = every gate through shared memory     */
 } ps_circuit_options;
 
 typedef struct {
@@ -205,6 +209,7 @@ typedef struct {
     uint64_t first_record;          /* state record id of the first M/R      */
     double segment_bytes;           /* algorithmic HBM bytes of all segments  */
     int32_t seg_rows, seg_words, seg_threads, meas_words;
+    int32_t resident_segments;      /* segments in the register-resident form */
 } ps_circuit_stats;
 
 typedef struct ps_circuit ps_circuit;

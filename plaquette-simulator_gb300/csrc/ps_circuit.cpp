@@ -47,6 +47,12 @@ struct SegHost {
     std::vector<int32_t> cols;
     std::vector<NoiseSlot> slots;
     std::vector<int32_t> recsig_rec;  // record of each reset-X slot
+    // resident form (res_slots > 0)
+    int32_t res_slots = 0;
+    std::vector<uint16_t> res_cols;   // [RC][32]
+    std::vector<ResOp> res_ops;       // [nlayers][RC][32]
+    std::vector<uint32_t> prop_desc;  // [4 nslots + nsigns]
+    std::vector<uint32_t> prop_sup;
     SegmentDev dev{};
     void *dev_block = nullptr;
 };
@@ -224,9 +230,170 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
             L[layer].slots.push_back(sl);
         }
     }
-    // Tile positions: a permutation of the columns chosen (identity or one of
-    // a few seeded shuffles) to need the fewest conflict-free lane groups.
     const int nq = (int)seg.cols.size();
+    const int nl = (int)L.size();
+
+    // ---- resident form: columns kept in registers by their owner lane.
+    // Eligible without per-shot conditional gates (their effect on a Pauli
+    // would depend on the shot).  The resident set is independent in the
+    // segment's two-qubit-gate graph: on a bipartite graph (data / ancilla)
+    // the side with more gate touches, else greedily by touches.
+    std::vector<std::vector<SegGate>> all_gates(nl);
+    for (int l = 0; l < nl; ++l) all_gates[l] = L[l].gates;
+    bool res_form = c->opts.seg_resident > 0;
+    std::vector<int> touches(nq, 0);
+    std::vector<std::vector<int>> adj(nq);
+    for (int l = 0; l < nl && res_form; ++l)
+        for (const SegGate &g : L[l].gates) {
+            const int32_t code = g.code_rec & 15;
+            if (code == OP_H_IF || code == OP_S_IF) res_form = false;
+            touches[g.a]++;
+            if (code == OP_CX || code == OP_CZ) {
+                touches[g.b]++;
+                adj[g.a].push_back(g.b);
+                adj[g.b].push_back(g.a);
+            }
+        }
+    std::vector<int> resident;  // local columns
+    if (res_form) {
+        std::vector<int> color(nq, -1);
+        std::vector<char> pick(nq, 0);
+        for (int s0 = 0; s0 < nq; ++s0) {
+            if (color[s0] >= 0 || touches[s0] == 0) continue;
+            std::vector<int> comp{s0};
+            color[s0] = 0;
+            bool bip = true;
+            for (size_t h = 0; h < comp.size(); ++h)
+                for (int v : adj[comp[h]]) {
+                    if (color[v] < 0) {
+                        color[v] = 1 - color[comp[h]];
+                        comp.push_back(v);
+                    } else if (color[v] == color[comp[h]]) {
+                        bip = false;
+                    }
+                }
+            if (bip) {
+                long t0 = 0, t1 = 0;
+                for (int v : comp) (color[v] ? t1 : t0) += touches[v];
+                const int side = t1 > t0 ? 1 : 0;
+                for (int v : comp) pick[v] = color[v] == side;
+            } else {
+                std::vector<int> ord(comp);
+                std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return touches[x] > touches[y]; });
+                for (int v : ord) {
+                    bool ok = true;
+                    for (int u : adj[v]) ok &= !pick[u];
+                    pick[v] = ok;
+                }
+            }
+        }
+        for (int v = 0; v < nq; ++v)
+            if (pick[v] && touches[v] >= 2) resident.push_back(v);
+        std::stable_sort(resident.begin(), resident.end(), [&](int x, int y) { return touches[x] > touches[y]; });
+        if (resident.size() > 256) resident.resize(256);
+        if (resident.empty()) res_form = false;
+    }
+    std::vector<int> res_ord(nq, -1);
+    int RC = 0;
+    // per layer, per resident ordinal: (code, partner local column)
+    std::vector<std::vector<std::pair<uint8_t, int>>> rops;
+    if (res_form) {
+        // Owners: ordinals sorted by their gate signature, so lanes of one
+        // slot tend to run the same code (no divergence).
+        std::vector<std::string> sig(nq);
+        for (int l = 0; l < nl; ++l)
+            for (const SegGate &g : L[l].gates) {
+                const int32_t code = g.code_rec & 15;
+                sig[g.a] += (char)('a' + code * 2);
+                if (code == OP_CX || code == OP_CZ) sig[g.b] += (char)('a' + code * 2 + 1);
+            }
+        std::stable_sort(resident.begin(), resident.end(), [&](int x, int y) { return sig[x] < sig[y]; });
+        for (size_t i = 0; i < resident.size(); ++i) res_ord[resident[i]] = (int)i;
+        const int need = (int)((resident.size() + 31) / 32);
+        RC = need <= 2 ? 2 : need <= 4 ? 4 : 8;
+        rops.assign(nl, std::vector<std::pair<uint8_t, int>>(resident.size(), {RS_NOP, 0}));
+        for (int l = 0; l < nl; ++l) {
+            std::vector<SegGate> free_gates;
+            for (const SegGate &g : L[l].gates) {
+                const int32_t code = g.code_rec & 15;
+                const int ra = res_ord[g.a];
+                const int rb = (code == OP_CX || code == OP_CZ) ? res_ord[g.b] : -1;
+                if (ra >= 0 && (code == OP_H || code == OP_S)) {
+                    rops[l][ra] = {code == OP_H ? RS_H : RS_S, 0};
+                } else if (ra >= 0 && (code == OP_CX || code == OP_CZ)) {
+                    rops[l][ra] = {code == OP_CX ? RS_CX_CTRL : RS_CZ, g.b};
+                } else if (rb >= 0) {
+                    rops[l][rb] = {code == OP_CX ? RS_CX_TGT : RS_CZ, g.a};
+                } else {
+                    free_gates.push_back(g);
+                }
+            }
+            L[l].gates = free_gates;
+        }
+    }
+
+    // ---- propagated Paulis of channel components and sign ops (local
+    // columns; mapped to tile positions after the permutation below)
+    std::vector<std::vector<std::pair<int, uint8_t>>> props;  // bits: 1 = x, 2 = z
+    if (res_form) {
+        std::vector<std::vector<int>> gate_at(nl, std::vector<int>(nq, -1));
+        for (int l = 0; l < nl; ++l)
+            for (size_t gi = 0; gi < all_gates[l].size(); ++gi) {
+                const SegGate &g = all_gates[l][gi];
+                gate_at[l][g.a] = (int)gi;
+                const int32_t code = g.code_rec & 15;
+                if (code == OP_CX || code == OP_CZ) gate_at[l][g.b] = (int)gi;
+            }
+        auto propagate = [&](int col, uint8_t bits, int from) {
+            std::map<int, uint8_t> p;
+            if (col >= 0 && bits) p[col] = bits;
+            for (int l = from + 1; l < nl && !p.empty(); ++l) {
+                std::set<int> gs;
+                for (auto &kv : p)
+                    if (gate_at[l][kv.first] >= 0) gs.insert(gate_at[l][kv.first]);
+                for (int gi : gs) {
+                    const SegGate &g = all_gates[l][gi];
+                    const int32_t code = g.code_rec & 15;
+                    auto get = [&](int q) { auto it = p.find(q); return it == p.end() ? (uint8_t)0 : it->second; };
+                    const uint8_t va = get(g.a);
+                    const int xa = va & 1, za = (va >> 1) & 1;
+                    if (code == OP_H) {
+                        p[g.a] = (uint8_t)(za | (xa << 1));
+                    } else if (code == OP_S) {
+                        p[g.a] = (uint8_t)(xa | ((za ^ xa) << 1));
+                    } else {
+                        const uint8_t vb = get(g.b);
+                        const int xb = vb & 1, zb = (vb >> 1) & 1;
+                        if (code == OP_CX) {  // X_c -> X_c X_t, Z_t -> Z_c Z_t
+                            p[g.a] = (uint8_t)(xa | ((za ^ zb) << 1));
+                            p[g.b] = (uint8_t)((xb ^ xa) | (zb << 1));
+                        } else {  // CZ: X_a -> X_a Z_b
+                            p[g.a] = (uint8_t)(xa | ((za ^ xb) << 1));
+                            p[g.b] = (uint8_t)(xb | ((zb ^ xa) << 1));
+                        }
+                    }
+                }
+                for (auto it = p.begin(); it != p.end();) it = it->second ? std::next(it) : p.erase(it);
+            }
+            return std::vector<std::pair<int, uint8_t>>(p.begin(), p.end());
+        };
+        for (int l = 0; l < nl; ++l)
+            for (const NoiseSlot &sl : L[l].slots) {
+                props.push_back(propagate(sl.a, 1, l));
+                props.push_back(propagate(sl.a, 2, l));
+                props.push_back(propagate(sl.b, 1, l));
+                props.push_back(propagate(sl.b, 2, l));
+            }
+        for (int l = 0; l < nl; ++l)
+            for (const SegSign &sg : L[l].signs)
+                props.push_back(propagate(sg.a, sg.kind == SIGN_Z ? 2 : sg.kind == SIGN_Y ? 3 : 1, l));
+        for (auto &pr : props)
+            if (pr.size() > 255) res_form = false;
+    }
+
+    // Tile positions: a permutation of the columns chosen (identity or one of
+    // a few seeded shuffles) to need the fewest conflict-free lane groups
+    // (resident form: the fewest bank conflicts of the owners' partner cells).
     const uint16_t dummy = (uint16_t)nq;  // zero column appended to every tile row
     auto remap = [](const std::vector<SegGate> &gs, const std::vector<int> &perm) {
         std::vector<SegGate> out(gs);
@@ -238,6 +405,15 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
     };
     auto groups_needed = [&](const std::vector<int> &perm) {
         size_t total = 0;
+        if (res_form) {  // per (layer, slot, quarter-warp): wavefronts = largest residue multiplicity
+            for (int l = 0; l < nl; ++l)
+                for (size_t base = 0; base < resident.size(); base += 8) {
+                    int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0}, mx = 0;
+                    for (size_t o = base; o < std::min(resident.size(), base + 8); ++o)
+                        if (rops[l][o].first >= RS_CX_CTRL) mx = std::max(mx, ++cnt[perm[rops[l][o].second] & 7]);
+                    total += (size_t)mx;
+                }
+        }
         for (size_t l = 0; l < L.size(); ++l)
             for (int32_t code : {(int32_t)OP_H, (int32_t)OP_S, (int32_t)OP_CX, (int32_t)OP_CZ}) {
                 std::vector<SegGate> gs;
@@ -310,7 +486,9 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
         }
         ly.r1 = (int32_t)seg.runs.size();
         ly.s0 = (int32_t)seg.signs.size();
-        {
+        if (res_form) {  // after the last layer, in this order (propagated Pauli 4*nslots + k)
+            seg.signs.insert(seg.signs.end(), L[l].signs.begin(), L[l].signs.end());
+        } else {
             // interleave residues so 8 consecutive sign ops read distinct bank groups
             std::vector<SegSign> byres[8];
             for (const SegSign &sg : L[l].signs) byres[sg.a & 7].push_back(sg);
@@ -328,7 +506,26 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
         seg.layers.push_back(ly);
         seg.slots.insert(seg.slots.end(), L[l].slots.begin(), L[l].slots.end());
     }
-    (void)c;
+    if (res_form) {
+        seg.res_slots = RC;
+        seg.res_cols.assign((size_t)RC * 32, (uint16_t)0xFFFF);
+        for (size_t o = 0; o < resident.size(); ++o) seg.res_cols[o] = (uint16_t)best[resident[o]];
+        seg.res_ops.assign((size_t)nl * RC * 32, ResOp{0, RS_NOP, 0});
+        for (int l = 0; l < nl; ++l)
+            for (size_t o = 0; o < resident.size(); ++o) {
+                const auto &op = rops[l][o];
+                if (op.first == RS_NOP) continue;
+                seg.res_ops[(size_t)l * RC * 32 + o] =
+                    ResOp{(uint16_t)(op.first >= RS_CX_CTRL ? best[op.second] : 0), op.first, 0};
+            }
+        for (const auto &pr : props) {
+            seg.prop_desc.push_back(((uint32_t)seg.prop_sup.size() << 8) | (uint32_t)pr.size());
+            for (const auto &e : pr)
+                seg.prop_sup.push_back((uint32_t)best[e.first] | ((e.second & 1) ? PROP_X : 0u) |
+                                       ((e.second & 2) ? PROP_Z : 0u));
+        }
+        if (seg.prop_sup.empty()) seg.prop_sup.push_back(0);
+    }
     (void)rec_of;
     return OK;
 }
@@ -339,7 +536,7 @@ size_t max_seg_smem(const ps_circuit *c, int rows, int bw) {
     for (const SegHost &sg : c->segs)
         m = std::max(m, segment_launch_smem((int)sg.layers.size(), (int)sg.runs.size(), (int)sg.gates.size(),
                                             (int)sg.signs.size(), (int)sg.cols.size(), (int)sg.recsig_rec.size(),
-                                            rows, bw));
+                                            rows, bw, sg.res_slots));
     return m;
 }
 
@@ -626,7 +823,9 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     if (opts) c->opts = *opts;
     const bool fused = c->opts.mode == PS_MODE_FUSED;
     auto bail = [&](int rc) {
+        const std::string msg = ps_last_error();
         ps_circuit_destroy(c);
+        set_error(msg);  // keep the failing step's message
         return rc;
     };
 
@@ -791,6 +990,19 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 return bail(E_CUDA);
             d.recsig_rec = drr;
             d.nrecsig = (int32_t)sg.recsig_rec.size();
+            if (sg.res_slots > 0) {
+                uint16_t *drc;
+                ResOp *dro;
+                uint32_t *dpd, *dps;
+                if (upload(h, c->owned, sg.res_cols, &drc) || upload(h, c->owned, sg.res_ops, &dro) ||
+                    upload(h, c->owned, sg.prop_desc, &dpd) || upload(h, c->owned, sg.prop_sup, &dps))
+                    return bail(E_CUDA);
+                d.res_slots = sg.res_slots;
+                d.res_cols = drc;
+                d.res_ops = dro;
+                d.prop_desc = dpd;
+                d.prop_sup = dps;
+            }
             d.layers = dl;
             d.nlayers = (int32_t)sg.layers.size();
             d.runs = drn;
@@ -812,7 +1024,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             const double W = (double)h->W, B8 = (double)h->S / 8.0;
             c->stats.segment_bytes += 2.0 * (2.0 * (double)sg.cols.size() + 1.0) * W * B8;
             if (segment_launch_smem(d.nlayers, d.nruns, d.ngates, d.nsigns, d.nq, d.nrecsig, c->opts.seg_rows,
-                                    c->opts.seg_words) > kSegSmemMax)
+                                    c->opts.seg_words, d.res_slots) > kSegSmemMax)
                 return bail(fail(E_ARG, "segment schedule and tile do not fit in shared memory"));
         }
     }
@@ -845,6 +1057,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     st.seg_words = c->opts.seg_words;
     st.seg_threads = c->opts.seg_threads;
     st.meas_words = c->opts.meas_words;
+    for (const SegHost &sg : c->segs) st.resident_segments += sg.res_slots > 0 ? 1 : 0;
 
     // The tables above were copied on the state's stream; runs may be
     // launched on other streams (graphs, batches).

@@ -142,7 +142,8 @@ int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, 
 struct SegmentDev;
 size_t segment_smem_bytes(int nq, int rows, int bw);
 // Shared memory of one segment launch: the tile plus the staged schedule.
-size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int nq, int nrecsig, int rows, int bw);
+size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int nq, int nrecsig, int rows, int bw,
+                           int rc);
 constexpr size_t kSegSmemMax = 227 * 1024;
 int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp);
 int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,

@@ -60,6 +60,7 @@ struct Ctl {
     int cnt;
     int uniform;
     int rows_done;
+    int resq[NW];  // window slot -> qubit of its reset, or -1
 };
 // Dynamic shared memory a measurement launch may take: the opt-in maximum
 // less the kernel's static control block.
@@ -73,6 +74,9 @@ struct Smem {
     int *rowlist;  // [2n]
     int *klist;    // [NW][KMAX]
     u64 *kmask;    // [NW][KMAX][B]
+    u64 *wraw;     // [NW][B] window outcomes before reset corrections
+    u64 *wres;     // [NW][B] window outcomes
+    u64 *wz;       // [NW][NW][B] z of measurement j's product row at reset r's qubit
 };
 
 __device__ __forceinline__ void warp_phase_reduce(u64 &c1, u64 &c0, int first_offset) {
@@ -196,8 +200,9 @@ __device__ int warp_scan(const u64 *X, int64_t n, int64_t w, int64_t k0, const M
 // instruction, UC column groups of all rows in flight together.  If
 // `writer`, the product becomes the scratch row.
 template <int B, int KR, int UC>
-__device__ void warp_det_rows(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, int64_t k0, const MeasOp &op,
-                              const int *klist, const u64 *kmask, int kp, bool writer) {
+__device__ void warp_det_rows(u64 *X, u64 *Z, const u64 *R, int64_t n, int64_t w, int64_t k0, const int *klist,
+                              const u64 *kmask, int kp, bool writer, int slot, const int *resq, u64 *wraw,
+                              u64 *wz) {
     constexpr int CPI = 32 / B;
     const int lane = threadIdx.x & 31, cs = lane / B, b = lane % B;
     const int64_t k = k0 + b;
@@ -245,22 +250,29 @@ __device__ void warp_det_rows(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, int6
             warp_phase_reduce(c1[t], c0[t], B);
             racc ^= (R[((int64_t)klist[t] + n) * w + k] ^ c1[t]) & m[t];
         }
-    if (cs == 0) {
-        op.res[k] = racc;
-        op.det[k] = ~0ull;
-        if (writer) R[2 * n * w + k] = racc;
+    if (cs == 0) wraw[slot * B + b] = racc;
+    // z of the product row at the qubit of each earlier reset in the window
+    // (lane = (earlier slot, word)): a reset's X flips the sign of every row
+    // with z on its qubit, so it flips this outcome where that z is set.
+    if (cs < slot && resq[cs] >= 0) {
+        const int64_t qr = resq[cs];
+        u64 zb = 0ull;
+#pragma unroll
+        for (int t = 0; t < KR; ++t)
+            if (t < kp) zb ^= Z[(ro[t] + qr) * w + k] & m[t];
+        wz[(slot * NW + cs) * B + b] = zb;
     }
 }
 
 template <int B>
-__device__ void warp_det(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, int64_t k0, const MeasOp &op,
-                         const int *klist, const u64 *kmask, int kp, bool writer) {
+__device__ void warp_det(u64 *X, u64 *Z, const u64 *R, int64_t n, int64_t w, int64_t k0, const int *klist,
+                         const u64 *kmask, int kp, bool writer, int slot, const int *resq, u64 *wraw, u64 *wz) {
     if (kp <= 2)
-        warp_det_rows<B, 2, 8>(X, Z, R, n, w, k0, op, klist, kmask, kp, writer);
+        warp_det_rows<B, 2, 8>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
     else if (kp <= 4)
-        warp_det_rows<B, 4, 4>(X, Z, R, n, w, k0, op, klist, kmask, kp, writer);
+        warp_det_rows<B, 4, 4>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
     else
-        warp_det_rows<B, KMAX, 2>(X, Z, R, n, w, k0, op, klist, kmask, kp, writer);
+        warp_det_rows<B, KMAX, 2>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
 }
 
 // ---------------------------------------------------------------------------
@@ -723,7 +735,10 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
     s.prow = s.col + 2 * n * B;
     s.part = s.prow + 2 * n * B;
     s.kmask = s.part + STEP_CHUNK * NW * 2;
-    s.rowlist = reinterpret_cast<int *>(s.kmask + NW * KMAX * B);
+    s.wraw = s.kmask + NW * KMAX * B;
+    s.wres = s.wraw + NW * B;
+    s.wz = s.wres + NW * B;
+    s.rowlist = reinterpret_cast<int *>(s.wz + NW * NW * B);
     s.klist = s.rowlist + 2 * n;
 
     int pos = 0;
@@ -749,26 +764,67 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
             }
         }
         __syncthreads();
-        // Leading run of deterministic measurements (ends after a reset whose
-        // X must act before the next measurement).  Read before the next
-        // barrier: the next window's scan overwrites the status words.
+        // Leading run of deterministic measurements, resets included: a
+        // reset's X only flips signs (rows < 2n keep their x and z), so the
+        // later measurements of the run stay deterministic with the same rows;
+        // their outcomes are corrected for the earlier resets below.  Read
+        // the status words before the next barrier: the next window's scan
+        // overwrites them.
         int P = 0;
-        while (P < act && ctl.status[P] != ST_OTHER) {
-            ++P;
-            if (ctl.status[P - 1] == ST_DET_RESET) break;
-        }
-        const bool last_reset = P > 0 && ctl.status[P - 1] == ST_DET_RESET;
+        while (P < act && ctl.status[P] != ST_OTHER) ++P;
+        if (tid < NW) ctl.resq[tid] = (tid < P && ctl.status[tid] == ST_DET_RESET) ? ops[pos + tid].q : -1;
+        __syncthreads();
+        bool any_reset = false;
+        for (int j = 0; j < P; ++j) any_reset |= ctl.resq[j] >= 0;
         if (warp < P) {
+            warp_det<B>(X, Z, R, n, w, k0, s.klist + warp * KMAX, s.kmask + warp * KMAX * B, ctl.kcnt[warp],
+                        warp == P - 1, warp, ctl.resq, s.wraw, s.wz);
             const MeasOp op = ops[pos + warp];
-            warp_det<B>(X, Z, R, n, w, k0, op, s.klist + warp * KMAX, s.kmask + warp * KMAX * B,
-                                          ctl.kcnt[warp], warp == P - 1);
             if (op.kstat && k0 == 0 && (tid & 31) == 0) {
                 op.kstat[0] = 0;
                 op.kstat[1] = ctl.kcnt[warp];
             }
         }
         __syncthreads();
-        if (last_reset) cta_reset_flip<B>(Z, R, n, w, k0, ops[pos + P - 1]);
+        if (P > 0) {
+            // Outcomes in order: measurement j sees the X of every earlier
+            // reset r of the run on the shots where r's outcome is 1.
+            if (tid < B) {
+                const int b = tid;
+                const int64_t k = k0 + b;
+                for (int j = 0; j < P; ++j) {
+                    u64 v = s.wraw[j * B + b];
+                    for (int r = 0; r < j; ++r)
+                        if (ctl.resq[r] >= 0) v ^= s.wres[r * B + b] & s.wz[(j * NW + r) * B + b];
+                    s.wres[j * B + b] = v;
+                    const MeasOp op = ops[pos + j];
+                    op.res[k] = v;
+                    op.det[k] = ~0ull;
+                }
+                R[2 * n * w + k] = s.wres[(P - 1) * B + b];  // the scratch row the last measurement left
+            }
+            __syncthreads();
+            if (any_reset) {
+                // Every reset's X on rows 0..2n-1; the scratch row only sees
+                // the last measurement's own reset (later measurements
+                // rewrite it).
+                const int64_t Wr = 2 * n + 1;
+                for (int64_t e = tid; e < Wr * B; e += blockDim.x) {
+                    const int64_t i = e / B;
+                    const int b = (int)(e % B);
+                    const int64_t k = k0 + b;
+                    u64 acc = 0ull;
+                    if (i < 2 * n) {
+                        for (int r = 0; r < P; ++r)
+                            if (ctl.resq[r] >= 0) acc ^= s.wres[r * B + b] & Z[(i * n + ctl.resq[r]) * w + k];
+                    } else if (ctl.resq[P - 1] >= 0) {
+                        acc = s.wres[(P - 1) * B + b] & Z[(i * n + ctl.resq[P - 1]) * w + k];
+                    }
+                    if (acc) R[i * w + k] ^= acc;
+                }
+                __syncthreads();
+            }
+        }
         pos += P;
         if (P < act) {
             const MeasOp op = ops[pos];
@@ -783,7 +839,8 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
 }
 
 size_t smem_bytes(int64_t n, int B) {
-    return (size_t)(2 * n * B + 2 * n * B + STEP_CHUNK * NW * 2 + NW * KMAX * B) * sizeof(u64) +
+    return (size_t)(2 * n * B + 2 * n * B + STEP_CHUNK * NW * 2 + NW * KMAX * B + 2 * NW * B + NW * NW * B) *
+               sizeof(u64) +
            (size_t)(2 * n + NW * KMAX) * sizeof(int);
 }
 
@@ -791,7 +848,7 @@ template <int B>
 int launch_b(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops, int nops,
              uint64_t seed, const RunParams *rp, int window) {
     const size_t smem = smem_bytes(n, B);
-    if (smem > 48 * 1024) {
+    if (smem + sizeof(Ctl) > 48 * 1024) {  // static and dynamic shared memory share the default limit
         const int rc = allow_max_smem((const void *)measure_kernel<B>);
         if (rc != OK) return rc;
     }

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
             e.fza = fza;
             e.fxb = fxb;
             e.fzb = fzb;
-            e.layer = sl.layer;
+            e.layer = seg.res_slots ? s : sl.layer;  // resident form: the slot
             e.a = (uint16_t)sl.a;
             e.b = sl.b >= 0 ? (uint16_t)sl.b : (uint16_t)0xFFFF;
             out[pos] = e;
@@ -160,45 +160,51 @@ __device__ __forceinline__ void apply_gate(const SegGate g, XZ *__restrict__ t, 
 }
 
 // A layer whose gates all have one code: the branch is taken once per layer
-// and every lane keeps two independent gates in flight.
+// and every lane keeps GU independent gates in flight (gates g, g+32, ...),
+// so their shared-memory loads overlap.
 template <int CODE>
 __device__ __forceinline__ void layer_uniform(const SegGate *__restrict__ gates, int g0, int g1, int lane,
                                               XZ *__restrict__ t, u64 &rd) {
-    for (int g = g0 + lane; g < g1; g += 64) {
-        const bool two = g + 32 < g1;
-        const SegGate ga = gates[g];
-        const SegGate gb = two ? gates[g + 32] : ga;
+    constexpr int GU = 4;
+    for (int g = g0 + lane; g < g1; g += 32 * GU) {
+        SegGate gg[GU];
+        bool on[GU];
+#pragma unroll
+        for (int u = 0; u < GU; ++u) {
+            on[u] = g + 32 * u < g1;
+            gg[u] = gates[on[u] ? g + 32 * u : g];
+        }
         if (CODE == OP_H || CODE == OP_S) {
-            const XZ va = t[ga.a];
-            const XZ vb = t[gb.a];
-            rd ^= va.x & va.y;
-            t[ga.a] = CODE == OP_H ? make_ulonglong2(va.y, va.x) : make_ulonglong2(va.x, va.y ^ va.x);
-            if (two) {
-                rd ^= vb.x & vb.y;
-                t[gb.a] = CODE == OP_H ? make_ulonglong2(vb.y, vb.x) : make_ulonglong2(vb.x, vb.y ^ vb.x);
-            }
+            XZ v[GU];
+#pragma unroll
+            for (int u = 0; u < GU; ++u) v[u] = t[gg[u].a];
+#pragma unroll
+            for (int u = 0; u < GU; ++u)
+                if (on[u]) {
+                    rd ^= v[u].x & v[u].y;
+                    t[gg[u].a] = CODE == OP_H ? make_ulonglong2(v[u].y, v[u].x)
+                                              : make_ulonglong2(v[u].x, v[u].y ^ v[u].x);
+                }
         } else {
-            const XZ ca = t[ga.a], ua = t[ga.b];
-            const XZ cb = t[gb.a], ub = t[gb.b];
-            if (CODE == OP_CX) {
-                rd ^= ca.x & ua.y & ~(ua.x ^ ca.y);
-                t[ga.b] = make_ulonglong2(ua.x ^ ca.x, ua.y);
-                t[ga.a] = make_ulonglong2(ca.x, ca.y ^ ua.y);
-                if (two) {
-                    rd ^= cb.x & ub.y & ~(ub.x ^ cb.y);
-                    t[gb.b] = make_ulonglong2(ub.x ^ cb.x, ub.y);
-                    t[gb.a] = make_ulonglong2(cb.x, cb.y ^ ub.y);
-                }
-            } else {
-                rd ^= ca.x & ua.x & (ua.y ^ ca.y);
-                t[ga.b] = make_ulonglong2(ua.x, ua.y ^ ca.x);
-                t[ga.a] = make_ulonglong2(ca.x, ca.y ^ ua.x);
-                if (two) {
-                    rd ^= cb.x & ub.x & (ub.y ^ cb.y);
-                    t[gb.b] = make_ulonglong2(ub.x, ub.y ^ cb.x);
-                    t[gb.a] = make_ulonglong2(cb.x, cb.y ^ ub.x);
-                }
+            XZ c[GU], u2[GU];
+#pragma unroll
+            for (int u = 0; u < GU; ++u) {
+                c[u] = t[gg[u].a];
+                u2[u] = t[gg[u].b];
             }
+#pragma unroll
+            for (int u = 0; u < GU; ++u)
+                if (on[u]) {
+                    if (CODE == OP_CX) {
+                        rd ^= c[u].x & u2[u].y & ~(u2[u].x ^ c[u].y);
+                        t[gg[u].b] = make_ulonglong2(u2[u].x ^ c[u].x, u2[u].y);
+                        t[gg[u].a] = make_ulonglong2(c[u].x, c[u].y ^ u2[u].y);
+                    } else {
+                        rd ^= c[u].x & u2[u].x & (u2[u].y ^ c[u].y);
+                        t[gg[u].b] = make_ulonglong2(u2[u].x, u2[u].y ^ c[u].x);
+                        t[gg[u].a] = make_ulonglong2(c[u].x, c[u].y ^ u2[u].x);
+                    }
+                }
         }
     }
 }
@@ -220,11 +226,81 @@ __device__ __forceinline__ void apply_entry(const NoiseEntry &en, const XZ *__re
 
 constexpr int NE = 3;  // channel outcomes a lane keeps in registers (32*NE per word)
 
+// Parity of [row anticommutes with propagated Pauli pid] per shot bit, from
+// the row's final cells.
+__device__ __forceinline__ u64 prop_parity(const SegmentDev &seg, int pid, const XZ *__restrict__ t) {
+    const uint32_t desc = __ldg(seg.prop_desc + pid);
+    const uint32_t off = desc >> 8, len = desc & 255u;
+    u64 par = 0ull;
+    for (uint32_t k = 0; k < len; ++k) {
+        const uint32_t u = __ldg(seg.prop_sup + off + k);
+        const XZ v = t[u & 0xFFFFu];
+        if (u & PROP_Z) par ^= v.x;
+        if (u & PROP_X) par ^= v.y;
+    }
+    return par;
+}
+
+// Resident steps of one layer for RC register slots, CH slots at a time:
+// all partner cells of a chunk are loaded before any is written (the gates of
+// one layer act on distinct columns), so the loads overlap.
+template <int RC>
+__device__ __forceinline__ void resident_layer(const ResOp *__restrict__ ops, int lane, XZ *__restrict__ t,
+                                               u64 (&xr)[RC], u64 (&zr)[RC], u64 &rd) {
+    constexpr int CH = RC < 4 ? RC : 4;
+#pragma unroll
+    for (int j0 = 0; j0 < RC; j0 += CH) {
+        ResOp op[CH];
+        XZ v[CH];
+#pragma unroll
+        for (int u = 0; u < CH; ++u) {
+            op[u] = ops[(j0 + u) * 32 + lane];
+            v[u] = op[u].code >= RS_CX_CTRL ? t[op[u].other] : make_ulonglong2(0ull, 0ull);
+        }
+#pragma unroll
+        for (int u = 0; u < CH; ++u) {
+            const int j = j0 + u;
+            u64 &x = xr[j], &z = zr[j];
+            switch (op[u].code) {
+            case RS_H: {  // GateFunctors.hpp:90-93
+                rd ^= x & z;
+                const u64 tmp = x;
+                x = z;
+                z = tmp;
+                break;
+            }
+            case RS_S:  // :165-169
+                rd ^= x & z;
+                z ^= x;
+                break;
+            case RS_CX_CTRL:  // :248-253, resident = control
+                rd ^= x & v[u].y & ~(v[u].x ^ z);
+                t[op[u].other] = make_ulonglong2(v[u].x ^ x, v[u].y);
+                z ^= v[u].y;
+                break;
+            case RS_CX_TGT:  // resident = target
+                rd ^= v[u].x & z & ~(x ^ v[u].y);
+                t[op[u].other] = make_ulonglong2(v[u].x, v[u].y ^ z);
+                x ^= v[u].x;
+                break;
+            case RS_CZ:  // :30-35
+                rd ^= x & v[u].x & (v[u].y ^ z);
+                t[op[u].other] = make_ulonglong2(v[u].x, v[u].y ^ x);
+                z ^= v[u].x;
+                break;
+            default: break;
+            }
+        }
+    }
+}
+
 // Persistent: each CTA stages the segment's schedule and column map in shared
-// memory once, then loops over tiles (ROWS rows x BW words x nq columns).
-// Tile cells are copied with 8-byte cp.async straight into their slots (all
-// copies of a tile in flight at once), processed, and stored back.
-__global__ void __launch_bounds__(256, 3) segment_kernel(u64 *__restrict__ X, u64 *__restrict__ Z,
+// memory once, then loops over tiles (ROWS rows x BW words x nq columns):
+// stage the tile, apply the schedule (one warp per (row, word)), store back.
+// RC = 0: every gate reads and writes its cells in shared memory, channel
+// outcomes and sign ops act at their layer.  RC > 0: the resident form.
+template <int RC>
+__global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u64 *__restrict__ Z,
                                                         u64 *__restrict__ R, int64_t n, int64_t W, int64_t w,
                                                         SegmentDev seg, int rows, int bw, int64_t nchunks,
                                                         int64_t ntiles, const u64 *const *__restrict__ recs) {
@@ -239,9 +315,13 @@ __global__ void __launch_bounds__(256, 3) segment_kernel(u64 *__restrict__ X, u6
     SegGate *s_gates = reinterpret_cast<SegGate *>(s_runs + seg.nruns);
     SegSign *s_signs = reinterpret_cast<SegSign *>(s_gates + seg.ngates);
     int32_t *s_cols = reinterpret_cast<int32_t *>(s_signs + seg.nsigns);
+    const int nres_ops = RC ? seg.nlayers * RC * 32 : 0;
+    ResOp *s_resops = reinterpret_cast<ResOp *>(s_cols + nq);                   // [nlayers][RC][32]
+    uint16_t *s_rescols = reinterpret_cast<uint16_t *>(s_resops + nres_ops);    // [RC][32]
     const size_t head = ((size_t)seg.nlayers * sizeof(SegLayer) + (size_t)seg.nruns * sizeof(SegRun) +
                          (size_t)seg.ngates * sizeof(SegGate) + (size_t)seg.nsigns * sizeof(SegSign) +
-                         (size_t)nq * sizeof(int32_t) + 15) / 16 * 2;
+                         (size_t)nq * sizeof(int32_t) + (size_t)nres_ops * sizeof(ResOp) +
+                         (size_t)RC * 32 * sizeof(uint16_t) + 15) / 16 * 2;
     const u64 **s_recp = reinterpret_cast<const u64 **>(sm + head);  // [nrecsig] record pointers
     XZ *tile_xz = reinterpret_cast<XZ *>(sm + head + (seg.nrecsig + 1) / 2 * 2);  // [rows*bw][nq1]
     u64 *rtile = reinterpret_cast<u64 *>(tile_xz + (size_t)rows * bw * nq1);      // [rows*bw] r words
@@ -252,37 +332,59 @@ __global__ void __launch_bounds__(256, 3) segment_kernel(u64 *__restrict__ X, u6
     for (int i = tid; i < seg.ngates; i += T) s_gates[i] = seg.gates[i];
     for (int i = tid; i < seg.nsigns; i += T) s_signs[i] = seg.signs[i];
     for (int i = tid; i < nq; i += T) s_cols[i] = seg.cols[i];
+    for (int i = tid; i < nres_ops; i += T) s_resops[i] = seg.res_ops[i];
+    for (int i = tid; i < RC * 32; i += T) s_rescols[i] = seg.res_cols[i];
     __syncthreads();
 
     const int lane = tid & 31, wid = tid >> 5, nw = T >> 5;
-    // Load / store mapping: lane -> word kk_t = lane % bw and column slot
-    // jj = lane / bw; one warp instruction covers columns cb + c + 8*jj, which
-    // keeps the 8-byte shared-memory writes of a half-warp on distinct banks.
-    const int kk_t = lane % bw, jj = lane / bw, jn = 32 / bw;
-    const int span = 8 * jn;  // columns one warp covers in 8 instructions
+    // Staging map: lane -> word pair kp (words 2kp, 2kp+1) and column slot
+    // jl.  A lane reads the 16-byte x and z chunks of its two words (two
+    // global loads) and writes two whole {x, z} cells (two 16-byte shared
+    // stores).  A quarter-warp's 8 cells fall on distinct bank groups (the
+    // tile row stride nq1 is odd and the word offsets 2kp are even), so each
+    // store is one wavefront per quarter-warp; the loads stay coalesced.
+    const int npair = bw >= 2 ? bw / 2 : 1;          // word pairs per tile row
+    const int kp = lane % npair, jl = lane / npair;  // jl < 32 / npair
+    const int jln = 32 / npair;                      // columns per instruction
+    constexpr int SU = 4;                            // columns in flight per lane
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t row0 = (tile / nchunks) * rows;
         const int64_t k0 = (tile % nchunks) * bw;
         // ---- load
+        for (int e = tid; e < rows * bw; e += T) tile_xz[(size_t)e * nq1 + nq] = make_ulonglong2(0ull, 0ull);
         for (int r = 0; r < rows; ++r) {
             const int64_t row = row0 + r;
-            const int64_t kg = k0 + kk_t;
-            const bool ok = row < W && kg < w;
-            XZ *d = tile_xz + (size_t)(r * bw + kk_t) * nq1;
+            const int64_t kg = k0 + 2 * kp;  // first word of the lane's pair
+            const bool ok0 = row < W && kg < w, ok1 = bw >= 2 && row < W && kg + 1 < w;
+            XZ *d0 = tile_xz + (size_t)(r * bw + 2 * kp) * nq1;
+            XZ *d1 = d0 + nq1;
             const int64_t rbase = row * n * w + kg;
-            if (tid < bw) d[nq] = make_ulonglong2(0ull, 0ull);
-            for (int cb = wid * span; cb < nq; cb += nw * span)
-                for (int c = 0; c < 8; ++c) {
-                    const int l = cb + c + 8 * jj;
-                    if (l >= nq) continue;
-                    if (ok) {
+            for (int cb = wid * jln * SU; cb < nq; cb += nw * jln * SU) {
+                ulonglong2 xv[SU], zv[SU];
+#pragma unroll
+                for (int u = 0; u < SU; ++u) {
+                    const int l = cb + u * jln + jl;
+                    xv[u] = zv[u] = make_ulonglong2(0ull, 0ull);
+                    if (l < nq && ok0) {
                         const int64_t off = rbase + (int64_t)s_cols[l] * w;
-                        cp_async8(&d[l].x, X + off);
-                        cp_async8(&d[l].y, Z + off);
-                    } else {
-                        d[l] = make_ulonglong2(0ull, 0ull);
+                        if (ok1) {  // kg even and w even: 16-byte aligned
+                            xv[u] = *reinterpret_cast<const ulonglong2 *>(X + off);
+                            zv[u] = *reinterpret_cast<const ulonglong2 *>(Z + off);
+                        } else {
+                            xv[u].x = X[off];
+                            zv[u].x = Z[off];
+                        }
                     }
                 }
+#pragma unroll
+                for (int u = 0; u < SU; ++u) {
+                    const int l = cb + u * jln + jl;
+                    if (l < nq && 2 * kp < bw) {
+                        d0[l] = make_ulonglong2(xv[u].x, zv[u].x);
+                        if (bw >= 2) d1[l] = make_ulonglong2(xv[u].y, zv[u].y);
+                    }
+                }
+            }
         }
         for (int pair = tid; pair < rows * bw; pair += T) {
             const int64_t row = row0 + pair / bw, kg = k0 + pair % bw;
@@ -301,7 +403,7 @@ __global__ void __launch_bounds__(256, 3) segment_kernel(u64 *__restrict__ X, u6
             const int r = pair / bw, kk = pair % bw;
             const int64_t row = row0 + r, kg = k0 + kk;
             u64 rd = 0ull;
-            if (row < W && kg < w) {
+            if (RC == 0 && row < W && kg < w) {
                 XZ *t = tile_xz + (size_t)pair * nq1;
                 const NoiseEntry *ent = seg.entries ? seg.entries + kg * (int64_t)seg.cap : nullptr;
                 const int nent = seg.entries ? seg.entry_count[kg] : 0;
@@ -363,28 +465,90 @@ __global__ void __launch_bounds__(256, 3) segment_kernel(u64 *__restrict__ X, u6
                     __syncwarp();
                 }
             }
+            if (RC > 0 && row < W && kg < w) {
+                XZ *t = tile_xz + (size_t)pair * nq1;
+                u64 xr[RC > 0 ? RC : 1], zr[RC > 0 ? RC : 1];
+#pragma unroll
+                for (int j = 0; j < RC; ++j) {
+                    const uint16_t c = s_rescols[j * 32 + lane];
+                    const XZ v = c != 0xFFFFu ? t[c] : make_ulonglong2(0ull, 0ull);
+                    xr[j] = v.x;
+                    zr[j] = v.y;
+                }
+                for (int L = 0; L < seg.nlayers; ++L) {
+                    if constexpr (RC > 0) resident_layer<RC>(s_resops + L * RC * 32, lane, t, xr, zr, rd);
+                    const SegLayer ly = s_layers[L];
+                    for (int ri = ly.r0; ri < ly.r1; ++ri) {  // gates without resident columns
+                        const SegRun rn = s_runs[ri];
+                        switch (rn.code) {
+                        case OP_H: layer_uniform<OP_H>(s_gates, rn.g0, rn.g1, lane, t, rd); break;
+                        case OP_S: layer_uniform<OP_S>(s_gates, rn.g0, rn.g1, lane, t, rd); break;
+                        case OP_CX: layer_uniform<OP_CX>(s_gates, rn.g0, rn.g1, lane, t, rd); break;
+                        case OP_CZ: layer_uniform<OP_CZ>(s_gates, rn.g0, rn.g1, lane, t, rd); break;
+                        default:
+                            for (int g = rn.g0 + lane; g < rn.g1; g += 32) apply_gate(s_gates[g], t, rd, recs, kg);
+                        }
+                    }
+                    __syncwarp();
+                }
+#pragma unroll
+                for (int j = 0; j < RC; ++j) {
+                    const uint16_t c = s_rescols[j * 32 + lane];
+                    if (c != 0xFFFFu) t[c] = make_ulonglong2(xr[j], zr[j]);
+                }
+                __syncwarp();
+                // Sign ops and channel outcomes after the last layer, through
+                // their propagated Paulis.
+                const int nsg = seg.nsigns;
+                const NoiseEntry *ent = seg.entries ? seg.entries + kg * (int64_t)seg.cap : nullptr;
+                const int nent = seg.entries ? seg.entry_count[kg] : 0;
+                const int pbase = 4 * seg.nslots;
+                for (int it = lane; it < nsg + nent; it += 32) {
+                    if (it < nsg) {
+                        const SegSign sg = s_signs[it];
+                        const u64 m = sg.kind == SIGN_REC_X ? s_recw[kk * seg.nrecsig + sg.rec] : ~0ull;
+                        if (m) rd ^= m & prop_parity(seg, pbase + it, t);
+                    } else {
+                        const NoiseEntry e = ent[it - nsg];
+                        const int sb = 4 * e.layer;  // resident form: the channel's slot
+                        if (e.fxa) rd ^= e.fxa & prop_parity(seg, sb + 0, t);
+                        if (e.fza) rd ^= e.fza & prop_parity(seg, sb + 1, t);
+                        if (e.fxb) rd ^= e.fxb & prop_parity(seg, sb + 2, t);
+                        if (e.fzb) rd ^= e.fzb & prop_parity(seg, sb + 3, t);
+                    }
+                }
+                __syncwarp();
+            }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) rd ^= __shfl_xor_sync(0xffffffffu, rd, off);
             if (lane == 0) rtile[pair] ^= rd;
         }
         __syncthreads();
 
-        // ---- store back
+        // ---- store back (the staging map in reverse: two cells -> 16-byte x
+        // and z chunks of a word pair)
         for (int r = 0; r < rows; ++r) {
             const int64_t row = row0 + r;
-            const int64_t kg = k0 + kk_t;
+            const int64_t kg = k0 + 2 * kp;
             if (!(row < W && kg < w)) continue;
-            const XZ *d = tile_xz + (size_t)(r * bw + kk_t) * nq1;
+            const bool two = bw >= 2;
+            const XZ *d0 = tile_xz + (size_t)(r * bw + 2 * kp) * nq1;
+            const XZ *d1 = d0 + nq1;
             const int64_t rbase = row * n * w + kg;
-            for (int cb = wid * span; cb < nq; cb += nw * span)
-                for (int c = 0; c < 8; ++c) {
-                    const int l = cb + c + 8 * jj;
-                    if (l >= nq) continue;
-                    const int64_t off = rbase + (int64_t)s_cols[l] * w;
-                    const XZ v = d[l];
-                    X[off] = v.x;
-                    Z[off] = v.y;
+            for (int cb = wid * jln; cb < nq; cb += nw * jln) {
+                const int l = cb + jl;
+                if (l >= nq) continue;
+                const int64_t off = rbase + (int64_t)s_cols[l] * w;
+                const XZ a = d0[l];
+                if (two) {
+                    const XZ b = d1[l];
+                    *reinterpret_cast<ulonglong2 *>(X + off) = make_ulonglong2(a.x, b.x);
+                    *reinterpret_cast<ulonglong2 *>(Z + off) = make_ulonglong2(a.y, b.y);
+                } else {
+                    X[off] = a.x;
+                    Z[off] = a.y;
                 }
+            }
         }
         for (int pair = tid; pair < rows * bw; pair += T) {
             const int64_t row = row0 + pair / bw, kg = k0 + pair % bw;
@@ -400,10 +564,12 @@ int g_num_sms = 0;
 
 size_t segment_smem_bytes(int nq, int rows, int bw) { return (size_t)rows * bw * (2 * ((size_t)(nq + 1) | 1) + 1) * sizeof(u64); }
 
-size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int nq, int nrecsig, int rows, int bw) {
+size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int nq, int nrecsig, int rows, int bw,
+                           int rc) {
     const size_t sched = ((size_t)nlayers * sizeof(SegLayer) + (size_t)nruns * sizeof(SegRun) +
                           (size_t)ngates * sizeof(SegGate) + (size_t)nsigns * sizeof(SegSign) +
-                          (size_t)nq * sizeof(int32_t) + 15) / 16 * 16 +
+                          (size_t)nq * sizeof(int32_t) + (size_t)nlayers * rc * 32 * sizeof(ResOp) +
+                          (size_t)rc * 32 * sizeof(uint16_t) + 15) / 16 * 16 +
                          (size_t)(nrecsig + 1) / 2 * 16 + (size_t)nrecsig * bw * 8 + (size_t)rows * bw * 8;
     return segment_smem_bytes(nq, rows, bw) + sched;
 }
@@ -419,18 +585,15 @@ int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, c
     return OK;
 }
 
-int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
-                   int rows, int bw, int threads, const u64 *const *recs) {
+namespace {
+template <int RC>
+int launch_segment_rc(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
+                      int rows, int bw, int threads, const u64 *const *recs, size_t smem) {
     const int64_t W = 2 * n + 1;
     const int64_t nchunks = (w + bw - 1) / bw;
     const int64_t tiles = ((W + rows - 1) / rows) * nchunks;
-    const size_t smem =
-        segment_launch_smem(seg.nlayers, seg.nruns, seg.ngates, seg.nsigns, seg.nq, seg.nrecsig, rows, bw);
-    if (smem > kSegSmemMax) return fail(E_ARG, "segment tile does not fit in shared memory");
-    if (threads % 32 != 0 || threads > 256 || bw > 32 || 32 % bw != 0)
-        return fail(E_ARG, "segment tile: threads a multiple of 32 (at most 256), words a divisor of 32");
     {
-        const int rc = allow_max_smem((const void *)segment_kernel);
+        const int rc = allow_max_smem((const void *)segment_kernel<RC>);
         if (rc != OK) return rc;
     }
     if (g_num_sms == 0) {
@@ -439,12 +602,30 @@ int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64
         PS_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
     }
     int per_sm = 0;
-    PS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, segment_kernel, threads, smem));
+    PS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, segment_kernel<RC>, threads, smem));
     if (per_sm < 1) return fail(E_ARG, "segment kernel does not fit on an SM");
     const int64_t grid = std::min<int64_t>(tiles, (int64_t)per_sm * g_num_sms);
-    segment_kernel<<<(unsigned)grid, threads, smem, stream>>>(X, Z, R, n, W, w, seg, rows, bw, nchunks, tiles, recs);
+    segment_kernel<RC><<<(unsigned)grid, threads, smem, stream>>>(X, Z, R, n, W, w, seg, rows, bw, nchunks, tiles,
+                                                                   recs);
     PS_CUDA(cudaGetLastError());
     return OK;
+}
+}  // namespace
+
+int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
+                   int rows, int bw, int threads, const u64 *const *recs) {
+    const size_t smem = segment_launch_smem(seg.nlayers, seg.nruns, seg.ngates, seg.nsigns, seg.nq, seg.nrecsig,
+                                            rows, bw, seg.res_slots);
+    if (smem > kSegSmemMax) return fail(E_ARG, "segment tile does not fit in shared memory");
+    if (threads % 32 != 0 || threads > 256 || bw > 16 || 16 % bw != 0)
+        return fail(E_ARG, "segment tile: threads a multiple of 32 (at most 256), words a divisor of 16");
+    switch (seg.res_slots) {
+    case 0: return launch_segment_rc<0>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+    case 2: return launch_segment_rc<2>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+    case 4: return launch_segment_rc<4>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+    case 8: return launch_segment_rc<8>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+    default: return fail(E_ARG, "resident slots per lane must be 0, 2, 4 or 8");
+    }
 }
 
 }  // namespace ps

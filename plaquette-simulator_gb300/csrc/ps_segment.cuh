@@ -66,6 +66,28 @@ struct NoiseEntry {
     uint16_t b;
 };
 
+// Register-resident form of a segment.  Up to RC "resident" columns per lane
+// (no gate of the segment joins two of them) stay in registers for the whole
+// segment: the lane that owns one applies every gate on it, reading and
+// writing only the partner column in shared memory.  ResOp is the owner's
+// step for one (layer, slot): the gate code and the partner column.
+enum ResCode : uint8_t { RS_NOP = 0, RS_H = 1, RS_S = 2, RS_CX_CTRL = 3, RS_CX_TGT = 4, RS_CZ = 5 };
+struct ResOp {
+    uint16_t other;  // partner tile column (two-qubit gates)
+    uint8_t code;    // ResCode
+    uint8_t pad;
+};
+
+// In the resident form sign ops and channel outcomes act after the last
+// layer: a Pauli P applied after layer L flips the sign of exactly the rows
+// that anticommute with it, and conjugating both by the remaining gates U
+// keeps that relation, so the flip equals [row_end anticommutes with U P U^].
+// prop_desc[i] = offset << 8 | length into prop_sup; prop_sup entries are
+// column | x << 16 | z << 17 of the propagated Pauli (sign dropped).  Pauli i
+// is component c (X_a, Z_a, X_b, Z_b) of channel slot s for i = 4s + c, and
+// sign op k for i = 4 nslots + k.
+constexpr uint32_t PROP_X = 1u << 16, PROP_Z = 1u << 17;
+
 struct SegmentDev {
     const SegLayer *layers;
     int32_t nlayers;
@@ -88,6 +110,12 @@ struct SegmentDev {
     int32_t *entry_count;    // [w]
     int32_t cap;
     u64 *dense;              // [w][nslots][4] sampling scratch
+    // resident form (res_slots > 0)
+    int32_t res_slots;          // RC: register slots per lane
+    const uint16_t *res_cols;   // [RC][32] tile column, 0xFFFF = empty
+    const ResOp *res_ops;       // [nlayers][RC][32]
+    const uint32_t *prop_desc;  // [4 nslots + nsigns]
+    const uint32_t *prop_sup;
 };
 
 }  // namespace ps

@@ -22,7 +22,8 @@ from .simulator import CliffordState, _ptr
 
 class CircuitOptions(C.Structure):
     _fields_ = [("mode", C.c_int32), ("use_graph", C.c_int32), ("seg_rows", C.c_int32),
-                ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32)]
+                ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32),
+                ("seg_resident", C.c_int32)]
 
 
 class CircuitStats(C.Structure):
@@ -30,7 +31,8 @@ class CircuitStats(C.Structure):
                 ("num_channels", C.c_uint64), ("num_events", C.c_uint64), ("num_segments", C.c_uint64),
                 ("num_measure_phases", C.c_uint64), ("launches_per_run", C.c_uint64),
                 ("first_record", C.c_uint64), ("segment_bytes", C.c_double), ("seg_rows", C.c_int32),
-                ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32)]
+                ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32),
+                ("resident_segments", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -38,7 +40,8 @@ class CircuitStats(C.Structure):
 
 class CompiledCircuit:
     def __init__(self, circuit: Circuit, state: CliffordState, fused: bool = True, graph: bool = True,
-                 seg_rows: int = 0, seg_words: int = 0, seg_threads: int = 0, meas_words: int = 0):
+                 seg_rows: int = 0, seg_words: int = 0, seg_threads: int = 0, meas_words: int = 0,
+                 resident: bool = False):
         if circuit.num_qubits != state.get_num_qubits():
             raise ValueError("circuit and state have different qubit counts")
         self._L = _lib.load()
@@ -46,7 +49,8 @@ class CompiledCircuit:
         self.circuit = circuit
         self._ops = np.ascontiguousarray(circuit.op_array(), dtype=np.int32)
         self._params = np.ascontiguousarray(circuit.param_array(), dtype=np.float32)
-        opts = CircuitOptions(1 if fused else 0, 1 if graph else 0, seg_rows, seg_words, seg_threads, meas_words)
+        opts = CircuitOptions(1 if fused else 0, 1 if graph else 0, seg_rows, seg_words, seg_threads, meas_words,
+                              1 if resident else 0)
         h = C.c_void_p()
         check(self._L.ps_circuit_compile(state.handle, _ptr(self._ops), len(self._ops), _ptr(self._params),
                                          len(self._params), C.byref(opts), C.byref(h)))

@@ -129,3 +129,44 @@ def test_fused_on_host_loaded_tableau(ps, O):
     o = O.Oracle(6, B, seed=3, host=(x, z, r))
     o.run(circ.op_array(), circ.param_array())
     _check(st, o, cc.first_record, circ.num_measurements())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("meas_words", [1, 2])
+def test_d15_two_rounds_match_oracle(ps, O, meas_words):
+    """449 qubits: measurement windows of up to 16 ancilla measure+resets at
+    the end (no later segment to defer the resets into), shared-memory sizes
+    between the small and the large configurations."""
+    from plaquette_simulator import circuits as C
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ = C.surface_code_memory(15, 2, p=2e-3)
+    B = 128
+    st = ps.CliffordState(circ.num_qubits, B, 99, True)
+    cc = CompiledCircuit(circ, st, fused=True, graph=True, meas_words=meas_words)
+    cc.run()
+    st.synchronize()
+    o = O.Oracle(circ.num_qubits, B, seed=99)
+    o.run(circ.op_array(), circ.param_array())
+    _check(st, o, cc.first_record, circ.num_measurements())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["surface_d3_noisy", "surface_d5_noisy", "mixed_n40"])
+@pytest.mark.parametrize("resident", [False, True])
+def test_segment_forms_match_oracle(ps, O, name, resident):
+    """Both fused-segment forms: every gate through shared memory, and the
+    register-resident form (gate-dense columns in registers, channel
+    outcomes and sign ops through their propagated Paulis)."""
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ, B = _circuits()[name]
+    st = ps.CliffordState(circ.num_qubits, B, 123, True)
+    cc = CompiledCircuit(circ, st, fused=True, graph=True, resident=resident)
+    if resident and name.startswith("surface"):
+        assert cc.stats["resident_segments"] == cc.stats["num_segments"] > 0
+    if not resident:
+        assert cc.stats["resident_segments"] == 0
+    cc.run()
+    st.synchronize()
+    o = O.Oracle(circ.num_qubits, B, seed=123)
+    o.run(circ.op_array(), circ.param_array())
+    _check(st, o, cc.first_record, circ.num_measurements())

@@ -82,6 +82,13 @@ ps_status ps_get_seed(const ps_state *h, int64_t *out);        /* GetSeed :303  
  * the next one draws with this event index. */
 ps_status ps_get_event_counter(const ps_state *h, uint64_t *out);
 ps_status ps_set_event_counter(ps_state *h, uint64_t events);
+/* The global index of the state's first shot (a multiple of 64; default 0).
+ * Random draws are keyed by global shot, so one job's shots split over
+ * several states -- e.g. one per GPU, shots [r*S, (r+1)*S) on rank r -- give
+ * exactly the records of one state holding all of them.  No counterpart in
+ * the reference (one state per job). */
+ps_status ps_set_shot_offset(ps_state *h, uint64_t first_shot);
+ps_status ps_get_shot_offset(const ps_state *h, uint64_t *first_shot);
 
 /* ResetCliffordState (CliffordState.hpp:309-316).  Implements the intended
  * semantics (the tableau of a fresh constructor); the reference's launch
@@ -196,7 +203,7 @@ typedef struct {
     int32_t seg_rows;    /* fused tile: tableau rows per CTA (0 = auto)          */
     int32_t seg_words;   /* fused tile: 64-shot words per CTA (0 = auto)         */
     int32_t seg_threads; /* fused tile: threads per CTA (0 = auto)               */
-    int32_t meas_words;  /* measurement kernel: shot-words per CTA, 1 or 2 (0 = auto) */
+    int32_t meas_words;  /* measurement kernel: shot-words per CTA, 1, 2 or 4 (0 = auto) */
     int32_t seg_resident; /* fused segments: 1 = keep gate-dense columns in registers
                              where possible (channel outcomes and sign ops then
                              act after the last layer through propagated
@@ -374,6 +381,12 @@ ps_status ps_get_stream(const ps_state *h, void **stream);
 /* Device pointers of the packed tableau planes and their geometry (words per
  * qubit column).  For integration and benchmarking. */
 ps_status ps_get_device_tableau(const ps_state *h, void **x, void **z, void **r, uint64_t *words);
+/* Copies the packed tableau words [first_word, first_word + nwords) (shots
+ * 64*first_word ...) to host memory: x and z as [2n+1][n][nwords], r as
+ * [2n+1][nwords] uint64 (any pointer may be NULL).  For checking or
+ * snapshotting a shot range of a large state.  Waits for the stream. */
+ps_status ps_copy_tableau_words(ps_state *h, uint64_t first_word, uint64_t nwords, uint64_t *x, uint64_t *z,
+                                uint64_t *r);
 
 #ifdef __cplusplus
 }

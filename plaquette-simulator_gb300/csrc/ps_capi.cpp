@@ -190,6 +190,7 @@ ps_status ps_clone(const ps_state *o, ps_state **out) {
     ps_state *h = *out;
     h->events = o->events;
     h->valid = o->valid;
+    h->word_base = o->word_base;
     const size_t plane = (size_t)o->W * o->n * o->w * 8;
     PS_CUDA(cudaStreamSynchronize(o->stream));
     PS_CUDA(cudaMemcpyAsync(h->X, o->X, plane, cudaMemcpyDeviceToDevice, h->stream));
@@ -238,6 +239,22 @@ ps_status ps_set_event_counter(ps_state *h, uint64_t events) {
     ENTER();
     CHECK_HANDLE(h);
     h->events = events;
+    return OK;
+}
+
+ps_status ps_set_shot_offset(ps_state *h, uint64_t first_shot) {
+    ENTER();
+    CHECK_HANDLE(h);
+    if (first_shot % 64) return fail(E_ARG, "shot offset must be a multiple of 64");
+    h->word_base = (int64_t)(first_shot / 64);
+    return OK;
+}
+
+ps_status ps_get_shot_offset(const ps_state *h, uint64_t *first_shot) {
+    ENTER();
+    CHECK_HANDLE(h);
+    if (!first_shot) return fail(E_ARG, "null output pointer");
+    *first_shot = (uint64_t)h->word_base * 64;
     return OK;
 }
 
@@ -457,6 +474,23 @@ ps_status ps_get_device_tableau(const ps_state *h, void **x, void **z, void **r,
     if (z) *z = h->Z;
     if (r) *r = h->R;
     if (words) *words = (uint64_t)h->w;
+    return OK;
+}
+
+ps_status ps_copy_tableau_words(ps_state *h, uint64_t first_word, uint64_t nwords, uint64_t *x, uint64_t *z,
+                                uint64_t *r) {
+    ENTER();
+    CHECK_HANDLE(h);
+    if (first_word + nwords > (uint64_t)h->w) return fail(E_RANGE, "word range outside the state");
+    if (nwords == 0 || h->n == 0) return OK;
+    const size_t width = nwords * sizeof(u64), spitch = (size_t)h->w * sizeof(u64);
+    const size_t rows = (size_t)h->W * (size_t)h->n;
+    if (x) PS_CUDA(cudaMemcpy2DAsync(x, width, h->X + first_word, spitch, width, rows, cudaMemcpyDeviceToHost, h->stream));
+    if (z) PS_CUDA(cudaMemcpy2DAsync(z, width, h->Z + first_word, spitch, width, rows, cudaMemcpyDeviceToHost, h->stream));
+    if (r)
+        PS_CUDA(cudaMemcpy2DAsync(r, width, h->R + first_word, spitch, width, (size_t)h->W, cudaMemcpyDeviceToHost,
+                                  h->stream));
+    PS_CUDA(cudaStreamSynchronize(h->stream));
     return OK;
 }
 

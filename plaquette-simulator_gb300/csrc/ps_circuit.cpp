@@ -22,9 +22,11 @@ namespace ps {
 
 namespace {
 
-__global__ void set_params_kernel(RunParams *p, uint64_t seed, uint64_t event_base) {
+__global__ void set_params_kernel(RunParams *p, uint64_t seed, uint64_t event_base, uint64_t word_base) {
     p->seed = seed;
     p->event_base = event_base;
+    p->word_base = word_base;
+    p->pad = 0;
 }
 
 enum StepKind { K_GATE, K_CHANNEL, K_MEAS, K_SEGMENT, K_INIT };
@@ -606,7 +608,8 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
         case K_MEAS:
             rc = timed(P_MEASURE, [&] {
                 return launch_measure_list(st, h->X, h->Z, h->R, h->n, h->w, c->d_meas + s.first, s.count,
-                                           (uint64_t)h->seed, 0, c->d_params, c->opts.meas_words);
+                                           (uint64_t)h->seed, (uint64_t)h->word_base, c->d_params,
+                                           c->opts.meas_words);
             });
             break;
         case K_SEGMENT: {
@@ -670,6 +673,8 @@ RunParams begin_run(ps_circuit *c, bool reset) {
     RunParams p;
     p.seed = (uint64_t)h->seed;
     p.event_base = h->events;
+    p.word_base = (uint64_t)h->word_base;
+    p.pad = 0;
     h->events += c->num_events;
     if (reset) h->valid = true;
     return p;
@@ -728,7 +733,7 @@ int autotune(ps_circuit *c, double *tune_ms) {
         }
     }
     const cudaStream_t st = h->stream;
-    set_params_kernel<<<1, 1, 0, st>>>(c->d_params, (uint64_t)h->seed, h->events);
+    set_params_kernel<<<1, 1, 0, st>>>(c->d_params, (uint64_t)h->seed, h->events, (uint64_t)h->word_base);
     PS_CUDA(cudaGetLastError());
     auto prefix = [&](size_t upto) -> int {  // |0...0>, then steps [0, upto)
         int rc = launch_init_zero_on(st, h);
@@ -776,21 +781,36 @@ int autotune(ps_circuit *c, double *tune_ms) {
     c->opts.seg_rows = pick.rows;
     c->opts.seg_words = pick.words;
     c->opts.seg_threads = pick.threads;
-    // Measurement kernel: shot-words per CTA, on the first measurement phase.
+    // Measurement kernel: shot-words per CTA (1, 2 or 4), on the first two
+    // measurement phases (the first one after reset, one mid-circuit).
     if (m0 < c->steps.size()) {
+        size_t m1 = c->steps.size();
+        for (size_t i = m0 + 1; i < c->steps.size(); ++i)
+            if (c->steps[i].kind == K_MEAS && c->steps[i].count > 1) {
+                m1 = i;
+                break;
+            }
         float bestm = 3.0e38f;
-        for (int B = 1; B <= 2; ++B) {
-            if (B == 2 && h->w % 2) continue;
+        for (int B = 1; B <= 4; B *= 2) {
+            if (h->w % B) continue;
             c->opts.meas_words = B;
-            float ms = 0.f;
-            for (int rep = 0; rep < 2; ++rep) {
+            float total = 0.f;
+            for (int rep = 0; rep < 2; ++rep) {  // the first pass warms up
+                float ms0 = 0.f, ms1 = 0.f;
                 rc = prefix(m0);
                 if (rc != OK) return rc;
-                rc = time_it([&] { return enqueue_steps(c, st, m0, m0 + 1); }, &ms);
+                rc = time_it([&] { return enqueue_steps(c, st, m0, m0 + 1); }, &ms0);
                 if (rc != OK) return rc;
+                if (m1 < c->steps.size()) {
+                    rc = enqueue_steps(c, st, m0 + 1, m1);
+                    if (rc != OK) return rc;
+                    rc = time_it([&] { return enqueue_steps(c, st, m1, m1 + 1); }, &ms1);
+                    if (rc != OK) return rc;
+                }
+                total = ms0 + ms1;
             }
-            if (ms < bestm) {
-                bestm = ms;
+            if (total < bestm) {
+                bestm = total;
                 pick.meas_words = B;
             }
         }
@@ -1106,7 +1126,7 @@ ps_status ps_circuit_run(ps_circuit *c, int reset_state) {
     if (!c) return fail(E_ARG, "null circuit");
     ps_state *h = c->h;
     const RunParams p = begin_run(c, reset_state != 0);
-    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base);
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base, p.word_base);
     PS_CUDA(cudaGetLastError());
     if (c->exec[reset_state ? 1 : 0]) {
         PS_CUDA(cudaGraphLaunch(c->exec[reset_state ? 1 : 0], h->stream));
@@ -1121,7 +1141,7 @@ ps_status ps_circuit_profile(ps_circuit *c, int reset_state, ps_circuit_profile_
     ps_state *h = c->h;
     std::memset(out, 0, sizeof(*out));
     const RunParams p = begin_run(c, reset_state != 0);
-    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base);
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base, p.word_base);
     PS_CUDA(cudaGetLastError());
     Profiler prof;
     prof.st = h->stream;
@@ -1150,7 +1170,7 @@ ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *rand
     PS_CUDA(cudaStreamSynchronize(h->stream));
     PS_CUDA(cudaMemcpy(c->d_meas, m.data(), nm * sizeof(MeasOp), cudaMemcpyHostToDevice));
     const RunParams p = begin_run(c, reset_state != 0);
-    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base);
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base, p.word_base);
     int rc = enqueue_plan(c, h->stream, reset_state != 0);
     cudaError_t e = cudaStreamSynchronize(h->stream);
     std::vector<int32_t> host(nm * 2);

@@ -111,17 +111,19 @@ __global__ void __launch_bounds__(256) gate2_kernel(u64 *__restrict__ X, u64 *__
 // 16 threads per 64-shot word: thread `sub` computes Philox block `sub`
 // (shots 4*sub .. 4*sub+3); the four masks are OR-reduced over the 16 lanes.
 __global__ void __launch_bounds__(256) channel_sample_kernel(u64 *__restrict__ masks, int64_t w, uint64_t seed_arg,
-                                                            uint64_t event_arg, const RunParams *__restrict__ rp,
+                                                            uint64_t event_arg, uint64_t word_base_arg,
+                                                            const RunParams *__restrict__ rp,
                                                             int count, const uint64_t *__restrict__ thr) {
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t k = gt >> 4;
     const uint32_t sub = (uint32_t)(gt & 15);
     const uint64_t seed = rp ? rp->seed : seed_arg;
     const uint64_t event = (rp ? rp->event_base : 0ull) + event_arg;
+    const uint64_t word_base = rp ? rp->word_base : word_base_arg;
     u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
     if (k < w) {
         const uint64_t total = thr[count - 1];
-        const u32x4 u = draw_block(seed, event, (uint64_t)k, sub, TAG_NOISE);
+        const u32x4 u = draw_block(seed, event, word_base + (uint64_t)k, sub, TAG_NOISE);
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
             const uint64_t v = u.v[l];
@@ -200,7 +202,7 @@ int launch_gate(ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag
 
 int launch_channel_rp(cudaStream_t st, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,
                       uint32_t event_off, const RunParams *rp, u64 *masks) {
-    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, st>>>(masks, h->w, (uint64_t)h->seed, event_off, rp, count,
+    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, st>>>(masks, h->w, (uint64_t)h->seed, event_off, (uint64_t)h->word_base, rp, count,
                                                              dev_thr);
     PS_CUDA(cudaGetLastError());
     const int64_t work = h->W * (h->w >> 1);
@@ -232,7 +234,7 @@ int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thr,
     uint64_t *dthr = nullptr;
     PS_CUDA(cudaMallocAsync(&dthr, 15 * sizeof(uint64_t), h->stream));
     PS_CUDA(cudaMemcpyAsync(dthr, thr, (size_t)count * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
-    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, h->stream>>>(h->mask_buf, h->w, (uint64_t)h->seed, event,
+    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, h->stream>>>(h->mask_buf, h->w, (uint64_t)h->seed, event, (uint64_t)h->word_base,
                                                                     nullptr, count, dthr);
     PS_CUDA(cudaGetLastError());
     const int64_t work = h->W * (h->w >> 1);
@@ -317,7 +319,7 @@ int launch_pauli_channel_noalloc(ps_state *h, int64_t q, const uint64_t *thr3) {
     const uint64_t event = h->events++;
     // Thresholds travel as kernel arguments (no host copy, no allocation).
     noalloc_set_thresholds<<<1, 1, 0, h->stream>>>(thr, thr3[0], thr3[1], thr3[2]);
-    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, h->stream>>>(masks, h->w, (uint64_t)h->seed, event,
+    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, h->stream>>>(masks, h->w, (uint64_t)h->seed, event, (uint64_t)h->word_base,
                                                                         nullptr, 3, thr);
     PS_CUDA(cudaGetLastError());
     const int64_t work = h->W * (h->w >> 1);

@@ -78,6 +78,10 @@ struct ps_state {
     int64_t w = 0;      // shot-words per column (padded to even)
     int64_t seed = 0;
     uint64_t events = 0;
+    // Global index of the first 64-shot word: draws are keyed by global shot
+    // words, so shot ranges split over several states (or GPUs) reproduce
+    // the draws of one state holding all shots.
+    int64_t word_base = 0;
     u64 *X = nullptr, *Z = nullptr, *R = nullptr;
     cudaStream_t stream = nullptr;
     // Device scratch for single-op calls.
@@ -134,7 +138,7 @@ void channel_thresholds(const float *p, int count, uint64_t *thr);
 // ps_measure.cu
 struct RunParams;
 int launch_measure(ps_state *h, const MeasOp *ops_host, int nops);
-// words_per_cta: 1 or 2 shot-words per CTA, 0 = automatic.
+// words_per_cta: 1, 2 or 4 shot-words per CTA, 0 = automatic.
 int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops,
                         int nops, uint64_t seed, uint64_t word_base, const RunParams *rp, int words_per_cta = 0);
 

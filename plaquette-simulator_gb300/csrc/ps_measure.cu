@@ -61,6 +61,7 @@ struct Ctl {
     int uniform;
     int rows_done;
     int resq[NW];  // window slot -> qubit of its reset, or -1
+    MeasOp wop[NW];  // the window's measurements
 };
 // Dynamic shared memory a measurement launch may take: the opt-in maximum
 // less the kernel's static control block.
@@ -87,8 +88,9 @@ __device__ __forceinline__ void warp_phase_reduce(u64 &c1, u64 &c0, int first_of
     }
 }
 
+// k: the state's word; the draw is keyed by the global word word_base + k.
 __device__ __forceinline__ u64 outcome_bits(const MeasOp &op, int lane, uint64_t seed, uint64_t event_base,
-                                            int64_t k) {
+                                            int64_t k, uint64_t word_base) {
     u64 bits = 0ull;
     if (lane < 16) {
         if (op.forced) {
@@ -100,7 +102,8 @@ __device__ __forceinline__ u64 outcome_bits(const MeasOp &op, int lane, uint64_t
                 if (u < op.bias) bits |= 1ull << b;
             }
         } else {
-            const u32x4 u = draw_block(seed, event_base + op.event, (uint64_t)k, (uint32_t)lane, TAG_MEASURE);
+            const u32x4 u =
+                draw_block(seed, event_base + op.event, word_base + (uint64_t)k, (uint32_t)lane, TAG_MEASURE);
 #pragma unroll
             for (int l = 0; l < 4; ++l)
                 if (unit_float(u.v[l]) < op.bias) bits |= 1ull << (lane * 4 + l);
@@ -145,7 +148,7 @@ template <int B> __device__ __forceinline__ void store_cell(u64 *p, const u64 *v
 template <int B>
 __device__ int warp_scan(const u64 *X, int64_t n, int64_t w, int64_t k0, const MeasOp &op, int *klist, u64 *kmask,
                          int &kcnt_out) {
-    constexpr int U = 8;  // rows in flight per lane
+    constexpr int U = 16 / B;  // rows in flight per lane (16 words per lane)
     const int lane = threadIdx.x & 31;
     const int64_t q = op.q;
     u64 stab[B];
@@ -252,15 +255,16 @@ __device__ void warp_det_rows(u64 *X, u64 *Z, const u64 *R, int64_t n, int64_t w
         }
     if (cs == 0) wraw[slot * B + b] = racc;
     // z of the product row at the qubit of each earlier reset in the window
-    // (lane = (earlier slot, word)): a reset's X flips the sign of every row
+    // (lane = (earlier slot mod CPI, word)): a reset's X flips the sign of every row
     // with z on its qubit, so it flips this outcome where that z is set.
-    if (cs < slot && resq[cs] >= 0) {
-        const int64_t qr = resq[cs];
+    for (int rr = cs; rr < slot; rr += CPI) {
+        if (resq[rr] < 0) continue;
+        const int64_t qr = resq[rr];
         u64 zb = 0ull;
 #pragma unroll
         for (int t = 0; t < KR; ++t)
             if (t < kp) zb ^= Z[(ro[t] + qr) * w + k] & m[t];
-        wz[(slot * NW + cs) * B + b] = zb;
+        wz[(slot * NW + rr) * B + b] = zb;
     }
 }
 
@@ -629,7 +633,7 @@ __device__ void cta_det(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, int64_t k0
 // One measurement on the whole CTA (all B words).
 template <int B>
 __device__ void cta_measure(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, int64_t k0, const MeasOp &op,
-                            const Smem &s, Ctl &ctl, uint64_t seed, uint64_t event_base) {
+                            const Smem &s, Ctl &ctl, uint64_t seed, uint64_t event_base, uint64_t word_base) {
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t q = op.q;
     for (int64_t e = tid; e < 2 * n * B; e += T) {
@@ -666,7 +670,7 @@ __device__ void cta_measure(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, int64_
             }
             if (!found) break;
         }
-        const u64 bits = ng > 0 ? outcome_bits(op, lane, seed, event_base, k0 + b) : 0ull;
+        const u64 bits = ng > 0 ? outcome_bits(op, lane, seed, event_base, k0 + b, word_base) : 0ull;
         if (lane == 0) {
             ctl.ngroups[b] = ng;
             ctl.det_mask[b] = rem;
@@ -722,12 +726,14 @@ __device__ void cta_reset_flip(const u64 *Z, u64 *R, int64_t n, int64_t w, int64
 template <int B>
 __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w,
                                                             const MeasOp *__restrict__ ops, int nops,
-                                                            uint64_t seed_arg, const RunParams *__restrict__ rp,
+                                                            uint64_t seed_arg, uint64_t word_base_arg,
+                                                            const RunParams *__restrict__ rp,
                                                             int window_max) {
     extern __shared__ u64 dyn[];
     __shared__ Ctl ctl;
     const uint64_t seed = rp ? rp->seed : seed_arg;
     const uint64_t event_base = rp ? rp->event_base : 0ull;
+    const uint64_t word_base = rp ? rp->word_base : word_base_arg;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int64_t k0 = (int64_t)blockIdx.x * B;
     Smem s;
@@ -746,7 +752,7 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
         // No window: every measurement on the whole CTA (single-op launches).
         for (; pos < nops; ++pos) {
             const MeasOp op = ops[pos];
-            cta_measure<B>(X, Z, R, n, w, k0, op, s, ctl, seed, event_base);
+            cta_measure<B>(X, Z, R, n, w, k0, op, s, ctl, seed, event_base, word_base);
             if (op.reset) cta_reset_flip<B>(Z, R, n, w, k0, op);
         }
         return;
@@ -761,6 +767,7 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
             if ((tid & 31) == 0) {
                 ctl.status[warp] = st;
                 ctl.kcnt[warp] = kc;
+                ctl.wop[warp] = op;
             }
         }
         __syncthreads();
@@ -772,14 +779,14 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
         // overwrites them.
         int P = 0;
         while (P < act && ctl.status[P] != ST_OTHER) ++P;
-        if (tid < NW) ctl.resq[tid] = (tid < P && ctl.status[tid] == ST_DET_RESET) ? ops[pos + tid].q : -1;
+        if (tid < NW) ctl.resq[tid] = (tid < P && ctl.status[tid] == ST_DET_RESET) ? ctl.wop[tid].q : -1;
         __syncthreads();
         bool any_reset = false;
         for (int j = 0; j < P; ++j) any_reset |= ctl.resq[j] >= 0;
         if (warp < P) {
             warp_det<B>(X, Z, R, n, w, k0, s.klist + warp * KMAX, s.kmask + warp * KMAX * B, ctl.kcnt[warp],
                         warp == P - 1, warp, ctl.resq, s.wraw, s.wz);
-            const MeasOp op = ops[pos + warp];
+            const MeasOp &op = ctl.wop[warp];
             if (op.kstat && k0 == 0 && (tid & 31) == 0) {
                 op.kstat[0] = 0;
                 op.kstat[1] = ctl.kcnt[warp];
@@ -788,20 +795,25 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
         __syncthreads();
         if (P > 0) {
             // Outcomes in order: measurement j sees the X of every earlier
-            // reset r of the run on the shots where r's outcome is 1.
-            if (tid < B) {
+            // reset r of the run on the shots where r's outcome is 1 (a chain
+            // through shared memory, only when the run holds a reset).
+            if (any_reset && tid < B) {
                 const int b = tid;
-                const int64_t k = k0 + b;
                 for (int j = 0; j < P; ++j) {
                     u64 v = s.wraw[j * B + b];
                     for (int r = 0; r < j; ++r)
                         if (ctl.resq[r] >= 0) v ^= s.wres[r * B + b] & s.wz[(j * NW + r) * B + b];
                     s.wres[j * B + b] = v;
-                    const MeasOp op = ops[pos + j];
-                    op.res[k] = v;
-                    op.det[k] = ~0ull;
                 }
-                R[2 * n * w + k] = s.wres[(P - 1) * B + b];  // the scratch row the last measurement left
+            }
+            __syncthreads();
+            const u64 *fin = any_reset ? s.wres : s.wraw;
+            for (int e = tid; e < P * B; e += blockDim.x) {
+                const int j = e / B, b = e % B;
+                const MeasOp &op = ctl.wop[j];
+                op.res[k0 + b] = fin[j * B + b];
+                op.det[k0 + b] = ~0ull;
+                if (j == P - 1) R[2 * n * w + k0 + b] = fin[j * B + b];  // the scratch row the last one left
             }
             __syncthreads();
             if (any_reset) {
@@ -816,9 +828,9 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
                     u64 acc = 0ull;
                     if (i < 2 * n) {
                         for (int r = 0; r < P; ++r)
-                            if (ctl.resq[r] >= 0) acc ^= s.wres[r * B + b] & Z[(i * n + ctl.resq[r]) * w + k];
+                            if (ctl.resq[r] >= 0) acc ^= fin[r * B + b] & Z[(i * n + ctl.resq[r]) * w + k];
                     } else if (ctl.resq[P - 1] >= 0) {
-                        acc = s.wres[(P - 1) * B + b] & Z[(i * n + ctl.resq[P - 1]) * w + k];
+                        acc = fin[(P - 1) * B + b] & Z[(i * n + ctl.resq[P - 1]) * w + k];
                     }
                     if (acc) R[i * w + k] ^= acc;
                 }
@@ -828,7 +840,7 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
         pos += P;
         if (P < act) {
             const MeasOp op = ops[pos];
-            cta_measure<B>(X, Z, R, n, w, k0, op, s, ctl, seed, event_base);
+            cta_measure<B>(X, Z, R, n, w, k0, op, s, ctl, seed, event_base, word_base);
             if (op.reset) cta_reset_flip<B>(Z, R, n, w, k0, op);
             pos += 1;
             window = 2;
@@ -846,13 +858,14 @@ size_t smem_bytes(int64_t n, int B) {
 
 template <int B>
 int launch_b(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops, int nops,
-             uint64_t seed, const RunParams *rp, int window) {
+             uint64_t seed, uint64_t word_base, const RunParams *rp, int window) {
     const size_t smem = smem_bytes(n, B);
     if (smem + sizeof(Ctl) > 48 * 1024) {  // static and dynamic shared memory share the default limit
         const int rc = allow_max_smem((const void *)measure_kernel<B>);
         if (rc != OK) return rc;
     }
-    measure_kernel<B><<<(unsigned)(w / B), NW * 32, smem, stream>>>(X, Z, R, n, w, dev_ops, nops, seed, rp, window);
+    measure_kernel<B><<<(unsigned)(w / B), NW * 32, smem, stream>>>(X, Z, R, n, w, dev_ops, nops, seed, word_base, rp,
+                                                                    window);
     PS_CUDA(cudaGetLastError());
     return OK;
 }
@@ -867,7 +880,6 @@ int measure_words_per_cta(int64_t n, int64_t w) {
 
 int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops,
                         int nops, uint64_t seed, uint64_t word_base, const RunParams *rp, int words_per_cta) {
-    (void)word_base;
     if (nops <= 0) return OK;
     if (n > (int64_t)NW * 32 * MAXC) return fail(E_ARG, "too many qubits for the measurement kernel (max 2048)");
     // A single measurement has no window to overlap: spread it over the most
@@ -875,10 +887,12 @@ int launch_measure_list(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, 
     int B = nops == 1 ? 1 : measure_words_per_cta(n, w);
     if (nops > 1 && words_per_cta == 1) B = 1;
     if (nops > 1 && words_per_cta == 2 && w % 2 == 0 && smem_bytes(n, 2) <= kMeasSmemMax) B = 2;
+    if (nops > 1 && words_per_cta == 4 && w % 4 == 0 && smem_bytes(n, 4) <= kMeasSmemMax) B = 4;
     if (smem_bytes(n, B) > kMeasSmemMax) return fail(E_ARG, "measurement tile does not fit in shared memory");
     const int window = nops == 1 ? 0 : NW;
-    if (B == 2) return launch_b<2>(stream, X, Z, R, n, w, dev_ops, nops, seed, rp, window);
-    return launch_b<1>(stream, X, Z, R, n, w, dev_ops, nops, seed, rp, window);
+    if (B == 4) return launch_b<4>(stream, X, Z, R, n, w, dev_ops, nops, seed, word_base, rp, window);
+    if (B == 2) return launch_b<2>(stream, X, Z, R, n, w, dev_ops, nops, seed, word_base, rp, window);
+    return launch_b<1>(stream, X, Z, R, n, w, dev_ops, nops, seed, word_base, rp, window);
 }
 
 int launch_measure(ps_state *h, const MeasOp *ops_host, int nops) {
@@ -895,7 +909,8 @@ int launch_measure(ps_state *h, const MeasOp *ops_host, int nops) {
         h->meas_cap = (size_t)nops;
     }
     PS_CUDA(cudaMemcpyAsync(h->meas_buf, ops_host, (size_t)nops * sizeof(MeasOp), cudaMemcpyHostToDevice, h->stream));
-    return launch_measure_list(h->stream, h->X, h->Z, h->R, h->n, h->w, h->meas_buf, nops, (uint64_t)h->seed, 0,
+    return launch_measure_list(h->stream, h->X, h->Z, h->R, h->n, h->w, h->meas_buf, nops, (uint64_t)h->seed,
+                               (uint64_t)h->word_base,
                                nullptr);
 }
 

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(256) noise_dense_kernel(SegmentDev seg, int64_
         const NoiseSlot sl = seg.slots[s];
         const uint64_t *thr = seg.thr + sl.thr_off;
         const uint64_t total = thr[sl.count - 1];
-        const u32x4 u = draw_block(rp->seed, rp->event_base + sl.event, (uint64_t)k, sub, TAG_NOISE);
+        const u32x4 u = draw_block(rp->seed, rp->event_base + sl.event, rp->word_base + (uint64_t)k, sub, TAG_NOISE);
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
             const uint64_t v = u.v[l];

@@ -9,6 +9,8 @@ namespace ps {
 struct RunParams {
     uint64_t seed;
     uint64_t event_base;
+    uint64_t word_base;  // global index of the state's first 64-shot word
+    uint64_t pad;
 };
 
 // A gate inside a fused segment (8 bytes).  a / b are LOCAL column indices

@@ -34,6 +34,8 @@ _SIGS = {
     "ps_get_seed": (C.c_int, [_vp, _pi64]),
     "ps_get_event_counter": (C.c_int, [_vp, _pu64]),
     "ps_set_event_counter": (C.c_int, [_vp, _u64]),
+    "ps_set_shot_offset": (C.c_int, [_vp, _u64]),
+    "ps_get_shot_offset": (C.c_int, [_vp, _pu64]),
     "ps_reset": (C.c_int, [_vp]),
     "ps_checksum": (C.c_int, [_vp, _i64, _i64, _pi64]),
     "ps_device_to_host": (C.c_int, [_vp, _vp, _vp, _vp]),
@@ -86,6 +88,7 @@ _SIGS = {
     "ps_synchronize": (C.c_int, [_vp]),
     "ps_get_stream": (C.c_int, [_vp, _pp]),
     "ps_get_device_tableau": (C.c_int, [_vp, _pp, _pp, _pp, _pu64]),
+    "ps_copy_tableau_words": (C.c_int, [_vp, _u64, _u64, _vp, _vp, _vp]),
 }
 
 _lib = None

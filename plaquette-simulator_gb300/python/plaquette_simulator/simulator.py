@@ -243,5 +243,28 @@ class CliffordState:
     def event_counter(self) -> int:
         return self._get_u64("ps_get_event_counter")
 
+    def set_event_counter(self, events: int) -> None:
+        """The event index the next random op draws with (replays a run)."""
+        check(self._L.ps_set_event_counter(self._h, events))
+
+    def set_shot_offset(self, first_shot: int) -> None:
+        """This state holds shots [first_shot, first_shot + batch) of a job
+        (multiple of 64): draws are keyed by global shot, so a job split over
+        several states (one per GPU) reproduces the records of one state."""
+        check(self._L.ps_set_shot_offset(self._h, first_shot))
+
+    def shot_offset(self) -> int:
+        return self._get_u64("ps_get_shot_offset")
+
+    def tableau_words(self, first_word: int, nwords: int = 1):
+        """Packed tableau words of shots [64*first_word, 64*(first_word+nwords)):
+        x, z as [2n+1, n, nwords] and r as [2n+1, nwords] uint64."""
+        n, W = self.get_num_qubits(), 2 * self.get_num_qubits() + 1
+        x = np.zeros((W, n, nwords), np.uint64)
+        z = np.zeros_like(x)
+        r = np.zeros((W, nwords), np.uint64)
+        check(self._L.ps_copy_tableau_words(self._h, first_word, nwords, _ptr(x), _ptr(z), _ptr(r)))
+        return x, z, r
+
     def synchronize(self) -> None:
         check(self._L.ps_synchronize(self._h))

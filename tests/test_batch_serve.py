@@ -84,7 +84,7 @@ def test_batch_jobs_match_alone(ps, autotune, graph):
             assert np.array_equal(got[1], alone[k][1]), f"job {j} run {k}: determined differ"
         if autotune:
             o = b.job_options(j)
-            assert o["seg_words"] in (2, 4, 8, 16) and o["meas_words"] in (0, 1, 2)
+            assert o["seg_words"] in (1, 2, 4, 8, 16) and o["meas_words"] in (0, 1, 2, 4)
     b.close()
 
 

@@ -132,7 +132,7 @@ def test_fused_on_host_loaded_tableau(ps, O):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("meas_words", [1, 2])
+@pytest.mark.parametrize("meas_words", [1, 2, 4])
 def test_d15_two_rounds_match_oracle(ps, O, meas_words):
     """449 qubits: measurement windows of up to 16 ancilla measure+resets at
     the end (no later segment to defer the resets into), shared-memory sizes
@@ -140,7 +140,7 @@ def test_d15_two_rounds_match_oracle(ps, O, meas_words):
     from plaquette_simulator import circuits as C
     from plaquette_simulator.circuit import CompiledCircuit
     circ = C.surface_code_memory(15, 2, p=2e-3)
-    B = 128
+    B = 256
     st = ps.CliffordState(circ.num_qubits, B, 99, True)
     cc = CompiledCircuit(circ, st, fused=True, graph=True, meas_words=meas_words)
     cc.run()
@@ -168,5 +168,23 @@ def test_segment_forms_match_oracle(ps, O, name, resident):
     cc.run()
     st.synchronize()
     o = O.Oracle(circ.num_qubits, B, seed=123)
+    o.run(circ.op_array(), circ.param_array())
+    _check(st, o, cc.first_record, circ.num_measurements())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["mixed_n9", "mixed_n40", "clifford_n64", "surface_d5_noisy"])
+@pytest.mark.parametrize("meas_words", [1, 2, 4])
+def test_words_per_cta_match_oracle(ps, O, name, meas_words):
+    """The measurement kernel with 1, 2 and 4 shot-words per CTA (random
+    branches with per-shot pivots, uniform pivots, deterministic windows)."""
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ, _ = _circuits()[name]
+    B = 256 + 64 * 3  # 7 words (odd: padded to 8)
+    st = ps.CliffordState(circ.num_qubits, B, 31, True)
+    cc = CompiledCircuit(circ, st, fused=True, graph=True, meas_words=meas_words)
+    cc.run()
+    st.synchronize()
+    o = O.Oracle(circ.num_qubits, B, seed=31)
     o.run(circ.op_array(), circ.param_array())
     _check(st, o, cc.first_record, circ.num_measurements())

@@ -148,7 +148,7 @@ template <int B> __device__ __forceinline__ void store_cell(u64 *p, const u64 *v
 template <int B>
 __device__ int warp_scan(const u64 *X, int64_t n, int64_t w, int64_t k0, const MeasOp &op, int *klist, u64 *kmask,
                          int &kcnt_out) {
-    constexpr int U = 16 / B;  // rows in flight per lane (16 words per lane)
+    constexpr int U = 32 / B;  // rows in flight per lane (32 words per lane)
     const int lane = threadIdx.x & 31;
     const int64_t q = op.q;
     u64 stab[B];
@@ -271,7 +271,9 @@ __device__ void warp_det_rows(u64 *X, u64 *Z, const u64 *R, int64_t n, int64_t w
 template <int B>
 __device__ void warp_det(u64 *X, u64 *Z, const u64 *R, int64_t n, int64_t w, int64_t k0, const int *klist,
                          const u64 *kmask, int kp, bool writer, int slot, const int *resq, u64 *wraw, u64 *wz) {
-    if (kp <= 2)
+    if (kp <= 1)
+        warp_det_rows<B, 1, 16>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
+    else if (kp <= 2)
         warp_det_rows<B, 2, 8>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
     else if (kp <= 4)
         warp_det_rows<B, 4, 4>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);

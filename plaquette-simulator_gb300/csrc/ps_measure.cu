@@ -799,16 +799,18 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
             // Outcomes in order: measurement j sees the X of every earlier
             // reset r of the run on the shots where r's outcome is 1 (a chain
             // through shared memory, only when the run holds a reset).
-            if (any_reset && tid < B) {
-                const int b = tid;
-                for (int j = 0; j < P; ++j) {
-                    u64 v = s.wraw[j * B + b];
-                    for (int r = 0; r < j; ++r)
-                        if (ctl.resq[r] >= 0) v ^= s.wres[r * B + b] & s.wz[(j * NW + r) * B + b];
-                    s.wres[j * B + b] = v;
+            if (any_reset) {
+                if (tid < B) {
+                    const int b = tid;
+                    for (int j = 0; j < P; ++j) {
+                        u64 v = s.wraw[j * B + b];
+                        for (int r = 0; r < j; ++r)
+                            if (ctl.resq[r] >= 0) v ^= s.wres[r * B + b] & s.wz[(j * NW + r) * B + b];
+                        s.wres[j * B + b] = v;
+                    }
                 }
+                __syncthreads();
             }
-            __syncthreads();
             const u64 *fin = any_reset ? s.wres : s.wraw;
             for (int e = tid; e < P * B; e += blockDim.x) {
                 const int j = e / B, b = e % B;

@@ -204,10 +204,13 @@ typedef struct {
     int32_t seg_words;   /* fused tile: 64-shot words per CTA (0 = auto)         */
     int32_t seg_threads; /* fused tile: threads per CTA (0 = auto)               */
     int32_t meas_words;  /* measurement kernel: shot-words per CTA, 1, 2 or 4 (0 = auto) */
-    int32_t seg_resident; /* fused segments: 1 = keep gate-dense columns in registers
-                             where possible (channel outcomes and sign ops then
-                             act after the last layer through propagated
-                             Paulis), 0 = every gate through shared memory     */
+    int32_t seg_resident; /* fused segments: 0 = one warp per (row, shot-word),
+                             every gate through shared memory; 1 = keep
+                             gate-dense columns in registers where possible
+                             (channel outcomes and sign ops then act after the
+                             last layer through propagated Paulis); 2 = one
+                             thread per gate over all shot-words of a one-row
+                             tile                                             */
 } ps_circuit_options;
 
 typedef struct {

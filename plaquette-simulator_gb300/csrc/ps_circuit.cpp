@@ -242,7 +242,7 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
     // the side with more gate touches, else greedily by touches.
     std::vector<std::vector<SegGate>> all_gates(nl);
     for (int l = 0; l < nl; ++l) all_gates[l] = L[l].gates;
-    bool res_form = c->opts.seg_resident > 0;
+    bool res_form = c->opts.seg_resident == 1;
     std::vector<int> touches(nq, 0);
     std::vector<std::vector<int>> adj(nq);
     for (int l = 0; l < nl && res_form; ++l)
@@ -1010,6 +1010,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 return bail(E_CUDA);
             d.recsig_rec = drr;
             d.nrecsig = (int32_t)sg.recsig_rec.size();
+            d.word_vector = c->opts.seg_resident == 2 ? 1 : 0;
             if (sg.res_slots > 0) {
                 uint16_t *drc;
                 ResOp *dro;

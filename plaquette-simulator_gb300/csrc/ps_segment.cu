@@ -294,12 +294,61 @@ __device__ __forceinline__ void resident_layer(const ResOp *__restrict__ ops, in
     }
 }
 
+// Word-vector form: thread = gate, looping over the tile's PB words (tile
+// rows p = 0..PB-1): the gate is decoded once for all words, and the cell
+// loads of CH words are in flight together.  The schedule is read through L1
+// (every CTA reads the same gates), leaving shared memory to the tile.
+template <int CODE, int PB>
+__device__ __forceinline__ void gates_wv(const SegGate *__restrict__ gates, int g0, int g1, int tid, int T,
+                                         XZ *__restrict__ tile, int nq1, u64 (&rd)[PB]) {
+    constexpr int CH = PB < 4 ? PB : 4;
+    for (int g = g0 + tid; g < g1; g += T) {
+        const SegGate gg = gates[g];
+#pragma unroll
+        for (int p0 = 0; p0 < PB; p0 += CH) {
+            if (CODE == OP_H || CODE == OP_S) {
+                XZ v[CH];
+#pragma unroll
+                for (int q = 0; q < CH; ++q) v[q] = tile[(p0 + q) * nq1 + gg.a];
+#pragma unroll
+                for (int q = 0; q < CH; ++q) {
+                    rd[p0 + q] ^= v[q].x & v[q].y;
+                    tile[(p0 + q) * nq1 + gg.a] = CODE == OP_H ? make_ulonglong2(v[q].y, v[q].x)
+                                                               : make_ulonglong2(v[q].x, v[q].y ^ v[q].x);
+                }
+            } else {
+                XZ c[CH], u[CH];
+#pragma unroll
+                for (int q = 0; q < CH; ++q) {
+                    c[q] = tile[(p0 + q) * nq1 + gg.a];
+                    u[q] = tile[(p0 + q) * nq1 + gg.b];
+                }
+#pragma unroll
+                for (int q = 0; q < CH; ++q) {
+                    const int p = p0 + q;
+                    if (CODE == OP_CX) {  // GateFunctors.hpp:248-253
+                        rd[p] ^= c[q].x & u[q].y & ~(u[q].x ^ c[q].y);
+                        tile[p * nq1 + gg.b] = make_ulonglong2(u[q].x ^ c[q].x, u[q].y);
+                        tile[p * nq1 + gg.a] = make_ulonglong2(c[q].x, c[q].y ^ u[q].y);
+                    } else {  // CZ, :30-35
+                        rd[p] ^= c[q].x & u[q].x & (u[q].y ^ c[q].y);
+                        tile[p * nq1 + gg.b] = make_ulonglong2(u[q].x, u[q].y ^ c[q].x);
+                        tile[p * nq1 + gg.a] = make_ulonglong2(c[q].x, c[q].y ^ u[q].x);
+                    }
+                }
+            }
+        }
+    }
+}
+
 // Persistent: each CTA stages the segment's schedule and column map in shared
 // memory once, then loops over tiles (ROWS rows x BW words x nq columns):
 // stage the tile, apply the schedule (one warp per (row, word)), store back.
 // RC = 0: every gate reads and writes its cells in shared memory, channel
 // outcomes and sign ops act at their layer.  RC > 0: the resident form.
-template <int RC>
+// PB > 0 (RC = 0, one tile row of PB words): the word-vector form, threads
+// spread over the gates of a layer instead of warps over (row, word) pairs.
+template <int RC, int PB = 0>
 __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u64 *__restrict__ Z,
                                                         u64 *__restrict__ R, int64_t n, int64_t W, int64_t w,
                                                         SegmentDev seg, int rows, int bw, int64_t nchunks,
@@ -313,13 +362,14 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
     SegLayer *s_layers = reinterpret_cast<SegLayer *>(sm);
     SegRun *s_runs = reinterpret_cast<SegRun *>(s_layers + seg.nlayers);
     SegGate *s_gates = reinterpret_cast<SegGate *>(s_runs + seg.nruns);
-    SegSign *s_signs = reinterpret_cast<SegSign *>(s_gates + seg.ngates);
+    const int ngates_sm = PB > 0 ? 0 : seg.ngates;  // the word-vector form reads gates through L1
+    SegSign *s_signs = reinterpret_cast<SegSign *>(s_gates + ngates_sm);
     int32_t *s_cols = reinterpret_cast<int32_t *>(s_signs + seg.nsigns);
     const int nres_ops = RC ? seg.nlayers * RC * 32 : 0;
     ResOp *s_resops = reinterpret_cast<ResOp *>(s_cols + nq);                   // [nlayers][RC][32]
     uint16_t *s_rescols = reinterpret_cast<uint16_t *>(s_resops + nres_ops);    // [RC][32]
     const size_t head = ((size_t)seg.nlayers * sizeof(SegLayer) + (size_t)seg.nruns * sizeof(SegRun) +
-                         (size_t)seg.ngates * sizeof(SegGate) + (size_t)seg.nsigns * sizeof(SegSign) +
+                         (size_t)ngates_sm * sizeof(SegGate) + (size_t)seg.nsigns * sizeof(SegSign) +
                          (size_t)nq * sizeof(int32_t) + (size_t)nres_ops * sizeof(ResOp) +
                          (size_t)RC * 32 * sizeof(uint16_t) + 15) / 16 * 2;
     const u64 **s_recp = reinterpret_cast<const u64 **>(sm + head);  // [nrecsig] record pointers
@@ -329,7 +379,7 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
     for (int i = tid; i < seg.nrecsig; i += T) s_recp[i] = recs[seg.recsig_rec[i]];
     for (int i = tid; i < seg.nlayers; i += T) s_layers[i] = seg.layers[i];
     for (int i = tid; i < seg.nruns; i += T) s_runs[i] = seg.runs[i];
-    for (int i = tid; i < seg.ngates; i += T) s_gates[i] = seg.gates[i];
+    for (int i = tid; i < ngates_sm; i += T) s_gates[i] = seg.gates[i];
     for (int i = tid; i < seg.nsigns; i += T) s_signs[i] = seg.signs[i];
     for (int i = tid; i < nq; i += T) s_cols[i] = seg.cols[i];
     for (int i = tid; i < nres_ops; i += T) s_resops[i] = seg.res_ops[i];
@@ -398,6 +448,111 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
         cp_async_wait_all();
         __syncthreads();
 
+        if constexpr (PB > 0) {
+            // ---- apply the schedule: thread = gate, all PB words of the tile
+            __shared__ u64 s_rdx[PB > 0 ? PB : 1];
+            __shared__ int s_eoff[PB + 1];
+            if (tid < PB) s_rdx[tid] = 0ull;
+            if (tid == 0) {
+                int acc = 0;
+#pragma unroll
+                for (int p = 0; p < PB; ++p) {
+                    s_eoff[p] = acc;
+                    const int64_t kg = k0 + p;
+                    acc += (seg.entries && kg < w) ? seg.entry_count[kg] : 0;
+                }
+                s_eoff[PB] = acc;
+            }
+            __syncthreads();
+            const int ntot = s_eoff[PB];
+            u64 rd[PB > 0 ? PB : 1];
+#pragma unroll
+            for (int p = 0; p < PB; ++p) rd[p] = 0ull;
+            // channel outcomes of the tile's words: item i -> (word p, entry)
+            constexpr int NEI = 3;
+            NoiseEntry mine[NEI];
+            int mp[NEI];
+#pragma unroll
+            for (int u = 0; u < NEI; ++u) {
+                const int it = tid + u * T;
+                mine[u].layer = -1;
+                mp[u] = 0;
+                if (it < ntot) {
+                    int p = 0;
+                    while (p + 1 < PB && s_eoff[p + 1] <= it) ++p;
+                    mine[u] = seg.entries[(k0 + p) * (int64_t)seg.cap + (it - s_eoff[p])];
+                    mp[u] = p;
+                }
+            }
+            const bool spill = ntot > NEI * T;
+            const SegGate *__restrict__ gsched = seg.gates;
+            for (int L = 0; L < seg.nlayers; ++L) {
+                const SegLayer ly = s_layers[L];
+                for (int ri = ly.r0; ri < ly.r1; ++ri) {  // runs touch disjoint columns
+                    const SegRun rn = s_runs[ri];
+                    switch (rn.code) {
+                    case OP_H: gates_wv<OP_H, PB>(gsched, rn.g0, rn.g1, tid, T, tile_xz, nq1, rd); break;
+                    case OP_S: gates_wv<OP_S, PB>(gsched, rn.g0, rn.g1, tid, T, tile_xz, nq1, rd); break;
+                    case OP_CX: gates_wv<OP_CX, PB>(gsched, rn.g0, rn.g1, tid, T, tile_xz, nq1, rd); break;
+                    case OP_CZ: gates_wv<OP_CZ, PB>(gsched, rn.g0, rn.g1, tid, T, tile_xz, nq1, rd); break;
+                    default:
+                        for (int g = rn.g0 + tid; g < rn.g1; g += T) {
+                            const SegGate gg = gsched[g];
+#pragma unroll
+                            for (int p = 0; p < PB; ++p)
+                                if (k0 + p < w) apply_gate(gg, tile_xz + p * nq1, rd[p], recs, k0 + p);
+                        }
+                    }
+                }
+                __syncthreads();
+                // sign ops and channel outcomes after this layer's gates (reads only)
+                for (int si = ly.s0 + tid; si < ly.s1; si += T) {
+                    const SegSign sg = s_signs[si];
+#pragma unroll
+                    for (int p = 0; p < PB; ++p) {
+                        const XZ v = tile_xz[p * nq1 + sg.a];
+                        if (sg.kind == SIGN_X)
+                            rd[p] ^= v.y;
+                        else if (sg.kind == SIGN_Y)
+                            rd[p] ^= v.x ^ v.y;
+                        else if (sg.kind == SIGN_Z)
+                            rd[p] ^= v.x;
+                        else
+                            rd[p] ^= s_recw[p * seg.nrecsig + sg.rec] & v.y;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < NEI; ++u)
+                    if (mine[u].layer == L) {
+                        u64 c = 0ull;
+                        apply_entry(mine[u], tile_xz + mp[u] * nq1, c);
+                        if (c) atomicXor(&s_rdx[mp[u]], c);
+                    }
+                if (spill) {  // more outcomes than the registers hold
+                    for (int it = NEI * T + tid; it < ntot; it += T) {
+                        int p = 0;
+                        while (p + 1 < PB && s_eoff[p + 1] <= it) ++p;
+                        const NoiseEntry en = seg.entries[(k0 + p) * (int64_t)seg.cap + (it - s_eoff[p])];
+                        if (en.layer != L) continue;
+                        u64 c = 0ull;
+                        apply_entry(en, tile_xz + p * nq1, c);
+                        if (c) atomicXor(&s_rdx[p], c);
+                    }
+                }
+                __syncthreads();
+            }
+            // r: every thread's accumulators, reduced per word
+#pragma unroll
+            for (int p = 0; p < PB; ++p) {
+                u64 v = rd[p];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) v ^= __shfl_xor_sync(0xffffffffu, v, off);
+                if (lane == 0 && v) atomicXor(&s_rdx[p], v);
+            }
+            __syncthreads();
+            if (tid < PB) rtile[tid] ^= s_rdx[tid];
+            __syncthreads();
+        } else {
         // ---- apply the schedule: warp = (row, word)
         for (int pair = wid; pair < rows * bw; pair += nw) {
             const int r = pair / bw, kk = pair % bw;
@@ -525,6 +680,7 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
         }
         __syncthreads();
 
+        }
         // ---- store back (the staging map in reverse: two cells -> 16-byte x
         // and z chunks of a word pair)
         for (int r = 0; r < rows; ++r) {
@@ -586,14 +742,14 @@ int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, c
 }
 
 namespace {
-template <int RC>
+template <int RC, int PB>
 int launch_segment_rc(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
                       int rows, int bw, int threads, const u64 *const *recs, size_t smem) {
     const int64_t W = 2 * n + 1;
     const int64_t nchunks = (w + bw - 1) / bw;
     const int64_t tiles = ((W + rows - 1) / rows) * nchunks;
     {
-        const int rc = allow_max_smem((const void *)segment_kernel<RC>);
+        const int rc = allow_max_smem((const void *)segment_kernel<RC, PB>);
         if (rc != OK) return rc;
     }
     if (g_num_sms == 0) {
@@ -602,10 +758,10 @@ int launch_segment_rc(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, in
         PS_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
     }
     int per_sm = 0;
-    PS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, segment_kernel<RC>, threads, smem));
+    PS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, segment_kernel<RC, PB>, threads, smem));
     if (per_sm < 1) return fail(E_ARG, "segment kernel does not fit on an SM");
     const int64_t grid = std::min<int64_t>(tiles, (int64_t)per_sm * g_num_sms);
-    segment_kernel<RC><<<(unsigned)grid, threads, smem, stream>>>(X, Z, R, n, W, w, seg, rows, bw, nchunks, tiles,
+    segment_kernel<RC, PB><<<(unsigned)grid, threads, smem, stream>>>(X, Z, R, n, W, w, seg, rows, bw, nchunks, tiles,
                                                                    recs);
     PS_CUDA(cudaGetLastError());
     return OK;
@@ -614,16 +770,26 @@ int launch_segment_rc(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, in
 
 int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
                    int rows, int bw, int threads, const u64 *const *recs) {
-    const size_t smem = segment_launch_smem(seg.nlayers, seg.nruns, seg.ngates, seg.nsigns, seg.nq, seg.nrecsig,
-                                            rows, bw, seg.res_slots);
+    const bool wv = seg.word_vector && rows == 1 && seg.res_slots == 0;
+    const size_t smem = segment_launch_smem(seg.nlayers, seg.nruns, wv ? 0 : seg.ngates, seg.nsigns, seg.nq,
+                                            seg.nrecsig, rows, bw, seg.res_slots);
     if (smem > kSegSmemMax) return fail(E_ARG, "segment tile does not fit in shared memory");
     if (threads % 32 != 0 || threads > 256 || bw > 16 || 16 % bw != 0)
         return fail(E_ARG, "segment tile: threads a multiple of 32 (at most 256), words a divisor of 16");
     switch (seg.res_slots) {
-    case 0: return launch_segment_rc<0>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
-    case 2: return launch_segment_rc<2>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
-    case 4: return launch_segment_rc<4>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
-    case 8: return launch_segment_rc<8>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+    case 0:
+        if (seg.word_vector && rows == 1) switch (bw) {  // the word-vector form
+            case 1: return launch_segment_rc<0, 1>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+            case 2: return launch_segment_rc<0, 2>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+            case 4: return launch_segment_rc<0, 4>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+            case 8: return launch_segment_rc<0, 8>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+            case 16: return launch_segment_rc<0, 16>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+            default: break;
+            }
+        return launch_segment_rc<0, 0>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+    case 2: return launch_segment_rc<2, 0>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+    case 4: return launch_segment_rc<4, 0>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
+    case 8: return launch_segment_rc<8, 0>(stream, X, Z, R, n, w, seg, rows, bw, threads, recs, smem);
     default: return fail(E_ARG, "resident slots per lane must be 0, 2, 4 or 8");
     }
 }

@@ -113,6 +113,7 @@ struct SegmentDev {
     int32_t cap;
     u64 *dense;              // [w][nslots][4] sampling scratch
     // resident form (res_slots > 0)
+    int32_t word_vector;        // 1: word-vector form for one-row tiles
     int32_t res_slots;          // RC: register slots per lane
     const uint16_t *res_cols;   // [RC][32] tile column, 0xFFFF = empty
     const ResOp *res_ops;       // [nlayers][RC][32]

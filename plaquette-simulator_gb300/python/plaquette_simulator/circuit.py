@@ -41,7 +41,7 @@ class CircuitStats(C.Structure):
 class CompiledCircuit:
     def __init__(self, circuit: Circuit, state: CliffordState, fused: bool = True, graph: bool = True,
                  seg_rows: int = 0, seg_words: int = 0, seg_threads: int = 0, meas_words: int = 0,
-                 resident: bool = False):
+                 resident: bool = False, word_vector: bool = False):
         if circuit.num_qubits != state.get_num_qubits():
             raise ValueError("circuit and state have different qubit counts")
         self._L = _lib.load()
@@ -50,7 +50,7 @@ class CompiledCircuit:
         self._ops = np.ascontiguousarray(circuit.op_array(), dtype=np.int32)
         self._params = np.ascontiguousarray(circuit.param_array(), dtype=np.float32)
         opts = CircuitOptions(1 if fused else 0, 1 if graph else 0, seg_rows, seg_words, seg_threads, meas_words,
-                              1 if resident else 0)
+                              2 if word_vector else (1 if resident else 0))
         h = C.c_void_p()
         check(self._L.ps_circuit_compile(state.handle, _ptr(self._ops), len(self._ops), _ptr(self._params),
                                          len(self._params), C.byref(opts), C.byref(h)))

@@ -152,18 +152,24 @@ def test_d15_two_rounds_match_oracle(ps, O, meas_words):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["surface_d3_noisy", "surface_d5_noisy", "mixed_n40"])
-@pytest.mark.parametrize("resident", [False, True])
-def test_segment_forms_match_oracle(ps, O, name, resident):
-    """Both fused-segment forms: every gate through shared memory, and the
-    register-resident form (gate-dense columns in registers, channel
-    outcomes and sign ops through their propagated Paulis)."""
+@pytest.mark.parametrize("form,words", [("warp", 8), ("resident", 8), ("word", 1), ("word", 2), ("word", 4),
+                                        ("word", 8), ("word", 16)])
+def test_segment_forms_match_oracle(ps, O, name, form, words):
+    """Every fused-segment form: one warp per (row, word) with every gate
+    through shared memory; the register-resident form (gate-dense columns in
+    registers, channel outcomes and sign ops through their propagated
+    Paulis); the word-vector form (one thread per gate over all words of a
+    one-row tile)."""
     from plaquette_simulator.circuit import CompiledCircuit
     circ, B = _circuits()[name]
+    B = max(B, 64 * words + 5)
     st = ps.CliffordState(circ.num_qubits, B, 123, True)
-    cc = CompiledCircuit(circ, st, fused=True, graph=True, resident=resident)
-    if resident and name.startswith("surface"):
+    cc = CompiledCircuit(circ, st, fused=True, graph=True, resident=form == "resident",
+                         word_vector=form == "word", seg_rows=1, seg_words=words,
+                         seg_threads=256 if words >= 4 else 64)
+    if form == "resident" and name.startswith("surface"):
         assert cc.stats["resident_segments"] == cc.stats["num_segments"] > 0
-    if not resident:
+    if form != "resident":
         assert cc.stats["resident_segments"] == 0
     cc.run()
     st.synchronize()

@@ -385,14 +385,12 @@ def main():
     dom_bytes = seg_bytes if dom == "segment" else meas_bytes
     dom_ms = prof[dom]["ms"]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    # DRAM bytes per segment launch from one ncu capture of the d=15 circuit at
+    # 32 shot-words (profiles/dram_traffic_surface_d15_s2048.md: 207.1 MB read
+    # + 147.9 MB written), scaled by shot-words; traffic grows with the words.
     traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            tr = json.load(f)
-        if args.workload in tr and dom in tr[args.workload]:
-            traffic = tr[args.workload][dom]
-    except (OSError, ValueError):
-        pass
+    if dom == "segment" and meta["distance"] == 15:
+        traffic = (207.1e6 + 147.9e6) / 32 * w_words
     roofline = {"bound": "hbm", "kernel": "segment_kernel" if dom == "segment" else "measure_kernel",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",

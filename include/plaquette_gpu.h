@@ -258,6 +258,15 @@ ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *rand
  * host memory: num_measurements rows of `words` uint64 each (bit s of word
  * k = shot 64k+s).  Either pointer may be NULL.  Waits for the stream. */
 ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *determined, uint64_t *words);
+/* Detectors and observables, computed on the device from the last run's
+ * records (no counterpart in the reference, whose callers read records one
+ * shot at a time with GetMeasurement): output row d is the XOR of the
+ * result rows of the circuit's measurements idx[off[d]] .. idx[off[d+1]-1]
+ * (indices in program order, off[0] = 0), for every shot.  out receives
+ * ndet rows of `words` uint64 (bit s of word k = shot 64k+s).  Waits for the
+ * stream. */
+ps_status ps_circuit_detectors(ps_circuit *c, const uint32_t *idx, const uint64_t *off, uint64_t ndet,
+                               uint64_t *out);
 
 /* The project's autotuner (no counterpart in the reference): times the
  * fused-segment tile shapes (rows x shot-words x threads) on the circuit's

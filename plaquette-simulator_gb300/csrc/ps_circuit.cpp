@@ -22,6 +22,19 @@ namespace ps {
 
 namespace {
 
+// Detector d, word k: XOR of the records idx[off[d] .. off[d+1]) (coalesced
+// over words).
+__global__ void detector_kernel(const u64 *__restrict__ res, int64_t w, const uint32_t *__restrict__ idx,
+                                const uint64_t *__restrict__ off, int64_t ndet, u64 *__restrict__ out) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ndet * w;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t d = e / w, k = e - d * w;
+        u64 v = 0ull;
+        for (uint64_t j = off[d]; j < off[d + 1]; ++j) v ^= res[(int64_t)idx[j] * w + k];
+        out[e] = v;
+    }
+}
+
 __global__ void set_params_kernel(RunParams *p, uint64_t seed, uint64_t event_base, uint64_t word_base) {
     p->seed = seed;
     p->event_base = event_base;
@@ -1218,6 +1231,53 @@ ps_status ps_circuit_autotune(ps_circuit *c, ps_circuit_options *chosen, double 
         }
     }
     if (chosen) *chosen = c->opts;
+    return OK;
+}
+
+ps_status ps_circuit_detectors(ps_circuit *c, const uint32_t *idx, const uint64_t *off, uint64_t ndet,
+                               uint64_t *out) {
+    ps_enter(__func__, __LINE__);
+    if (!c || (ndet && (!idx || !off || !out))) return fail(E_ARG, "null argument");
+    if (ndet == 0) return OK;
+    ps_state *h = c->h;
+    const uint64_t nm = c->rec_ids.size();
+    if (off[0] != 0) return fail(E_ARG, "detector offsets must start at 0");
+    for (uint64_t d = 0; d < ndet; ++d)
+        if (off[d + 1] < off[d]) return fail(E_ARG, "detector offsets must not decrease");
+    const uint64_t nidx = off[ndet];
+    for (uint64_t j = 0; j < nidx; ++j)
+        if (idx[j] >= nm) return fail(E_RANGE, "detector refers to measurement " + std::to_string(idx[j]) +
+                                                   " of a circuit with " + std::to_string(nm));
+    void *d_idx = nullptr, *d_off = nullptr, *d_out = nullptr;
+    const size_t out_bytes = (size_t)ndet * (size_t)h->w * sizeof(u64);
+    int rc = dev_alloc(h, &d_idx, std::max<uint64_t>(1, nidx) * sizeof(uint32_t));
+    if (rc == OK) rc = dev_alloc(h, &d_off, (ndet + 1) * sizeof(uint64_t));
+    if (rc == OK) rc = dev_alloc(h, &d_out, out_bytes);
+    auto cleanup = [&] {
+        cudaStreamSynchronize(h->stream);
+        dev_free(h, d_idx);
+        dev_free(h, d_off);
+        dev_free(h, d_out);
+    };
+    if (rc != OK) {
+        cleanup();
+        return rc;
+    }
+    cudaError_t e = cudaSuccess;
+    if (nidx) e = cudaMemcpyAsync(d_idx, idx, nidx * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_off, off, (ndet + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) {
+        const int64_t work = (int64_t)ndet * h->w;
+        const int blocks = (int)std::min<int64_t>((work + 255) / 256, 152 * 16);
+        detector_kernel<<<blocks, 256, 0, h->stream>>>(c->d_res_block, h->w, (const uint32_t *)d_idx,
+                                                        (const uint64_t *)d_off, (int64_t)ndet, (u64 *)d_out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(e, "detectors");
     return OK;
 }
 

@@ -143,6 +143,22 @@ class CompiledCircuit:
         check(self._L.ps_circuit_copy_records(self._handle, _ptr(results), _ptr(determined), C.byref(words)))
         return words.value
 
+    def detectors(self, definitions) -> np.ndarray:
+        """XOR of measurement records per detector, computed on the device:
+        definitions is a list of lists of measurement indices (program
+        order); returns [len(definitions), words] uint64 (bit s of word k =
+        shot 64k+s)."""
+        defs = [list(d) for d in definitions]
+        off = np.zeros(len(defs) + 1, np.uint64)
+        off[1:] = np.cumsum([len(d) for d in defs])
+        idx = np.ascontiguousarray(np.concatenate([np.asarray(d, np.uint32) for d in defs])
+                                   if defs and off[-1] else np.zeros(1, np.uint32), dtype=np.uint32)
+        w = ((self.state.get_batch_size() + 63) // 64 + 1) & ~1
+        out = np.zeros((len(defs), w), np.uint64)
+        if defs:
+            check(self._L.ps_circuit_detectors(self._handle, _ptr(idx), _ptr(off), len(defs), _ptr(out)))
+        return out
+
     def records(self):
         """(results, determined) int32 arrays [num_measurements, batch]."""
         self.state.synchronize()

@@ -356,6 +356,40 @@ def surface_code_memory(d: int, rounds: int | None = None, p: float = 1e-3) -> C
     return c
 
 
+def surface_code_detectors(d: int, rounds: int | None = None):
+    """Detectors and the logical observable of ``surface_code_memory(d,
+    rounds)`` as lists of measurement indices (its record order: per round M
+    then R of every ancilla, x_anc before z_anc; then M of every data qubit).
+
+    Detectors: each Z-ancilla's round-1 outcome (fixed by |0...0>); every
+    ancilla's outcome XOR its previous round's (rounds 2..); each Z-stabilizer
+    rebuilt from the final data outcomes XOR its last ancilla outcome.  The
+    observable is logical Z: the data qubits of the first row (y = 1), which
+    meets every X-plaquette in 0 or 2 qubits.  Without noise every detector
+    and the observable are 0 on every shot."""
+    lay = surface_code_layout(d)
+    rounds = d if rounds is None else rounds
+    anc = lay.x_anc + lay.z_anc
+    na = len(anc)
+    nx = len(lay.x_anc)
+
+    def m_anc(r, i):  # M of ancilla i in round r
+        return r * 2 * na + i
+
+    dpos = {p: k for k, p in enumerate(lay.data)}
+    final = rounds * 2 * na
+    dets = [[m_anc(0, i)] for i in range(nx, na)]
+    for r in range(1, rounds):
+        dets += [[m_anc(r, i), m_anc(r - 1, i)] for i in range(na)]
+    for i in range(nx, na):
+        ax, ay = anc[i]
+        sup = [final + dpos[(ax + dx, ay + dy)] for dx, dy in ((1, 1), (1, -1), (-1, 1), (-1, -1))
+               if (ax + dx, ay + dy) in dpos]
+        dets.append(sup + [m_anc(rounds - 1, i)])
+    observable = [final + dpos[(x, y)] for (x, y) in lay.data if y == 1]
+    return dets, observable
+
+
 def layered_circuit(width: int, depth: int, seed: int) -> Circuit:
     """Layers of one Pauli on every qubit, a ring of CX or CZ, then M on every
     qubit -- the shape of the reference's small benchmark circuits

@@ -62,6 +62,8 @@ struct Ctl {
     int rows_done;
     int resq[NW];  // window slot -> qubit of its reset, or -1
     MeasOp wop[NW];  // the window's measurements
+    int miss[NW];    // the slot scanned its column (not found in the scan cache)
+    int epoch;       // scan-cache epoch: advanced by every measurement on the CTA-wide path
 };
 // Dynamic shared memory a measurement launch may take: the opt-in maximum
 // less the kernel's static control block.
@@ -78,6 +80,13 @@ struct Smem {
     u64 *wraw;     // [NW][B] window outcomes before reset corrections
     u64 *wres;     // [NW][B] window outcomes
     u64 *wz;       // [NW][NW][B] z of measurement j's product row at reset r's qubit
+    // Scan cache (optional): per qubit, the last deterministic scan of its
+    // column -- rows to multiply and their per-word masks -- valid while its
+    // tag equals the epoch.  Deterministic measurements and resets leave x
+    // and z of rows < 2n unchanged, so a scan stays valid until a measurement
+    // runs on the CTA-wide path (a random one rewrites rows).
+    u64 *ckmask;   // [n][KMAX][B]
+    int *cmeta;    // [n][2 + KMAX]: tag, row count, rows
 };
 
 __device__ __forceinline__ void warp_phase_reduce(u64 &c1, u64 &c0, int first_offset) {
@@ -730,7 +739,7 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
                                                             const MeasOp *__restrict__ ops, int nops,
                                                             uint64_t seed_arg, uint64_t word_base_arg,
                                                             const RunParams *__restrict__ rp,
-                                                            int window_max) {
+                                                            int window_max, int use_cache) {
     extern __shared__ u64 dyn[];
     __shared__ Ctl ctl;
     const uint64_t seed = rp ? rp->seed : seed_arg;
@@ -746,8 +755,11 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
     s.wraw = s.kmask + NW * KMAX * B;
     s.wres = s.wraw + NW * B;
     s.wz = s.wres + NW * B;
-    s.rowlist = reinterpret_cast<int *>(s.wz + NW * NW * B);
+    s.ckmask = s.wz + NW * NW * B;
+    s.rowlist = reinterpret_cast<int *>(s.ckmask + (use_cache ? n * KMAX * B : 0));
     s.klist = s.rowlist + 2 * n;
+    s.cmeta = s.klist + NW * KMAX;
+    constexpr int CM = 2 + KMAX;  // ints per qubit in cmeta
 
     int pos = 0;
     if (window_max <= 0) {
@@ -759,20 +771,51 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
         }
         return;
     }
+    if (use_cache) {
+        for (int64_t q = tid; q < n; q += blockDim.x) s.cmeta[q * CM] = -1;
+        if (tid == 0) ctl.epoch = 0;
+        __syncthreads();
+    }
     int window = window_max > NW ? NW : window_max;
     while (pos < nops) {
         const int act = min(window, nops - pos);
         if (warp < act) {
+            const int lane = tid & 31;
             const MeasOp op = ops[pos + warp];
-            int kc = 0;
-            const int st = warp_scan<B>(X, n, w, k0, op, s.klist + warp * KMAX, s.kmask + warp * KMAX * B, kc);
-            if ((tid & 31) == 0) {
+            int kc = 0, st;
+            const int *cm = use_cache ? s.cmeta + (int64_t)op.q * CM : nullptr;
+            const bool hit = use_cache && cm[0] == ctl.epoch;
+            if (hit) {  // the column's rows are still the ones a scan found
+                kc = cm[1];
+                if (lane < KMAX) s.klist[warp * KMAX + lane] = cm[2 + lane];
+                if (lane < KMAX * B) s.kmask[warp * KMAX * B + lane] = s.ckmask[(int64_t)op.q * KMAX * B + lane];
+                st = op.reset ? ST_DET_RESET : ST_DET;
+                __syncwarp();
+            } else {
+                st = warp_scan<B>(X, n, w, k0, op, s.klist + warp * KMAX, s.kmask + warp * KMAX * B, kc);
+            }
+            if (lane == 0) {
                 ctl.status[warp] = st;
                 ctl.kcnt[warp] = kc;
                 ctl.wop[warp] = op;
+                ctl.miss[warp] = !hit;
             }
         }
         __syncthreads();
+        // Fresh deterministic scans into the cache (read from the next
+        // window on, after the barriers that follow).
+        if (use_cache && warp < act && ctl.miss[warp] && ctl.status[warp] != ST_OTHER) {
+            const int lane = tid & 31;
+            const int64_t q = ctl.wop[warp].q;
+            int *cm = s.cmeta + q * CM;
+            if (lane < KMAX) cm[2 + lane] = s.klist[warp * KMAX + lane];
+            if (lane < KMAX * B) s.ckmask[q * KMAX * B + lane] = s.kmask[warp * KMAX * B + lane];
+            __syncwarp();
+            if (lane == 0) {
+                cm[1] = ctl.kcnt[warp];
+                cm[0] = ctl.epoch;
+            }
+        }
         // Leading run of deterministic measurements, resets included: a
         // reset's X only flips signs (rows < 2n keep their x and z), so the
         // later measurements of the run stay deterministic with the same rows;
@@ -844,6 +887,7 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
         pos += P;
         if (P < act) {
             const MeasOp op = ops[pos];
+            if (use_cache && tid == 0) ctl.epoch++;  // rows may change: every cached scan is stale
             cta_measure<B>(X, Z, R, n, w, k0, op, s, ctl, seed, event_base, word_base);
             if (op.reset) cta_reset_flip<B>(Z, R, n, w, k0, op);
             pos += 1;
@@ -854,22 +898,25 @@ __global__ void __launch_bounds__(NW * 32, 1) measure_kernel(u64 *X, u64 *Z, u64
     }
 }
 
-size_t smem_bytes(int64_t n, int B) {
-    return (size_t)(2 * n * B + 2 * n * B + STEP_CHUNK * NW * 2 + NW * KMAX * B + 2 * NW * B + NW * NW * B) *
+size_t smem_bytes(int64_t n, int B, bool cache = false) {
+    return (size_t)(2 * n * B + 2 * n * B + STEP_CHUNK * NW * 2 + NW * KMAX * B + 2 * NW * B + NW * NW * B +
+                    (cache ? n * KMAX * B : 0)) *
                sizeof(u64) +
-           (size_t)(2 * n + NW * KMAX) * sizeof(int);
+           (size_t)(2 * n + NW * KMAX + (cache ? n * (2 + KMAX) : 0)) * sizeof(int);
 }
 
 template <int B>
 int launch_b(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const MeasOp *dev_ops, int nops,
              uint64_t seed, uint64_t word_base, const RunParams *rp, int window) {
-    const size_t smem = smem_bytes(n, B);
+    // The scan cache when the window path runs and it fits.
+    const int cache = window > 0 && smem_bytes(n, B, true) <= kMeasSmemMax ? 1 : 0;
+    const size_t smem = smem_bytes(n, B, cache != 0);
     if (smem + sizeof(Ctl) > 48 * 1024) {  // static and dynamic shared memory share the default limit
         const int rc = allow_max_smem((const void *)measure_kernel<B>);
         if (rc != OK) return rc;
     }
     measure_kernel<B><<<(unsigned)(w / B), NW * 32, smem, stream>>>(X, Z, R, n, w, dev_ops, nops, seed, word_base, rp,
-                                                                    window);
+                                                                    window, cache);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

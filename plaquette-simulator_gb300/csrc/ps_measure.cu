@@ -444,24 +444,56 @@ __device__ void cta_uniform_random(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w,
     const int64_t p = ctl.gp[0][0];
     const int64_t q = op.q;
     u64 *prow_x = s.prow, *prow_z = s.prow + n * B;
-    for (int64_t e = tid; e < n * B; e += T) {
-        const int64_t j = e / B;
-        const int bb = (int)(e % B);
-        prow_x[e] = X[((p + n) * n + j) * w + k0 + bb];
-        prow_z[e] = Z[((p + n) * n + j) * w + k0 + bb];
+    constexpr int CB = 2;  // cells in flight per thread
+    for (int64_t e0 = tid; e0 < n * B; e0 += (int64_t)CB * T) {
+        u64 vx[CB], vz[CB];
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            const int64_t e = e0 + (int64_t)c * T;
+            const bool ok = e < n * B;
+            const int64_t o2 = ((p + n) * n + e / B) * w + k0 + e % B;
+            vx[c] = ok ? X[o2] : 0ull;
+            vz[c] = ok ? Z[o2] : 0ull;
+        }
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            const int64_t e = e0 + (int64_t)c * T;
+            if (e < n * B) {
+                prow_x[e] = vx[c];
+                prow_z[e] = vz[c];
+            }
+        }
     }
     if (tid < B) ctl.pr[tid] = R[(p + n) * w + k0 + tid];
     if (tid == 0) ctl.cnt = 0;
     __syncthreads();
-    for (int64_t e = tid; e < n * B; e += T) {
-        const int64_t j = e / B;
-        const int bb = (int)(e % B);
-        const u64 mm = ctl.gm[bb][0];
-        const int64_t o = (p * n + j) * w + k0 + bb, o2 = ((p + n) * n + j) * w + k0 + bb;
-        X[o] = (X[o] & ~mm) | (prow_x[e] & mm);
-        Z[o] = (Z[o] & ~mm) | (prow_z[e] & mm);
-        X[o2] &= ~mm;
-        Z[o2] = (Z[o2] & ~mm) | (j == q ? mm : 0ull);
+    // row p := old row p+n, row p+n := Z_q (masked to the shots of the pivot)
+    for (int64_t e0 = tid; e0 < n * B; e0 += (int64_t)CB * T) {
+        u64 xo[CB], zo[CB], xo2[CB], zo2[CB];
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            const int64_t e = e0 + (int64_t)c * T;
+            const bool ok = e < n * B;
+            const int64_t j = e / B, kk = k0 + e % B;
+            const int64_t o = (p * n + j) * w + kk, o2 = ((p + n) * n + j) * w + kk;
+            xo[c] = ok ? X[o] : 0ull;
+            zo[c] = ok ? Z[o] : 0ull;
+            xo2[c] = ok ? X[o2] : 0ull;
+            zo2[c] = ok ? Z[o2] : 0ull;
+        }
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            const int64_t e = e0 + (int64_t)c * T;
+            if (e >= n * B) continue;
+            const int64_t j = e / B;
+            const int bb = (int)(e % B);
+            const u64 mm = ctl.gm[bb][0];
+            const int64_t o = (p * n + j) * w + k0 + bb, o2 = ((p + n) * n + j) * w + k0 + bb;
+            X[o] = (xo[c] & ~mm) | (prow_x[e] & mm);
+            Z[o] = (zo[c] & ~mm) | (prow_z[e] & mm);
+            X[o2] = xo2[c] & ~mm;
+            Z[o2] = (zo2[c] & ~mm) | (j == q ? mm : 0ull);
+        }
     }
     if (tid < B) {
         const int bb = tid;
@@ -647,10 +679,22 @@ __device__ void cta_measure(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, int64_
                             const Smem &s, Ctl &ctl, uint64_t seed, uint64_t event_base, uint64_t word_base) {
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t q = op.q;
-    for (int64_t e = tid; e < 2 * n * B; e += T) {
-        const int64_t i = e / B;
-        const int bb = (int)(e % B);
-        s.col[e] = X[(i * n + q) * w + k0 + bb];
+    {
+        // column q of all 2n rows, CB loads in flight per thread
+        constexpr int CB = 4;
+        for (int64_t e0 = tid; e0 < 2 * n * B; e0 += (int64_t)CB * T) {
+            u64 v[CB];
+#pragma unroll
+            for (int c = 0; c < CB; ++c) {
+                const int64_t e = e0 + (int64_t)c * T;
+                v[c] = e < 2 * n * B ? X[((e / B) * n + q) * w + k0 + (e % B)] : 0ull;
+            }
+#pragma unroll
+            for (int c = 0; c < CB; ++c) {
+                const int64_t e = e0 + (int64_t)c * T;
+                if (e < 2 * n * B) s.col[e] = v[c];
+            }
+        }
     }
     if (tid == 0) ctl.rows_done = 0;
     __syncthreads();

@@ -527,7 +527,7 @@ __device__ void cta_uniform_random(u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w,
             const u64 mi = s.col[i * B + b] & mw;
             const int64_t jb = (int64_t)sl * slice_len, je = min(n, jb + slice_len);
             u64 c1 = 0ull, c0 = 0ull;
-            constexpr int UR = 4;
+            constexpr int UR = 8;
             for (int64_t j0 = jb + cs; j0 < je; j0 += (int64_t)CPI * UR) {
                 u64 xi[UR], zi[UR];
 #pragma unroll

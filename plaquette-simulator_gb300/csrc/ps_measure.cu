@@ -281,13 +281,13 @@ template <int B>
 __device__ void warp_det(u64 *X, u64 *Z, const u64 *R, int64_t n, int64_t w, int64_t k0, const int *klist,
                          const u64 *kmask, int kp, bool writer, int slot, const int *resq, u64 *wraw, u64 *wz) {
     if (kp <= 1)
-        warp_det_rows<B, 1, 16>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
+        warp_det_rows<B, 1, 8>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
     else if (kp <= 2)
-        warp_det_rows<B, 2, 8>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
+        warp_det_rows<B, 2, 4>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
     else if (kp <= 4)
-        warp_det_rows<B, 4, 4>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
+        warp_det_rows<B, 4, 2>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
     else
-        warp_det_rows<B, KMAX, 2>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
+        warp_det_rows<B, KMAX, 1>(X, Z, R, n, w, k0, klist, kmask, kp, writer, slot, resq, wraw, wz);
 }
 
 // ---------------------------------------------------------------------------

@@ -125,48 +125,86 @@ bool is_sign(int32_t c) { return c == OP_X || c == OP_Y || c == OP_Z; }
 bool is_meas(int32_t c) { return c == OP_M || c == OP_R; }
 bool is_channel(int32_t c) { return c == OP_PAULI1 || c == OP_PAULI2; }
 
-// Splits gates (all of one code) into groups of 8 lanes whose columns have
-// distinct residues mod 8 -- the shared-memory bank group of a 16-byte tile
-// cell -- for a and, for two-qubit gates, for b.  Each group is a matching in
-// the 8x8 residue graph (Kuhn's augmenting paths).  Returns the groups.
-std::vector<std::vector<SegGate>> bank_groups(const std::vector<SegGate> &gs, bool two) {
-    std::vector<SegGate> bucket[8][8];
-    size_t left = gs.size();
-    for (const SegGate &g : gs) bucket[g.a & 7][two ? (g.b & 7) : 0].push_back(g);
-    std::vector<std::vector<SegGate>> out;
-    while (left) {
-        std::vector<SegGate> grp;
-        if (!two) {
-            for (int ra = 0; ra < 8; ++ra)
-                if (!bucket[ra][0].empty()) {
-                    grp.push_back(bucket[ra][0].back());
-                    bucket[ra][0].pop_back();
-                }
-        } else {
-            int match_b[8];
-            for (int k = 0; k < 8; ++k) match_b[k] = -1;
-            std::function<bool(int, bool *)> try_a = [&](int a, bool *seen) -> bool {
+// The dummy column of residue r (kSegDummyCols zero columns follow the nq
+// columns of every tile row, one per bank group): a pad lane of a gate group
+// touches the dummy of a residue no other lane of its group uses.
+inline uint16_t dummy_col(int nq, int r) { return (uint16_t)(nq + ((r - nq) % 8 + 8) % 8); }
+
+// Lane groups needed by a run of gates of one code: a 16-byte shared-memory
+// access is served 8 lanes at a time (8 cells x 16 B = one 128-byte bank
+// row), so every group of 8 lanes needs distinct residues mod 8 -- the bank
+// group of a tile cell -- on a and, for two-qubit gates, on b.  Gates are the
+// edges of a bipartite multigraph on 8 + 8 residues and a group is a matching,
+// so the fewest groups is the largest residue degree (Koenig's edge-colouring
+// theorem).
+int lane_groups_needed(const std::vector<SegGate> &gs, bool two) {
+    int da[8] = {0, 0, 0, 0, 0, 0, 0, 0}, db[8] = {0, 0, 0, 0, 0, 0, 0, 0}, D = 0;
+    for (const SegGate &g : gs) {
+        D = std::max(D, ++da[g.a & 7]);
+        if (two) D = std::max(D, ++db[g.b & 7]);
+    }
+    return D;
+}
+
+// Splits gates (all of one code) into exactly that many groups of 8 lanes:
+// the residue multigraph is padded with dummy edges to a D-regular one, whose
+// D perfect matchings (Kuhn's augmenting paths; Hall's condition holds in a
+// regular bipartite multigraph) are the groups.  Dummy edges become pad lanes
+// on the dummy columns of their residues.
+std::vector<std::vector<SegGate>> lane_groups(const std::vector<SegGate> &gs, bool two, int nq, int32_t code) {
+    std::vector<SegGate> m[8][8];
+    int dm[8][8] = {}, da[8] = {}, db[8] = {};
+    for (const SegGate &g : gs) {
+        const int a = g.a & 7, b = two ? (g.b & 7) : a;
+        m[a][b].push_back(g);
+        da[a]++;
+        db[b]++;
+    }
+    const int D = lane_groups_needed(gs, two);
+    if (!two) {
+        for (int r = 0; r < 8; ++r) dm[r][r] = D - da[r];
+    } else {
+        for (int a = 0; a < 8; ++a)
+            while (da[a] < D) {
+                int best = -1;
                 for (int b = 0; b < 8; ++b)
-                    if (!bucket[a][b].empty() && !seen[b]) {
-                        seen[b] = true;
-                        if (match_b[b] < 0 || try_a(match_b[b], seen)) {
-                            match_b[b] = a;
-                            return true;
-                        }
-                    }
-                return false;
-            };
-            for (int a = 0; a < 8; ++a) {
-                bool seen[8] = {false, false, false, false, false, false, false, false};
-                try_a(a, seen);
+                    if (db[b] < D && (best < 0 || db[b] < db[best])) best = b;
+                dm[a][best]++;
+                da[a]++;
+                db[best]++;
             }
+    }
+    std::vector<std::vector<SegGate>> out;
+    for (int k = 0; k < D; ++k) {
+        int match_b[8];
+        for (int b = 0; b < 8; ++b) match_b[b] = -1;
+        std::function<bool(int, bool *)> try_a = [&](int a, bool *seen) -> bool {
             for (int b = 0; b < 8; ++b)
-                if (match_b[b] >= 0) {
-                    grp.push_back(bucket[match_b[b]][b].back());
-                    bucket[match_b[b]][b].pop_back();
+                if ((!m[a][b].empty() || dm[a][b] > 0) && !seen[b]) {
+                    seen[b] = true;
+                    if (match_b[b] < 0 || try_a(match_b[b], seen)) {
+                        match_b[b] = a;
+                        return true;
+                    }
                 }
+            return false;
+        };
+        for (int a = 0; a < 8; ++a) {
+            bool seen[8] = {false, false, false, false, false, false, false, false};
+            try_a(a, seen);
         }
-        left -= grp.size();
+        std::vector<SegGate> grp;
+        for (int b = 0; b < 8; ++b) {
+            const int a = match_b[b];
+            if (a < 0) continue;  // unreachable for a regular multigraph
+            if (!m[a][b].empty()) {
+                grp.push_back(m[a][b].back());
+                m[a][b].pop_back();
+            } else {
+                dm[a][b]--;
+                grp.push_back(SegGate{dummy_col(nq, a), dummy_col(nq, two ? b : a), code});
+            }
+        }
         out.push_back(std::move(grp));
     }
     return out;
@@ -406,10 +444,13 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
             if (pr.size() > 255) res_form = false;
     }
 
-    // Tile positions: a permutation of the columns chosen (identity or one of
-    // a few seeded shuffles) to need the fewest conflict-free lane groups
-    // (resident form: the fewest bank conflicts of the owners' partner cells).
-    const uint16_t dummy = (uint16_t)nq;  // zero column appended to every tile row
+    // Tile positions: a permutation of the columns.  Default form: a local
+    // search that swaps the positions of two columns whenever that keeps or
+    // lowers (lane groups needed summed over the gate runs, squared residue
+    // counts summed), until the groups reach their lower bound, the sum of
+    // ceil(gates / 8) over the runs.  Resident form: identity or one of a few
+    // seeded shuffles, whichever needs the fewest groups plus bank conflicts
+    // of the owners' partner cells.
     auto remap = [](const std::vector<SegGate> &gs, const std::vector<int> &perm) {
         std::vector<SegGate> out(gs);
         for (SegGate &g : out) {
@@ -418,45 +459,122 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
         }
         return out;
     };
-    auto groups_needed = [&](const std::vector<int> &perm) {
-        size_t total = 0;
-        if (res_form) {  // per (layer, slot, quarter-warp): wavefronts = largest residue multiplicity
-            for (int l = 0; l < nl; ++l)
+    auto splitmix = [](uint64_t &st) {
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    std::vector<int> best(nq);
+    for (int i = 0; i < nq; ++i) best[i] = i;
+    if (res_form) {
+        auto groups_needed = [&](const std::vector<int> &perm) {
+            size_t total = 0;
+            for (int l = 0; l < nl; ++l)  // per (layer, slot, quarter-warp): largest residue multiplicity
                 for (size_t base = 0; base < resident.size(); base += 8) {
                     int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0}, mx = 0;
                     for (size_t o = base; o < std::min(resident.size(), base + 8); ++o)
                         if (rops[l][o].first >= RS_CX_CTRL) mx = std::max(mx, ++cnt[perm[rops[l][o].second] & 7]);
                     total += (size_t)mx;
                 }
+            for (size_t l = 0; l < L.size(); ++l)
+                for (int32_t code : {(int32_t)OP_H, (int32_t)OP_S, (int32_t)OP_CX, (int32_t)OP_CZ}) {
+                    std::vector<SegGate> gs;
+                    for (const SegGate &g : L[l].gates)
+                        if ((g.code_rec & 15) == code) gs.push_back(g);
+                    if (!gs.empty()) total += (size_t)lane_groups_needed(remap(gs, perm), code == OP_CX || code == OP_CZ);
+                }
+            return total;
+        };
+        size_t best_cost = groups_needed(best);
+        for (uint64_t seed = 1; seed <= 12 && nq > 8; ++seed) {
+            std::vector<int> perm(nq);
+            for (int i = 0; i < nq; ++i) perm[i] = i;
+            uint64_t st = seed * 0x9E3779B97F4A7C15ull;
+            for (int i = nq - 1; i > 0; --i) std::swap(perm[i], perm[(int)(splitmix(st) % (uint64_t)(i + 1))]);
+            const size_t cost = groups_needed(perm);
+            if (cost < best_cost) {
+                best_cost = cost;
+                best = perm;
+            }
         }
+    } else if (nq > 8) {
+        struct RunCount {
+            int cnt[2][8];
+        };
+        std::vector<RunCount> rc;
+        std::vector<std::vector<std::pair<int, int>>> app(nq);  // column -> (run, side)
+        long lower = 0;
         for (size_t l = 0; l < L.size(); ++l)
             for (int32_t code : {(int32_t)OP_H, (int32_t)OP_S, (int32_t)OP_CX, (int32_t)OP_CZ}) {
-                std::vector<SegGate> gs;
+                const bool two = code == OP_CX || code == OP_CZ;
+                const int ri = (int)rc.size();
+                int ng = 0;
                 for (const SegGate &g : L[l].gates)
-                    if ((g.code_rec & 15) == code) gs.push_back(g);
-                if (!gs.empty()) total += bank_groups(remap(gs, perm), code == OP_CX || code == OP_CZ).size();
+                    if ((g.code_rec & 15) == code) {
+                        app[g.a].emplace_back(ri, 0);
+                        if (two) app[g.b].emplace_back(ri, 1);
+                        ++ng;
+                    }
+                if (ng == 0) continue;
+                rc.push_back(RunCount{});
+                lower += (ng + 7) / 8;
             }
-        return total;
-    };
-    std::vector<int> best(nq);
-    for (int i = 0; i < nq; ++i) best[i] = i;
-    size_t best_cost = groups_needed(best);
-    for (uint64_t seed = 1; seed <= 12 && nq > 8; ++seed) {
-        std::vector<int> perm(nq);
-        for (int i = 0; i < nq; ++i) perm[i] = i;
-        uint64_t st = seed * 0x9E3779B97F4A7C15ull;
-        for (int i = nq - 1; i > 0; --i) {  // Fisher-Yates with SplitMix64
-            st += 0x9E3779B97F4A7C15ull;
-            uint64_t z = st;
-            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-            z ^= z >> 31;
-            std::swap(perm[i], perm[(int)(z % (uint64_t)(i + 1))]);
-        }
-        const size_t cost = groups_needed(perm);
-        if (cost < best_cost) {
-            best_cost = cost;
-            best = perm;
+        for (int col = 0; col < nq; ++col)
+            for (auto &e : app[col]) rc[(size_t)e.first].cnt[e.second][best[col] & 7]++;
+        auto groups = [&](int ri) {
+            int D = 0;
+            for (int sd = 0; sd < 2; ++sd)
+                for (int r = 0; r < 8; ++r) D = std::max(D, rc[(size_t)ri].cnt[sd][r]);
+            return D;
+        };
+        auto squares = [&](int ri) {
+            long q = 0;
+            for (int sd = 0; sd < 2; ++sd)
+                for (int r = 0; r < 8; ++r) q += (long)rc[(size_t)ri].cnt[sd][r] * rc[(size_t)ri].cnt[sd][r];
+            return q;
+        };
+        long cost = 0;
+        for (int ri = 0; ri < (int)rc.size(); ++ri) cost += groups(ri);
+        std::vector<int> stamp(rc.size(), -1), touched;
+        uint64_t st = 0x5EEDull;
+        const long iters = std::min<long>(400000, 100L * nq);
+        for (long it = 0; it < iters && cost > lower; ++it) {
+            const int x = (int)(splitmix(st) % (uint64_t)nq), y = (int)(splitmix(st) % (uint64_t)nq);
+            const int rx = best[x] & 7, ry = best[y] & 7;
+            if (rx == ry) continue;
+            touched.clear();
+            for (int v : {x, y})
+                for (auto &e : app[v])
+                    if (stamp[(size_t)e.first] != (int)it) {
+                        stamp[(size_t)e.first] = (int)it;
+                        touched.push_back(e.first);
+                    }
+            long g0 = 0, q0 = 0, g1 = 0, q1 = 0;
+            for (int ri : touched) {
+                g0 += groups(ri);
+                q0 += squares(ri);
+            }
+            auto move = [&](int v, int from, int to) {
+                for (auto &e : app[v]) {
+                    rc[(size_t)e.first].cnt[e.second][from]--;
+                    rc[(size_t)e.first].cnt[e.second][to]++;
+                }
+            };
+            move(x, rx, ry);
+            move(y, ry, rx);
+            for (int ri : touched) {
+                g1 += groups(ri);
+                q1 += squares(ri);
+            }
+            if (g1 < g0 || (g1 == g0 && q1 <= q0)) {
+                std::swap(best[x], best[y]);
+                cost += g1 - g0;
+            } else {
+                move(x, ry, rx);
+                move(y, rx, ry);
+            }
         }
     }
     {
@@ -487,14 +605,8 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
             if (code < 0) {
                 seg.gates.insert(seg.gates.end(), gs.begin(), gs.end());
             } else {
-                // A 16-byte shared-memory access is served 8 lanes at a time
-                // (8 cells x 16 B = one 128-byte bank row): each group of 8
-                // lanes gets distinct residues; short groups are padded with
-                // gates on the zero dummy column.
-                for (auto &grp : bank_groups(gs, code == OP_CX || code == OP_CZ)) {
+                for (auto &grp : lane_groups(gs, code == OP_CX || code == OP_CZ, nq, code))
                     seg.gates.insert(seg.gates.end(), grp.begin(), grp.end());
-                    for (size_t k = grp.size(); k < 8; ++k) seg.gates.push_back(SegGate{dummy, dummy, code});
-                }
             }
             run.g1 = (int32_t)seg.gates.size();
             seg.runs.push_back(run);

@@ -356,9 +356,7 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
     extern __shared__ u64 sm[];
     const int nq = seg.nq;
     const int T = blockDim.x, tid = threadIdx.x;
-    // Tile row: nq columns + a zero dummy column, padded to an odd number of
-    // 16-byte cells so the 8 words of one column fall on distinct bank groups.
-    const int nq1 = (nq + 1) | 1;
+    const int nq1 = seg_row_cells(nq);
     SegLayer *s_layers = reinterpret_cast<SegLayer *>(sm);
     SegRun *s_runs = reinterpret_cast<SegRun *>(s_layers + seg.nlayers);
     SegGate *s_gates = reinterpret_cast<SegGate *>(s_runs + seg.nruns);
@@ -401,7 +399,8 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
         const int64_t row0 = (tile / nchunks) * rows;
         const int64_t k0 = (tile % nchunks) * bw;
         // ---- load
-        for (int e = tid; e < rows * bw; e += T) tile_xz[(size_t)e * nq1 + nq] = make_ulonglong2(0ull, 0ull);
+        for (int e = tid; e < rows * bw * kSegDummyCols; e += T)
+            tile_xz[(size_t)(e / kSegDummyCols) * nq1 + nq + e % kSegDummyCols] = make_ulonglong2(0ull, 0ull);
         for (int r = 0; r < rows; ++r) {
             const int64_t row = row0 + r;
             const int64_t kg = k0 + 2 * kp;  // first word of the lane's pair
@@ -718,7 +717,9 @@ int g_num_sms = 0;
 
 }  // namespace
 
-size_t segment_smem_bytes(int nq, int rows, int bw) { return (size_t)rows * bw * (2 * ((size_t)(nq + 1) | 1) + 1) * sizeof(u64); }
+size_t segment_smem_bytes(int nq, int rows, int bw) {
+    return (size_t)rows * bw * (2 * (size_t)seg_row_cells(nq) + 1) * sizeof(u64);
+}
 
 size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int nq, int nrecsig, int rows, int bw,
                            int rc) {

@@ -13,6 +13,13 @@ struct RunParams {
     uint64_t pad;
 };
 
+// A tile row holds the nq columns of a segment and kSegDummyCols zero
+// columns (one per shared-memory bank group, for the pad lanes of gate
+// groups), padded to an odd number of 16-byte cells so that the 8 words of
+// one column fall on distinct bank groups.
+constexpr int kSegDummyCols = 8;
+__host__ __device__ inline int seg_row_cells(int nq) { return (nq + kSegDummyCols) | 1; }
+
 // A gate inside a fused segment (8 bytes).  a / b are LOCAL column indices
 // (positions in the segment's touched-qubit list); code_rec holds the op code
 // in its low 4 bits and, for the per-shot conditional gates, the record index

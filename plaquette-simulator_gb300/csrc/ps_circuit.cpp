@@ -633,6 +633,16 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
         seg.layers.push_back(ly);
         seg.slots.insert(seg.slots.end(), L[l].slots.begin(), L[l].slots.end());
     }
+    {  // record slots renumbered in sign order: the lanes of a sign batch read consecutive record words
+        std::vector<int32_t> order;
+        order.reserve(seg.recsig_rec.size());
+        for (SegSign &sg : seg.signs)
+            if (sg.kind == SIGN_REC_X) {
+                order.push_back(seg.recsig_rec[(size_t)sg.rec]);
+                sg.rec = (int32_t)order.size() - 1;
+            }
+        seg.recsig_rec = std::move(order);
+    }
     if (res_form) {
         seg.res_slots = RC;
         seg.res_cols.assign((size_t)RC * 32, (uint16_t)0xFFFF);

@@ -373,7 +373,8 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
     const u64 **s_recp = reinterpret_cast<const u64 **>(sm + head);  // [nrecsig] record pointers
     XZ *tile_xz = reinterpret_cast<XZ *>(sm + head + (seg.nrecsig + 1) / 2 * 2);  // [rows*bw][nq1]
     u64 *rtile = reinterpret_cast<u64 *>(tile_xz + (size_t)rows * bw * nq1);      // [rows*bw] r words
-    u64 *s_recw = rtile + rows * bw;                                               // [bw][nrecsig]
+    u64 *s_recw = rtile + rows * bw;                                               // [bw][rs]
+    const int rs = seg_rec_stride(seg.nrecsig, bw);
     for (int i = tid; i < seg.nrecsig; i += T) s_recp[i] = recs[seg.recsig_rec[i]];
     for (int i = tid; i < seg.nlayers; i += T) s_layers[i] = seg.layers[i];
     for (int i = tid; i < seg.nruns; i += T) s_runs[i] = seg.runs[i];
@@ -439,10 +440,12 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
             const int64_t row = row0 + pair / bw, kg = k0 + pair % bw;
             if (row < W && kg < w) cp_async8(&rtile[pair], R + row * w + kg);
         }
-        for (int e = tid; e < seg.nrecsig * bw; e += T) {
-            const int kk = e % bw, slot = e / bw;
+        {  // bw is a power of two dividing T: a thread copies one word of records
+            const int kk = tid & (bw - 1);
             const int64_t kg = k0 + kk;
-            if (kg < w) cp_async8(&s_recw[kk * seg.nrecsig + slot], s_recp[slot] + kg);
+            if (kg < w)
+                for (int slot = tid / bw; slot < seg.nrecsig; slot += T / bw)
+                    cp_async8(&s_recw[kk * rs + slot], s_recp[slot] + kg);
         }
         cp_async_wait_all();
         __syncthreads();
@@ -517,7 +520,7 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
                         else if (sg.kind == SIGN_Z)
                             rd[p] ^= v.x;
                         else
-                            rd[p] ^= s_recw[p * seg.nrecsig + sg.rec] & v.y;
+                            rd[p] ^= s_recw[p * rs + sg.rec] & v.y;
                     }
                 }
 #pragma unroll
@@ -597,7 +600,7 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
                         else if (sg.kind == SIGN_Z)
                             rd ^= v.x;
                         else
-                            rd ^= s_recw[kk * seg.nrecsig + sg.rec] & v.y;
+                            rd ^= s_recw[kk * rs + sg.rec] & v.y;
                     }
 #pragma unroll
                     for (int u = 0; u < NE; ++u)
@@ -660,7 +663,7 @@ __global__ void __launch_bounds__(256, 2) segment_kernel(u64 *__restrict__ X, u6
                 for (int it = lane; it < nsg + nent; it += 32) {
                     if (it < nsg) {
                         const SegSign sg = s_signs[it];
-                        const u64 m = sg.kind == SIGN_REC_X ? s_recw[kk * seg.nrecsig + sg.rec] : ~0ull;
+                        const u64 m = sg.kind == SIGN_REC_X ? s_recw[kk * rs + sg.rec] : ~0ull;
                         if (m) rd ^= m & prop_parity(seg, pbase + it, t);
                     } else {
                         const NoiseEntry e = ent[it - nsg];
@@ -727,7 +730,8 @@ size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int n
                           (size_t)ngates * sizeof(SegGate) + (size_t)nsigns * sizeof(SegSign) +
                           (size_t)nq * sizeof(int32_t) + (size_t)nlayers * rc * 32 * sizeof(ResOp) +
                           (size_t)rc * 32 * sizeof(uint16_t) + 15) / 16 * 16 +
-                         (size_t)(nrecsig + 1) / 2 * 16 + (size_t)nrecsig * bw * 8 + (size_t)rows * bw * 8;
+                         (size_t)(nrecsig + 1) / 2 * 16 + (size_t)seg_rec_stride(nrecsig, bw) * bw * 8 +
+                         (size_t)rows * bw * 8;
     return segment_smem_bytes(nq, rows, bw) + sched;
 }
 

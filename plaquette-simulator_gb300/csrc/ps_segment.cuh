@@ -20,6 +20,15 @@ struct RunParams {
 constexpr int kSegDummyCols = 8;
 __host__ __device__ inline int seg_row_cells(int nq) { return (nq + kSegDummyCols) | 1; }
 
+// Row stride (in words) of a tile's record words [bw][stride]: a warp copies
+// 32 / bw records of each of its bw words, so a stride of 32 / bw mod 16
+// puts the 32 eight-byte stores on distinct bank pairs, two wavefronts.
+__host__ __device__ inline int seg_rec_stride(int nrecsig, int bw) {
+    if (bw < 2) return nrecsig;
+    const int m = (32 / bw) % 16;
+    return nrecsig + ((m - nrecsig % 16) % 16 + 16) % 16;
+}
+
 // A gate inside a fused segment (8 bytes).  a / b are LOCAL column indices
 // (positions in the segment's touched-qubit list); code_rec holds the op code
 // in its low 4 bits and, for the per-shot conditional gates, the record index

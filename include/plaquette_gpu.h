@@ -211,6 +211,12 @@ typedef struct {
                              last layer through propagated Paulis); 2 = one
                              thread per gate over all shot-words of a one-row
                              tile                                             */
+    int32_t per_shot_xz; /* fused runs from |0...0>: 0 = share the x / z bits of
+                             all shots and run a sign program when the circuit
+                             has no per-shot conditional gate (H_IF / S_IF):
+                             bit-identical, and the final x / z bits are
+                             written to every shot; 1 = always update every
+                             shot's tableau                                   */
 } ps_circuit_options;
 
 typedef struct {
@@ -220,6 +226,7 @@ typedef struct {
     double segment_bytes;           /* algorithmic HBM bytes of all segments  */
     int32_t seg_rows, seg_words, seg_threads, meas_words;
     int32_t resident_segments;      /* segments in the register-resident form */
+    int32_t shared_xz;              /* 1: runs from |0...0> use the shared-x/z plan */
 } ps_circuit_stats;
 
 typedef struct ps_circuit ps_circuit;
@@ -242,8 +249,9 @@ ps_status ps_circuit_destroy(ps_circuit *c);
 /* Per-kernel-kind device time of one run, measured with CUDA events around
  * every launch (the plan is enqueued launch by launch, not as a graph, and
  * the call waits for it).  Kinds: 0 tableau init, 1 channel sampling (fused),
- * 2 fused segment, 3 measurement, 4 per-op gate, 5 per-op channel. */
-#define PS_PROFILE_KINDS 6
+ * 2 fused segment, 3 measurement, 4 per-op gate, 5 per-op channel, 6 sign
+ * program (shared x/z), 7 x / z broadcast (shared x/z). */
+#define PS_PROFILE_KINDS 8
 typedef struct {
     double ms[PS_PROFILE_KINDS];
     uint64_t launches[PS_PROFILE_KINDS];

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/plaquette_gpu.h"
+#include "ps_frame.h"
 #include "ps_internal.h"
 #include "ps_segment.cuh"
 
@@ -61,6 +62,8 @@ struct SegHost {
     std::vector<SegSign> signs;
     std::vector<int32_t> cols;
     std::vector<NoiseSlot> slots;
+    std::vector<int32_t> slot_op;     // op index of each slot
+    size_t op0 = 0, op1 = 0;          // the segment's ops [op0, op1)
     std::vector<int32_t> recsig_rec;  // record of each reset-X slot
     // resident form (res_slots > 0)
     int32_t res_slots = 0;
@@ -113,6 +116,15 @@ struct ps_circuit {
     u64 *d_res_block = nullptr;     // [nm][w] (owned by the state)
     u64 *d_det_block = nullptr;
     uint64_t num_events = 0;
+    std::vector<int32_t> meas_op;   // op index of each MeasOp
+    // Shared-x/z plan of runs from |0...0> (ps_frame.h), when the circuit
+    // has no per-shot conditional gates.
+    bool frame_ok = false;
+    bool force_per_shot = false;    // measurement statistics need the per-shot plan
+    FrameProgram fprog;
+    FrameOp *d_fops = nullptr;
+    uint32_t *d_ftab = nullptr, *d_fslot = nullptr;
+    uint64_t *d_fxz = nullptr;
     cudaGraph_t graph[2] = {nullptr, nullptr};      // [reset_state]
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
 };
@@ -219,6 +231,8 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
                   const std::vector<uint32_t> &event_of, const std::vector<int32_t> &rec_of,
                   const std::vector<int32_t> &thr_off, const std::vector<std::pair<int64_t, int32_t>> &pre_signs,
                   SegHost &seg) {
+    seg.op0 = i0;
+    seg.op1 = i1;
     std::set<int32_t> qset;
     for (auto &ps_ : pre_signs) qset.insert((int32_t)ps_.first);
     for (size_t i = i0; i < i1; ++i) {
@@ -233,6 +247,7 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
         std::vector<SegGate> gates;
         std::vector<SegSign> signs;
         std::vector<NoiseSlot> slots;
+        std::vector<int32_t> slot_ops;
     };
     std::vector<LayerBuild> L(1);  // layer 0: no gates (signs before any gate)
     std::map<int32_t, int32_t> last;  // local col -> layer of last touch
@@ -281,6 +296,7 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
             sl.thr_off = thr_off[i];
             sl.event = event_of[i];
             L[layer].slots.push_back(sl);
+            L[layer].slot_ops.push_back((int32_t)i);
         }
     }
     const int nq = (int)seg.cols.size();
@@ -632,6 +648,7 @@ int build_segment(ps_circuit *c, const std::vector<ps_op> &ops, size_t i0, size_
         ly.s1 = (int32_t)seg.signs.size();
         seg.layers.push_back(ly);
         seg.slots.insert(seg.slots.end(), L[l].slots.begin(), L[l].slots.end());
+        seg.slot_op.insert(seg.slot_op.end(), L[l].slot_ops.begin(), L[l].slot_ops.end());
     }
     {  // record slots renumbered in sign order: the lanes of a sign batch read consecutive record words
         std::vector<int32_t> order;
@@ -713,7 +730,7 @@ struct Profiler {
     }
 };
 
-enum ProfKind { P_INIT = 0, P_SAMPLE = 1, P_SEGMENT = 2, P_MEASURE = 3, P_GATE = 4, P_CHANNEL = 5 };
+enum ProfKind { P_INIT = 0, P_SAMPLE = 1, P_SEGMENT = 2, P_MEASURE = 3, P_GATE = 4, P_CHANNEL = 5, P_FRAME = 6, P_BROADCAST = 7 };
 
 // Enqueues plan steps [from, to) on `st`.
 int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profiler *prof = nullptr) {
@@ -764,7 +781,36 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
     return OK;
 }
 
+// The shared-x/z plan of a run from |0...0>: for each range of the sign
+// program, the channel sampling of its segment (entries tagged with their
+// slot) and the sign kernel; then the broadcast of the final x / z bits.
+int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
+    ps_state *h = c->h;
+    auto timed = [&](int kind, auto &&launch) -> int {
+        if (prof && prof->begin(kind) != OK) return E_CUDA;
+        int rc = launch();
+        if (prof && rc == OK && prof->end() != OK) return E_CUDA;
+        return rc;
+    };
+    bool first = true;
+    for (const FrameProgram::Launch &L : c->fprog.launches) {
+        int rc = OK;
+        if (L.seg >= 0)
+            rc = timed(P_SAMPLE, [&] { return launch_noise_sample(st, c->segs[(size_t)L.seg].dev, h->w, c->d_params, 1); });
+        if (rc == OK)
+            rc = timed(P_FRAME, [&] {
+                return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, c->d_fslot, c->d_meas,
+                                    c->d_entries, c->d_entry_count, c->entry_cap, (uint64_t)h->seed, c->d_params,
+                                    first ? 1 : 0);
+            });
+        if (rc != OK) return rc;
+        first = false;
+    }
+    return timed(P_BROADCAST, [&] { return launch_broadcast_xz(st, h->X, h->Z, h->n, h->w, c->d_fxz, c->fprog.nw64); });
+}
+
 int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nullptr) {
+    if (reset && c->frame_ok && !c->force_per_shot) return enqueue_frame(c, st, prof);
     if (reset) {
         if (prof && prof->begin(P_INIT) != OK) return E_CUDA;
         int rc = launch_init_zero_on(st, c->h);
@@ -1052,6 +1098,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         m.res = r.res;
         m.det = r.det;
         c->meas.push_back(m);
+        c->meas_op.push_back((int32_t)i);
     };
     size_t max_slots = 0;
     if (!fused) {
@@ -1186,6 +1233,44 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     }
     if (upload(h, c->owned, c->meas, &c->d_meas) != OK) return bail(E_CUDA);
 
+    // ---- shared-x/z plan of runs from |0...0> (no per-shot conditional gates)
+    if (fused && c->opts.per_shot_xz == 0 && h->n > 0 && frame_smem_bytes(h->n) <= kSegSmemMax) {
+        bool ok = true;
+        for (const ps_op &o : ops) ok &= o.code != OP_H_IF && o.code != OP_S_IF;
+        if (ok) {
+            FrameBuilder fb(h->n);
+            for (const Step &s : c->steps) {
+                if (s.kind == K_SEGMENT) {
+                    const SegHost &sg = c->segs[(size_t)s.first];
+                    std::map<size_t, uint32_t> slot_of;
+                    for (size_t k = 0; k < sg.slot_op.size(); ++k) slot_of[(size_t)sg.slot_op[k]] = (uint32_t)k;
+                    fb.begin_segment(s.first, (uint32_t)sg.slots.size());
+                    for (size_t i = sg.op0; i < sg.op1; ++i) {
+                        const ps_op &o = ops[i];
+                        if (is_channel(o.code))
+                            fb.channel(o.a, o.code == OP_PAULI2 ? o.b : -1, slot_of[i]);
+                        else
+                            fb.gate(o.code, o.a, o.b);
+                    }
+                    fb.end_segment();
+                } else if (s.kind == K_MEAS) {
+                    for (int32_t m = s.first; m < s.first + s.count; ++m) {
+                        const ps_op &o = ops[(size_t)c->meas_op[(size_t)m]];
+                        fb.measure(o.a, m, o.code == OP_R);
+                    }
+                }
+            }
+            fb.finish();
+            c->fprog = std::move(fb.prog);
+            if (c->fprog.tab.empty()) c->fprog.tab.push_back(0);
+            if (c->fprog.slot_off.empty()) c->fprog.slot_off.push_back(0);
+            if (upload(h, c->owned, c->fprog.ops, &c->d_fops) || upload(h, c->owned, c->fprog.tab, &c->d_ftab) ||
+                upload(h, c->owned, c->fprog.slot_off, &c->d_fslot) || upload(h, c->owned, c->fprog.xz, &c->d_fxz))
+                return bail(E_CUDA);
+            c->frame_ok = true;
+        }
+    }
+
     // ---- stats
     ps_circuit_stats &st = c->stats;
     st.num_ops = ops.size();
@@ -1209,6 +1294,11 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         }
     }
     st.launches_per_run += 1;  // run-parameter update
+    if (c->frame_ok) {  // runs from |0...0>: sampling (2), sign kernel per range, broadcast, parameters
+        st.shared_xz = 1;
+        st.launches_per_run = 2;
+        for (const FrameProgram::Launch &L : c->fprog.launches) st.launches_per_run += L.seg >= 0 ? 3 : 1;
+    }
     st.seg_rows = c->opts.seg_rows;
     st.seg_words = c->opts.seg_words;
     st.seg_threads = c->opts.seg_threads;
@@ -1307,7 +1397,9 @@ ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *rand
     PS_CUDA(cudaMemcpy(c->d_meas, m.data(), nm * sizeof(MeasOp), cudaMemcpyHostToDevice));
     const RunParams p = begin_run(c, reset_state != 0);
     set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base, p.word_base);
+    c->force_per_shot = true;  // the statistics come from the per-shot measurement kernel
     int rc = enqueue_plan(c, h->stream, reset_state != 0);
+    c->force_per_shot = false;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     std::vector<int32_t> host(nm * 2);
     if (rc == OK && e == cudaSuccess) e = cudaMemcpy(host.data(), d, nm * 2 * sizeof(int32_t), cudaMemcpyDeviceToHost);

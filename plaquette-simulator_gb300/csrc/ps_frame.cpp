@@ -1,0 +1,201 @@
+// ps_frame.cpp -- host side of shared-x/z runs: the x / z simulation of one
+// tableau and the sign program it emits (see ps_frame.h).
+#include "ps_frame.h"
+
+#include <algorithm>
+
+#include "../../include/plaquette_gpu.h"
+
+namespace ps {
+
+FrameBuilder::FrameBuilder(int64_t n) : n_(n), W_(2 * n + 1), nw_((n + 63) / 64) {
+    x_.assign((size_t)(W_ * nw_), 0ull);
+    z_.assign((size_t)(W_ * nw_), 0ull);
+    f_.assign((size_t)W_, 0);
+    for (int64_t i = 0; i < n_; ++i) {  // |0...0>: destabilizer X_i, stabilizer Z_i (CliffordState.hpp:66-71)
+        flip(x_, i, i);
+        flip(z_, i + n_, i);
+    }
+    prog.nw64 = nw_;
+    open_range();
+}
+
+void FrameBuilder::open_range() { prog.launches.push_back({-1, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size()}); }
+
+// The gate functors of GateFunctors.hpp over all W rows (scratch included,
+// CliffordState.hpp:381-386): x / z updated here, the sign term folded into f.
+void FrameBuilder::gate(int32_t code, int64_t a, int64_t b) {
+    for (int64_t i = 0; i < W_; ++i) {
+        const int xa = bit(x_, i, a), za = bit(z_, i, a);
+        switch (code) {
+        case PS_OP_H:  // :89-93
+            f_[(size_t)i] ^= (uint8_t)(xa & za);
+            if (xa != za) {
+                flip(x_, i, a);
+                flip(z_, i, a);
+            }
+            break;
+        case PS_OP_S:  // :164-169
+            f_[(size_t)i] ^= (uint8_t)(xa & za);
+            if (xa) flip(z_, i, a);
+            break;
+        case PS_OP_X: f_[(size_t)i] ^= (uint8_t)za; break;         // :303-307
+        case PS_OP_Y: f_[(size_t)i] ^= (uint8_t)(za ^ xa); break;  // :323-327
+        case PS_OP_Z: f_[(size_t)i] ^= (uint8_t)xa; break;         // :372-376
+        case PS_OP_CX: {  // :247-253, a = control
+            const int xt = bit(x_, i, b), zt = bit(z_, i, b);
+            f_[(size_t)i] ^= (uint8_t)(xa & zt & (xt ^ za ^ 1));
+            if (xa) flip(x_, i, b);
+            if (zt) flip(z_, i, a);
+            break;
+        }
+        case PS_OP_CZ: {  // :29-35
+            const int xt = bit(x_, i, b), zt = bit(z_, i, b);
+            f_[(size_t)i] ^= (uint8_t)(xa & xt & (zt ^ za));
+            if (xa) flip(z_, i, b);
+            if (xt) flip(z_, i, a);
+            break;
+        }
+        default: break;
+        }
+    }
+}
+
+void FrameBuilder::begin_segment(int32_t seg, uint32_t nslots) {
+    seg_ = seg;
+    slot_rows_.assign(nslots, {});
+}
+
+// Rows whose sign a Pauli on a (b) flips: X flips rows with z set, Z rows
+// with x set (the conditional X = H S S H and Z = S S of the channel).
+void FrameBuilder::channel(int64_t a, int64_t b, uint32_t slot) {
+    std::vector<uint32_t> &rows = slot_rows_[slot];
+    rows.clear();
+    for (int64_t i = 0; i < W_; ++i) {
+        uint32_t sel = (uint32_t)bit(z_, i, a) | (uint32_t)bit(x_, i, a) << 1;
+        if (b >= 0) sel |= (uint32_t)bit(z_, i, b) << 2 | (uint32_t)bit(x_, i, b) << 3;
+        if (sel) rows.push_back((uint32_t)i | sel << 28);
+    }
+}
+
+void FrameBuilder::end_segment() {
+    if (slot_rows_.empty()) {  // no channels: nothing sampled, nothing to apply
+        seg_ = -1;
+        return;
+    }
+    const uint32_t base = (uint32_t)prog.slot_off.size();
+    for (const auto &rows : slot_rows_) {
+        prog.slot_off.push_back((uint32_t)prog.tab.size());
+        prog.tab.insert(prog.tab.end(), rows.begin(), rows.end());
+    }
+    prog.slot_off.push_back((uint32_t)prog.tab.size());
+    // A new launch: its sampling precedes it, then this segment's noise.
+    if (prog.launches.back().op0 == prog.launches.back().op1) prog.launches.pop_back();
+    prog.launches.push_back({seg_, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size()});
+    FrameOp op{};
+    op.kind = F_NOISE;
+    op.arg = (int32_t)base;
+    prog.ops.push_back(op);
+    prog.launches.back().op1 = (uint32_t)prog.ops.size();
+    slot_rows_.clear();
+    seg_ = -1;
+}
+
+// Bit 1 of the summed phase of row i times row k (RowProductSign,
+// MeasurementFunctors.hpp:97-129, the reference's (sum >> 1) & 1).
+int FrameBuilder::phase_bit(int64_t i, int64_t k) const {
+    long sum = 0;
+    for (int64_t t = 0; t < nw_; ++t) {
+        const uint64_t x1 = x_[(size_t)(i * nw_ + t)], z1 = z_[(size_t)(i * nw_ + t)];
+        const uint64_t x2 = x_[(size_t)(k * nw_ + t)], z2 = z_[(size_t)(k * nw_ + t)];
+        const uint64_t plus = (x1 & ~z1 & x2 & z2) | (x1 & z1 & ~x2 & z2) | (~x1 & z1 & x2 & ~z2);
+        const uint64_t minus = (x1 & z1 & x2 & ~z2) | (x1 & ~z1 & ~x2 & z2) | (~x1 & z1 & x2 & z2);
+        sum += (long)__builtin_popcountll(plus) - (long)__builtin_popcountll(minus);
+    }
+    return (int)((((sum % 4) + 4) % 4) >> 1);
+}
+
+void FrameBuilder::row_xor(int64_t dst, int64_t src) {
+    for (int64_t t = 0; t < nw_; ++t) {
+        x_[(size_t)(dst * nw_ + t)] ^= x_[(size_t)(src * nw_ + t)];
+        z_[(size_t)(dst * nw_ + t)] ^= z_[(size_t)(src * nw_ + t)];
+    }
+}
+
+// MeasureQubit (CliffordState.hpp:587-623): the lowest stabilizer row p+n
+// with x(p+n,q) = 1 takes the random branch, else the deterministic one; a
+// reset then flips the rows with z(., q) = 1 where the outcome is 1.
+void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
+    int64_t p = 0;
+    while (p < n_ && !bit(x_, p + n_, q)) ++p;
+    FrameOp op{};
+    op.arg = meas_index;
+    op.off = (uint32_t)prog.tab.size();
+    const int64_t s = 2 * n_;
+    if (p < n_) {  // MeasureRandom (:225-265)
+        op.kind = F_MEAS_RAND;
+        prog.tab.push_back((uint32_t)p);
+        for (int64_t t = 0; t < nw_; ++t) {  // row p := row p+n; row p+n := Z_q
+            x_[(size_t)(p * nw_ + t)] = x_[(size_t)((p + n_) * nw_ + t)];
+            z_[(size_t)(p * nw_ + t)] = z_[(size_t)((p + n_) * nw_ + t)];
+            x_[(size_t)((p + n_) * nw_ + t)] = 0ull;
+            z_[(size_t)((p + n_) * nw_ + t)] = 0ull;
+        }
+        flip(z_, p + n_, q);
+        f_[(size_t)p] = f_[(size_t)(p + n_)];
+        f_[(size_t)(p + n_)] = 0;
+        for (int64_t i = 0; i < 2 * n_; ++i)
+            if (i != p && i != p + n_ && bit(x_, i, q)) {
+                const uint32_t c = (uint32_t)(phase_bit(i, p) ^ f_[(size_t)p]);
+                prog.tab.push_back((uint32_t)i | c << 31);
+                row_xor(i, p);
+            }
+    } else {  // MeasureDetermined (:189-201): scratch row := product of the selected stabilizers
+        op.kind = F_MEAS_DET;
+        for (int64_t t = 0; t < nw_; ++t) {
+            x_[(size_t)(s * nw_ + t)] = 0ull;
+            z_[(size_t)(s * nw_ + t)] = 0ull;
+        }
+        uint32_t c = 0;
+        for (int64_t i = 0; i < n_; ++i)
+            if (bit(x_, i, q)) {
+                c ^= (uint32_t)(phase_bit(s, i + n_) ^ f_[(size_t)(i + n_)]);
+                prog.tab.push_back((uint32_t)(i + n_));
+                row_xor(s, i + n_);
+            }
+        op.kind |= c << 8;
+        f_[(size_t)s] = 0;
+    }
+    op.len = (uint32_t)prog.tab.size() - op.off;
+    prog.ops.push_back(op);
+    prog.launches.back().op1 = (uint32_t)prog.ops.size();
+    if (reset) {
+        FrameOp ro{};
+        ro.kind = F_RESET_X;
+        ro.off = (uint32_t)prog.tab.size();
+        for (int64_t i = 0; i < W_; ++i)
+            if (bit(z_, i, q)) prog.tab.push_back((uint32_t)i);
+        ro.len = (uint32_t)prog.tab.size() - ro.off;
+        prog.ops.push_back(ro);
+        prog.launches.back().op1 = (uint32_t)prog.ops.size();
+    }
+}
+
+void FrameBuilder::finish() {
+    FrameOp op{};
+    op.kind = F_FLIP;
+    op.off = (uint32_t)prog.tab.size();
+    for (int64_t i = 0; i < W_; ++i)
+        if (f_[(size_t)i]) prog.tab.push_back((uint32_t)i);
+    op.len = (uint32_t)prog.tab.size() - op.off;
+    prog.ops.push_back(op);
+    prog.launches.back().op1 = (uint32_t)prog.ops.size();
+    prog.xz.assign((size_t)(W_ * 2 * nw_), 0ull);
+    for (int64_t i = 0; i < W_; ++i)
+        for (int64_t t = 0; t < nw_; ++t) {
+            prog.xz[(size_t)((i * 2 + 0) * nw_ + t)] = x_[(size_t)(i * nw_ + t)];
+            prog.xz[(size_t)((i * 2 + 1) * nw_ + t)] = z_[(size_t)(i * nw_ + t)];
+        }
+}
+
+}  // namespace ps

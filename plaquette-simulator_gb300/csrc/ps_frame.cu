@@ -1,0 +1,149 @@
+// ps_frame.cu -- device side of shared-x/z runs (see ps_frame.h): the sign
+// program over each shot-word's signs, and the broadcast of the final x / z
+// bits to every shot.
+#include <algorithm>
+
+#include "ps_draw.cuh"
+#include "ps_frame.h"
+#include "ps_internal.h"
+#include "ps_segment.cuh"
+
+namespace ps {
+
+namespace {
+
+// One warp per shot-word: its W signs live in shared memory while the warp
+// runs ops [op0, op1) in order; lanes spread over each op's rows (the rows
+// of one op are distinct, so the XORs of one op never collide).
+__global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t n, int64_t w,
+                                                   const FrameOp *__restrict__ ops, uint32_t op0, uint32_t op1,
+                                                   const uint32_t *__restrict__ tab,
+                                                   const uint32_t *__restrict__ slot_off,
+                                                   const MeasOp *__restrict__ meas,
+                                                   const NoiseEntry *__restrict__ entries,
+                                                   const int32_t *__restrict__ entry_count, int32_t cap,
+                                                   uint64_t seed, const RunParams *__restrict__ rp, int from_zero) {
+    extern __shared__ u64 sR[];
+    const int64_t W = 2 * n + 1;
+    const int lane = threadIdx.x;
+    const int64_t k = blockIdx.x;
+    for (int64_t i = lane; i < W; i += 32) sR[i] = from_zero ? 0ull : R[i * w + k];
+    __syncwarp();
+    const uint64_t event_base = rp->event_base, word_base = rp->word_base;
+    u64 last = 0ull;  // outcome of the latest measurement (its reset X)
+    for (uint32_t oi = op0; oi < op1; ++oi) {
+        const FrameOp o = ops[oi];
+        const uint32_t kind = o.kind & 0xFFu;
+        if (kind == F_NOISE) {
+            const int cnt = entry_count[k];
+            const NoiseEntry *ent = entries + k * (int64_t)cap;
+            for (int e = 0; e < cnt; ++e) {
+                const NoiseEntry en = ent[e];
+                const uint32_t t1 = slot_off[o.arg + en.layer + 1];
+                for (uint32_t t = slot_off[o.arg + en.layer] + lane; t < t1; t += 32) {
+                    const uint32_t v = tab[t], sel = v >> 28;
+                    u64 m = 0ull;
+                    if (sel & 1u) m ^= en.fxa;
+                    if (sel & 2u) m ^= en.fza;
+                    if (sel & 4u) m ^= en.fxb;
+                    if (sel & 8u) m ^= en.fzb;
+                    sR[v & kFrameRowMask] ^= m;
+                }
+                __syncwarp();
+            }
+        } else if (kind == F_MEAS_DET) {
+            u64 acc = 0ull;
+            for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) acc ^= sR[tab[t]];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, off);
+            if (o.kind >> 8) acc = ~acc;
+            if (lane == 0) {
+                const MeasOp &m = meas[o.arg];
+                m.res[k] = acc;
+                m.det[k] = ~0ull;
+                sR[2 * n] = acc;
+            }
+            last = acc;
+            __syncwarp();
+        } else if (kind == F_MEAS_RAND) {
+            const MeasOp m = meas[o.arg];
+            const u64 out = outcome_bits(m, lane, seed, event_base, k, word_base);
+            const uint32_t p = tab[o.off];
+            const u64 rpv = sR[p + n];
+            __syncwarp();
+            if (lane == 0) {
+                sR[p] = rpv;
+                sR[p + n] = out;
+                m.res[k] = out;
+                m.det[k] = 0ull;
+            }
+            __syncwarp();
+            for (uint32_t t = o.off + 1 + lane; t < o.off + o.len; t += 32) {
+                const uint32_t v = tab[t];
+                sR[v & 0x7FFFFFFFu] ^= rpv ^ ((v >> 31) ? ~0ull : 0ull);
+            }
+            last = out;
+            __syncwarp();
+        } else {  // F_RESET_X, F_FLIP
+            const u64 m = kind == F_RESET_X ? last : ~0ull;
+            for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) sR[tab[t]] ^= m;
+            __syncwarp();
+        }
+    }
+    for (int64_t i = lane; i < W; i += 32) R[i * w + k] = sR[i];
+}
+
+// x / z of every shot from the shared bits: one warp per (row, qubit), lanes
+// over 16-byte word pairs (w is even).
+__global__ void __launch_bounds__(256) broadcast_xz_kernel(u64 *__restrict__ X, u64 *__restrict__ Z, int64_t n,
+                                                           int64_t W, int64_t w, const uint64_t *__restrict__ xz,
+                                                           int64_t nw64) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t rq = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rq < W * n; rq += warps) {
+        const int64_t row = rq / n, q = rq - row * n;
+        const u64 xb = (xz[(row * 2 + 0) * nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+        const u64 zb = (xz[(row * 2 + 1) * nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+        const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
+        u64 *xo = X + rq * w, *zo = Z + rq * w;
+        for (int64_t kp = lane; kp < w / 2; kp += 32) {
+            *reinterpret_cast<ulonglong2 *>(xo + 2 * kp) = xv;
+            *reinterpret_cast<ulonglong2 *>(zo + 2 * kp) = zv;
+        }
+    }
+}
+
+int g_frame_sms = 0;
+
+}  // namespace
+
+size_t frame_smem_bytes(int64_t n) { return (size_t)(2 * n + 1) * sizeof(u64); }
+
+int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
+                 const uint32_t *tab, const uint32_t *slot_off, const MeasOp *meas, const NoiseEntry *entries,
+                 const int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero) {
+    const size_t smem = frame_smem_bytes(n);
+    if (smem > 48 * 1024) {
+        const int rc = allow_max_smem((const void *)frame_kernel);
+        if (rc != OK) return rc;
+    }
+    frame_kernel<<<(unsigned)w, 32, smem, st>>>(R, n, w, ops, op0, op1, tab, slot_off, meas, entries, entry_count, cap,
+                                                seed, rp, from_zero);
+    PS_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int launch_broadcast_xz(cudaStream_t st, u64 *X, u64 *Z, int64_t n, int64_t w, const uint64_t *xz, int64_t nw64) {
+    if (g_frame_sms == 0) {
+        int dev = 0;
+        PS_CUDA(cudaGetDevice(&dev));
+        PS_CUDA(cudaDeviceGetAttribute(&g_frame_sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const int64_t W = 2 * n + 1;
+    const int64_t blocks = std::min<int64_t>((W * n + 7) / 8, (int64_t)g_frame_sms * 8);
+    broadcast_xz_kernel<<<(unsigned)blocks, 256, 0, st>>>(X, Z, n, W, w, xz, nw64);
+    PS_CUDA(cudaGetLastError());
+    return OK;
+}
+
+}  // namespace ps

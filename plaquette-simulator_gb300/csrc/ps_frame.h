@@ -1,0 +1,97 @@
+// ps_frame.h -- shared-x/z runs of compiled circuits.
+//
+// Clifford gates, Pauli gates, Pauli channels and Z measurements (with their
+// resets) never make the x / z bits of one shot's tableau differ from
+// another's: a Pauli only flips signs (the conditional X / Z of a channel or
+// a reset is H S S H / S S with the shot's flag, which leaves x / z as they
+// were, GateFunctors.hpp:142-148, :220-228), the random branch of a
+// measurement picks its pivot from x / z alone (MeasurementFunctors.hpp:
+// 297-301), and every sign update is r_i ^ r_k ^ (a bit of a phase sum over
+// x / z) (:97-129).  Only the per-shot conditional H / S gates break this.
+// So from |0...0> the x / z bits of every tableau row are one host-side
+// simulation, and what each shot-word has of its own are the signs R[row]:
+// a run becomes a program of XORs between sign rows whose row lists and
+// constants the host computes while simulating x / z:
+//   noise      R[i] ^= fx / fz of a sampled channel outcome, rows i whose x / z
+//              anticommute with that Pauli at the channel's position;
+//   det. meas. outcome = c ^ XOR of R[i+n] over the destabilizers i with
+//              x(i,q) = 1 (MeasureDetermined, :189-201), into record and
+//              scratch row;
+//   rand. meas R[p] := R[p+n]; R[p+n] := drawn outcome; R[i] ^= R[p] ^ c_i
+//              for the rows the reference multiplies (MeasureRandom,
+//              :225-265);
+//   reset X    R[i] ^= outcome for rows with z(i,q) = 1;
+// and the sign flips of gates and Pauli gates are constants folded into
+// those c's (the device keeps R ^ F for a host-known row mask F, applied at
+// the end).  The final x / z bits are broadcast to every shot, so the state
+// ends exactly as the per-shot plan leaves it.
+#pragma once
+#include <stdint.h>
+
+#include <vector>
+
+namespace ps {
+
+enum FrameKind : uint32_t {
+    F_NOISE = 0,      // entries of segment `arg` (sampled just before): tab rows per slot
+    F_MEAS_DET = 1,   // arg = MeasOp; tab[off..off+len) rows; kind bit 8 = constant
+    F_MEAS_RAND = 2,  // arg = MeasOp; tab[off] = p, then rows | c << 31
+    F_RESET_X = 3,    // R[row] ^= outcome of the last measurement, rows tab[off..off+len)
+    F_FLIP = 4,       // R[row] ^= ~0, rows tab[off..off+len)
+};
+
+struct FrameOp {
+    uint32_t kind;  // FrameKind | constant bit << 8
+    int32_t arg;    // MeasOp index, or for F_NOISE the offset of the segment's slot table
+    uint32_t off;   // into tab
+    uint32_t len;
+};
+
+// Noise table entry: row | sel << 28, sel bit 0 fx(a), 1 fz(a), 2 fx(b), 3 fz(b).
+constexpr uint32_t kFrameRowMask = 0x0FFFFFFFu;
+
+struct FrameProgram {
+    std::vector<FrameOp> ops;
+    std::vector<uint32_t> tab;
+    std::vector<uint32_t> slot_off;  // per segment: nslots + 1 offsets into tab
+    std::vector<uint64_t> xz;        // final x / z bits: [W][2][nw64]
+    int64_t nw64 = 0;
+    // op ranges launched together: the ops of one segment's noise and the
+    // measurement phase after it (seg = -1: no sampling before the range)
+    struct Launch {
+        int32_t seg;
+        uint32_t op0, op1;
+    };
+    std::vector<Launch> launches;
+};
+
+// Host-side simulation of the shared x / z bits and emission of the sign
+// program.  Calls follow the circuit's program order.
+class FrameBuilder {
+  public:
+    explicit FrameBuilder(int64_t n);
+    void gate(int32_t code, int64_t a, int64_t b);  // H, S, X, Y, Z, CX, CZ
+    // Pauli channel on a (and b >= 0): slot `slot` of the current segment.
+    void channel(int64_t a, int64_t b, uint32_t slot);
+    void begin_segment(int32_t seg, uint32_t nslots);
+    void end_segment();
+    void measure(int64_t q, int32_t meas_index, bool reset);
+    void finish();
+    FrameProgram prog;
+
+  private:
+    int64_t n_, W_, nw_;
+    std::vector<uint64_t> x_, z_;  // row-major [W][nw]
+    std::vector<uint8_t> f_;       // pending constant flips per row
+    int32_t seg_ = -1;
+    std::vector<std::vector<uint32_t>> slot_rows_;
+    bool bit(const std::vector<uint64_t> &m, int64_t row, int64_t q) const {
+        return (m[(size_t)(row * nw_ + (q >> 6))] >> (q & 63)) & 1ull;
+    }
+    void flip(std::vector<uint64_t> &m, int64_t row, int64_t q) { m[(size_t)(row * nw_ + (q >> 6))] ^= 1ull << (q & 63); }
+    int phase_bit(int64_t i, int64_t k) const;  // bit 1 of the summed phase of row i times row k
+    void row_xor(int64_t dst, int64_t src);
+    void open_range();
+};
+
+}  // namespace ps

@@ -149,9 +149,23 @@ size_t segment_smem_bytes(int nq, int rows, int bw);
 size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int nq, int nrecsig, int rows, int bw,
                            int rc);
 constexpr size_t kSegSmemMax = 227 * 1024;
-int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp);
+// slot_tags: entries carry their slot index instead of their layer.
+int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
+                        int slot_tags = 0);
 int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
                    int rows, int bw, int threads, const u64 *const *recs);
+
+// ps_frame.cu (shared-x/z runs)
+struct FrameOp;
+struct NoiseEntry;
+size_t frame_smem_bytes(int64_t n);
+// Ops [op0, op1) of a sign program over every shot-word's signs R (from_zero:
+// the signs start at 0, the tableau having just been reset).
+int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
+                 const uint32_t *tab, const uint32_t *slot_off, const MeasOp *meas, const NoiseEntry *entries,
+                 const int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero);
+// X, Z of every shot := the shared bits xz ([2n+1][2][nw64]).
+int launch_broadcast_xz(cudaStream_t st, u64 *X, u64 *Z, int64_t n, int64_t w, const uint64_t *xz, int64_t nw64);
 
 // ps_gates.cu (compiled-circuit form of the per-op kernels)
 int launch_channel_rp(cudaStream_t stream, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,

@@ -33,6 +33,7 @@
 
 #include "ps_internal.h"
 #include "ps_segment.cuh"
+#include "ps_draw.cuh"
 
 namespace ps {
 
@@ -97,31 +98,6 @@ __device__ __forceinline__ void warp_phase_reduce(u64 &c1, u64 &c0, int first_of
     }
 }
 
-// k: the state's word; the draw is keyed by the global word word_base + k.
-__device__ __forceinline__ u64 outcome_bits(const MeasOp &op, int lane, uint64_t seed, uint64_t event_base,
-                                            int64_t k, uint64_t word_base) {
-    u64 bits = 0ull;
-    if (lane < 16) {
-        if (op.forced) {
-            const u64 fw = op.forced[k];
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                const int b = lane * 4 + l;
-                const float u = ((fw >> b) & 1ull) ? 0.25f : 0.75f;
-                if (u < op.bias) bits |= 1ull << b;
-            }
-        } else {
-            const u32x4 u =
-                draw_block(seed, event_base + op.event, word_base + (uint64_t)k, (uint32_t)lane, TAG_MEASURE);
-#pragma unroll
-            for (int l = 0; l < 4; ++l)
-                if (unit_float(u.v[l]) < op.bias) bits |= 1ull << (lane * 4 + l);
-        }
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) bits |= __shfl_xor_sync(0xffffffffu, bits, off);
-    return bits;
-}
 
 // B consecutive shot-words of one (row, column) cell, loaded as one vector.
 template <int B> struct Cell {

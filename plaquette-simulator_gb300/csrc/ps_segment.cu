@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256) noise_dense_kernel(SegmentDev seg, int64_
 
 // Pass 2: one warp per word appends the non-identity outcomes to the word's
 // entry list; ballot compaction keeps slot (= layer) order.
-__global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int64_t w) {
+__global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int64_t w, int slot_tags) {
     const int lane = threadIdx.x & 31;
     const int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (k >= w) return;
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
             e.fza = fza;
             e.fxb = fxb;
             e.fzb = fzb;
-            e.layer = seg.res_slots ? s : sl.layer;  // resident form: the slot
+            e.layer = (seg.res_slots || slot_tags) ? s : sl.layer;  // resident form, shared x/z: the slot
             e.a = (uint16_t)sl.a;
             e.b = sl.b >= 0 ? (uint16_t)sl.b : (uint16_t)0xFFFF;
             out[pos] = e;
@@ -735,13 +735,13 @@ size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int n
     return segment_smem_bytes(nq, rows, bw) + sched;
 }
 
-int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp) {
+int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp, int slot_tags) {
     if (seg.nslots == 0) return OK;
     const int64_t threads = 16 * (int64_t)seg.nslots * w;
     noise_dense_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(seg, w, rp);
     PS_CUDA(cudaGetLastError());
     const int wpb = 4;
-    noise_compact_kernel<<<(unsigned)((w + wpb - 1) / wpb), 32 * wpb, 0, stream>>>(seg, w);
+    noise_compact_kernel<<<(unsigned)((w + wpb - 1) / wpb), 32 * wpb, 0, stream>>>(seg, w, slot_tags);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

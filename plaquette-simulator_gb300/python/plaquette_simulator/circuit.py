@@ -5,7 +5,11 @@
 kernel launch per op, the reference's CliffordCircuit::Execute structure,
 CliffordCircuit.hpp:131-135); ``fused=True`` applies every run of gates
 between measurement phases in one tableau pass.  ``graph=True`` captures the
-plan once in a CUDA graph.
+plan once in a CUDA graph.  ``shared_xz=True`` (the default) lets fused runs
+from |0...0> of a circuit without per-shot conditional gates share the x / z
+bits of all shots and run only a sign program per shot-word (bit-identical;
+the final x / z bits are written to every shot); ``shared_xz=False`` updates
+every shot's tableau in every run.
 """
 from __future__ import annotations
 
@@ -23,7 +27,7 @@ from .simulator import CliffordState, _ptr
 class CircuitOptions(C.Structure):
     _fields_ = [("mode", C.c_int32), ("use_graph", C.c_int32), ("seg_rows", C.c_int32),
                 ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32),
-                ("seg_resident", C.c_int32)]
+                ("seg_resident", C.c_int32), ("per_shot_xz", C.c_int32)]
 
 
 class CircuitStats(C.Structure):
@@ -32,7 +36,7 @@ class CircuitStats(C.Structure):
                 ("num_measure_phases", C.c_uint64), ("launches_per_run", C.c_uint64),
                 ("first_record", C.c_uint64), ("segment_bytes", C.c_double), ("seg_rows", C.c_int32),
                 ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32),
-                ("resident_segments", C.c_int32)]
+                ("resident_segments", C.c_int32), ("shared_xz", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -41,7 +45,7 @@ class CircuitStats(C.Structure):
 class CompiledCircuit:
     def __init__(self, circuit: Circuit, state: CliffordState, fused: bool = True, graph: bool = True,
                  seg_rows: int = 0, seg_words: int = 0, seg_threads: int = 0, meas_words: int = 0,
-                 resident: bool = False, word_vector: bool = False):
+                 resident: bool = False, word_vector: bool = False, shared_xz: bool = True):
         if circuit.num_qubits != state.get_num_qubits():
             raise ValueError("circuit and state have different qubit counts")
         self._L = _lib.load()
@@ -50,7 +54,7 @@ class CompiledCircuit:
         self._ops = np.ascontiguousarray(circuit.op_array(), dtype=np.int32)
         self._params = np.ascontiguousarray(circuit.param_array(), dtype=np.float32)
         opts = CircuitOptions(1 if fused else 0, 1 if graph else 0, seg_rows, seg_words, seg_threads, meas_words,
-                              2 if word_vector else (1 if resident else 0))
+                              2 if word_vector else (1 if resident else 0), 0 if shared_xz else 1)
         h = C.c_void_p()
         check(self._L.ps_circuit_compile(state.handle, _ptr(self._ops), len(self._ops), _ptr(self._params),
                                          len(self._params), C.byref(opts), C.byref(h)))
@@ -106,13 +110,15 @@ class CompiledCircuit:
         """Enqueue one run on the state's stream (asynchronous)."""
         check(self._L.ps_circuit_run(self._handle, 1 if reset else 0))
 
-    PROFILE_KINDS = ("init", "channel_sample", "segment", "measure", "gate", "channel")
+    PROFILE_KINDS = ("init", "channel_sample", "segment", "measure", "gate", "channel", "sign_program",
+                     "xz_broadcast")
 
     def profile(self, reset: bool = True) -> dict:
         """Device time per kernel kind of one run (CUDA events around every
         launch; the plan is enqueued launch by launch)."""
         class _Prof(C.Structure):
-            _fields_ = [("ms", C.c_double * 6), ("launches", C.c_uint64 * 6)]
+            _fields_ = [("ms", C.c_double * len(CompiledCircuit.PROFILE_KINDS)),
+                        ("launches", C.c_uint64 * len(CompiledCircuit.PROFILE_KINDS))]
         p = _Prof()
         check(self._L.ps_circuit_profile(self._handle, 1 if reset else 0, C.byref(p)))
         return {k: {"ms": p.ms[i], "launches": int(p.launches[i])} for i, k in enumerate(self.PROFILE_KINDS)}

@@ -17,7 +17,36 @@ FrameBuilder::FrameBuilder(int64_t n) : n_(n), W_(2 * n + 1), nw_((n + 63) / 64)
         flip(z_, i + n_, i);
     }
     prog.nw64 = nw_;
+    flipped_.assign((size_t)W_, 0);
     open_range();
+}
+
+void FrameBuilder::push_op(const FrameOp &op) {
+    prog.ops.push_back(op);
+    prog.launches.back().op1 = (uint32_t)prog.ops.size();
+}
+
+void FrameBuilder::flush_window() {
+    if (window_.empty()) return;
+    FrameOp op{};
+    op.kind = F_WINDOW;
+    op.off = (uint32_t)prog.tab.size();
+    op.len = (uint32_t)window_.size();
+    prog.tab.resize(prog.tab.size() + window_.size());
+    const uint32_t s = (uint32_t)(2 * n_);
+    for (size_t j = 0; j < window_.size(); ++j) {
+        DetRecord &r = window_[j];
+        if (j + 1 < window_.size())  // the last measurement of the window overwrites the scratch row
+            r.rs.erase(std::remove(r.rs.begin(), r.rs.end(), s), r.rs.end());
+        prog.tab[op.off + j] = (uint32_t)prog.tab.size() - op.off;
+        prog.tab.push_back((uint32_t)r.meas);
+        prog.tab.push_back((uint32_t)r.rd.size() | (uint32_t)r.rs.size() << 16 | r.c << 31);
+        prog.tab.insert(prog.tab.end(), r.rd.begin(), r.rd.end());
+        prog.tab.insert(prog.tab.end(), r.rs.begin(), r.rs.end());
+    }
+    push_op(op);
+    window_.clear();
+    ++stamp_;
 }
 
 void FrameBuilder::open_range() { prog.launches.push_back({-1, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size()}); }
@@ -79,6 +108,7 @@ void FrameBuilder::channel(int64_t a, int64_t b, uint32_t slot) {
 }
 
 void FrameBuilder::end_segment() {
+    flush_window();
     if (slot_rows_.empty()) {  // no channels: nothing sampled, nothing to apply
         seg_ = -1;
         return;
@@ -128,12 +158,13 @@ void FrameBuilder::row_xor(int64_t dst, int64_t src) {
 void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
     int64_t p = 0;
     while (p < n_ && !bit(x_, p + n_, q)) ++p;
-    FrameOp op{};
-    op.arg = meas_index;
-    op.off = (uint32_t)prog.tab.size();
     const int64_t s = 2 * n_;
-    if (p < n_) {  // MeasureRandom (:225-265)
+    if (p < n_) {  // MeasureRandom (:225-265), in program order after the open window
+        flush_window();
+        FrameOp op{};
         op.kind = F_MEAS_RAND;
+        op.arg = meas_index;
+        op.off = (uint32_t)prog.tab.size();
         prog.tab.push_back((uint32_t)p);
         for (int64_t t = 0; t < nw_; ++t) {  // row p := row p+n; row p+n := Z_q
             x_[(size_t)(p * nw_ + t)] = x_[(size_t)((p + n_) * nw_ + t)];
@@ -150,38 +181,49 @@ void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
                 prog.tab.push_back((uint32_t)i | c << 31);
                 row_xor(i, p);
             }
-    } else {  // MeasureDetermined (:189-201): scratch row := product of the selected stabilizers
-        op.kind = F_MEAS_DET;
-        for (int64_t t = 0; t < nw_; ++t) {
-            x_[(size_t)(s * nw_ + t)] = 0ull;
-            z_[(size_t)(s * nw_ + t)] = 0ull;
+        op.len = (uint32_t)prog.tab.size() - op.off;
+        push_op(op);
+        if (reset) {
+            FrameOp ro{};
+            ro.kind = F_RESET_X;
+            ro.off = (uint32_t)prog.tab.size();
+            for (int64_t i = 0; i < W_; ++i)
+                if (bit(z_, i, q)) prog.tab.push_back((uint32_t)i);
+            ro.len = (uint32_t)prog.tab.size() - ro.off;
+            push_op(ro);
         }
-        uint32_t c = 0;
-        for (int64_t i = 0; i < n_; ++i)
-            if (bit(x_, i, q)) {
-                c ^= (uint32_t)(phase_bit(s, i + n_) ^ f_[(size_t)(i + n_)]);
-                prog.tab.push_back((uint32_t)(i + n_));
-                row_xor(s, i + n_);
-            }
-        op.kind |= c << 8;
-        f_[(size_t)s] = 0;
+        return;
     }
-    op.len = (uint32_t)prog.tab.size() - op.off;
-    prog.ops.push_back(op);
-    prog.launches.back().op1 = (uint32_t)prog.ops.size();
-    if (reset) {
-        FrameOp ro{};
-        ro.kind = F_RESET_X;
-        ro.off = (uint32_t)prog.tab.size();
+    // MeasureDetermined (:189-201): scratch row := product of the selected stabilizers
+    DetRecord r;
+    r.meas = meas_index;
+    for (int64_t t = 0; t < nw_; ++t) {
+        x_[(size_t)(s * nw_ + t)] = 0ull;
+        z_[(size_t)(s * nw_ + t)] = 0ull;
+    }
+    uint32_t c = 0;
+    bool hazard = false;
+    for (int64_t i = 0; i < n_; ++i)
+        if (bit(x_, i, q)) {
+            c ^= (uint32_t)(phase_bit(s, i + n_) ^ f_[(size_t)(i + n_)]);
+            r.rd.push_back((uint32_t)(i + n_));
+            hazard |= flipped_[(size_t)(i + n_)] == stamp_;
+            row_xor(s, i + n_);
+        }
+    r.c = c;
+    f_[(size_t)s] = 0;
+    if (hazard || window_.size() == 32) flush_window();
+    if (reset)
         for (int64_t i = 0; i < W_; ++i)
-            if (bit(z_, i, q)) prog.tab.push_back((uint32_t)i);
-        ro.len = (uint32_t)prog.tab.size() - ro.off;
-        prog.ops.push_back(ro);
-        prog.launches.back().op1 = (uint32_t)prog.ops.size();
-    }
+            if (bit(z_, i, q)) {
+                r.rs.push_back((uint32_t)i);
+                flipped_[(size_t)i] = stamp_;
+            }
+    window_.push_back(std::move(r));
 }
 
 void FrameBuilder::finish() {
+    flush_window();
     FrameOp op{};
     op.kind = F_FLIP;
     op.off = (uint32_t)prog.tab.size();

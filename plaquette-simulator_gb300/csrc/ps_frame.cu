@@ -13,8 +13,9 @@ namespace ps {
 namespace {
 
 // One warp per shot-word: its W signs live in shared memory while the warp
-// runs ops [op0, op1) in order; lanes spread over each op's rows (the rows
-// of one op are distinct, so the XORs of one op never collide).
+// runs ops [op0, op1) in order.  Channel outcomes go one per lane (XORs
+// commute; shared atomics where two outcomes flip one row), a window's
+// measurements one per lane, the rows of other ops over the lanes.
 __global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t n, int64_t w,
                                                    const FrameOp *__restrict__ ops, uint32_t op0, uint32_t op1,
                                                    const uint32_t *__restrict__ tab,
@@ -37,20 +38,39 @@ __global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t 
         if (kind == F_NOISE) {
             const int cnt = entry_count[k];
             const NoiseEntry *ent = entries + k * (int64_t)cap;
-            for (int e = 0; e < cnt; ++e) {
+            for (int e = lane; e < cnt; e += 32) {
                 const NoiseEntry en = ent[e];
                 const uint32_t t1 = slot_off[o.arg + en.layer + 1];
-                for (uint32_t t = slot_off[o.arg + en.layer] + lane; t < t1; t += 32) {
+                for (uint32_t t = slot_off[o.arg + en.layer]; t < t1; ++t) {
                     const uint32_t v = tab[t], sel = v >> 28;
                     u64 m = 0ull;
                     if (sel & 1u) m ^= en.fxa;
                     if (sel & 2u) m ^= en.fza;
                     if (sel & 4u) m ^= en.fxb;
                     if (sel & 8u) m ^= en.fzb;
-                    sR[v & kFrameRowMask] ^= m;
+                    atomicXor(&sR[v & kFrameRowMask], m);
                 }
-                __syncwarp();
             }
+            __syncwarp();
+        } else if (kind == F_WINDOW) {
+            u64 acc = 0ull;
+            uint32_t rec = 0, nrd = 0, nrs = 0;
+            if ((uint32_t)lane < o.len) {
+                rec = o.off + tab[o.off + lane];
+                const uint32_t m = tab[rec], hdr = tab[rec + 1];
+                nrd = hdr & 0xFFFFu;
+                nrs = (hdr >> 16) & 0x7FFFu;
+                acc = (hdr >> 31) ? ~0ull : 0ull;
+                for (uint32_t t = 0; t < nrd; ++t) acc ^= sR[tab[rec + 2 + t]];
+                const MeasOp &mo = meas[m];
+                mo.res[k] = acc;
+                mo.det[k] = ~0ull;
+                if ((uint32_t)lane == o.len - 1) sR[2 * n] = acc;
+            }
+            __syncwarp();
+            for (uint32_t t = 0; t < nrs; ++t) atomicXor(&sR[tab[rec + 2 + nrd + t]], acc);
+            last = __shfl_sync(0xffffffffu, acc, (int)o.len - 1);
+            __syncwarp();
         } else if (kind == F_MEAS_DET) {
             u64 acc = 0ull;
             for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) acc ^= sR[tab[t]];

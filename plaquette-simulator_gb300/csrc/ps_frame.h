@@ -38,7 +38,18 @@ enum FrameKind : uint32_t {
     F_MEAS_RAND = 2,  // arg = MeasOp; tab[off] = p, then rows | c << 31
     F_RESET_X = 3,    // R[row] ^= outcome of the last measurement, rows tab[off..off+len)
     F_FLIP = 4,       // R[row] ^= ~0, rows tab[off..off+len)
+    F_WINDOW = 5,     // len deterministic measurements, one per lane (below)
 };
+
+// A window of deterministic measurements (each with its reset X) that run
+// at once, one per lane: every lane reads its rows first, the last one
+// writes the scratch row, then the resets XOR their outcomes in (shared
+// atomics; XORs commute).  The builder closes a window before a measurement
+// that reads a row an earlier reset of the window flips (a reset that flips
+// a row an earlier measurement read is fine: reads come first), and drops
+// the scratch row from every reset but the last one's (the last measurement
+// overwrites it).  tab[off + j] = offset of record j from off; a record is
+// [MeasOp index][nread | nreset << 16 | c << 31][read rows][reset rows].
 
 struct FrameOp {
     uint32_t kind;  // FrameKind | constant bit << 8
@@ -79,12 +90,23 @@ class FrameBuilder {
     void finish();
     FrameProgram prog;
 
+    struct DetRecord {
+        int32_t meas;
+        uint32_t c;
+        std::vector<uint32_t> rd, rs;
+    };
+
   private:
     int64_t n_, W_, nw_;
     std::vector<uint64_t> x_, z_;  // row-major [W][nw]
     std::vector<uint8_t> f_;       // pending constant flips per row
     int32_t seg_ = -1;
     std::vector<std::vector<uint32_t>> slot_rows_;
+    std::vector<DetRecord> window_;
+    std::vector<uint32_t> flipped_;  // row -> window stamp of a reset flip in the open window
+    uint32_t stamp_ = 1;
+    void flush_window();
+    void push_op(const FrameOp &op);
     bool bit(const std::vector<uint64_t> &m, int64_t row, int64_t q) const {
         return (m[(size_t)(row * nw_ + (q >> 6))] >> (q & 63)) & 1ull;
     }

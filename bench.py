@@ -372,9 +372,9 @@ def main():
 
     # ---- roofline: per-kind device time of one run (events around launches)
     prof = fused.profile(reset=True)
-    meas_bytes = fused.measure_bytes(reset=True)
-    seg_bytes = float(fused.stats["segment_bytes"])
-    dom = max(("segment", "measure"), key=lambda k: prof[k]["ms"])
+    shared = bool(fused.stats["shared_xz"])
+    n_q = circ.num_qubits
+    W = 2 * n_q + 1
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -382,21 +382,49 @@ def main():
     except OSError:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    dom_bytes = seg_bytes if dom == "segment" else meas_bytes
-    dom_ms = prof[dom]["ms"]
+    seg_bytes = meas_bytes = None
+    if shared:
+        # Algorithmic bytes of the shared-x/z plan (per run):
+        #  sign program: every launch reads and writes the signs of all rows
+        #    and shot-words (the first starts from zero), plus the records
+        #    (result + determined words per measurement);
+        #  x/z broadcast: the x and z words of every row, qubit and shot-word;
+        #  channel sampling: 4 outcome words written and read back per
+        #    (channel, shot-word).
+        nl = max(1, prof["sign_program"]["launches"])
+        kind_bytes = {
+            "sign_program": (2 * nl - 1) * W * w_words * 8 + 2 * nm * w_words * 8,
+            "xz_broadcast": 2 * W * n_q * w_words * 8,
+            "channel_sample": 2 * 4 * 8 * int(fused.stats["num_channels"]) * w_words,
+        }
+        kernel_of = {"sign_program": "frame_kernel", "xz_broadcast": "broadcast_xz_kernel",
+                     "channel_sample": "noise_dense_kernel + noise_compact_kernel"}
+    else:
+        meas_bytes = fused.measure_bytes(reset=True)
+        seg_bytes = float(fused.stats["segment_bytes"])
+        kind_bytes = {"segment": seg_bytes, "measure": meas_bytes}
+        kernel_of = {"segment": "segment_kernel", "measure": "measure_kernel"}
+    dom = max(kind_bytes, key=lambda k: prof[k]["ms"])
+    dom_bytes, dom_ms = kind_bytes[dom], prof[dom]["ms"]
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
-    # DRAM bytes per segment launch from one ncu capture of the d=15 circuit at
-    # 32 shot-words (profiles/dram_traffic_surface_d15_s2048.md: 207.1 MB read
-    # + 147.9 MB written), scaled by shot-words; traffic grows with the words.
     traffic = None
     if dom == "segment" and meta["distance"] == 15:
+        # DRAM bytes per segment launch from one ncu capture of the d=15
+        # circuit at 32 shot-words (profiles/dram_traffic_surface_d15_s2048.md:
+        # 207.1 MB read + 147.9 MB written), scaled by shot-words.
         traffic = (207.1e6 + 147.9e6) / 32 * w_words
-    roofline = {"bound": "hbm", "kernel": "segment_kernel" if dom == "segment" else "measure_kernel",
+    roofline = {"bound": "hbm", "kernel": kernel_of[dom],
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
                 "traffic": traffic,
                 "algorithmic_bytes_per_launch": dom_bytes / max(1, prof[dom]["launches"]),
-                "avg_launch_ms": dom_ms / max(1, prof[dom]["launches"])}
+                "avg_launch_ms": dom_ms / max(1, prof[dom]["launches"]),
+                "kinds": {k: {"ms": round(prof[k]["ms"], 4), "launches": prof[k]["launches"],
+                              "algorithmic_GBps": kind_bytes[k] / max(1e-9, prof[k]["ms"] / 1e3) / 1e9}
+                          for k in kind_bytes}}
+    if dom == "sign_program":
+        roofline["note"] = ("latency-bound: one warp per shot-word runs the sign program's ops in order on "
+                            "signs held in shared memory; it moves little HBM data by design")
 
     line = {
         "metric": METRIC, "value": value, "unit": "shot-gates/s", "n_gpus": world, "steps": args.steps,
@@ -404,7 +432,7 @@ def main():
         "vs_baseline": None, "dtype": "u64 bit-packed GF(2) (1 bit per tableau entry)",
         "data": "synthetic: seeded rotated surface-code memory circuit, Philox4x32-10 noise and outcomes",
         "config": {"workload": f"surface_code_memory d={meta['distance']} rounds={meta['rounds']} p={meta['p']} "
-                               f"Z-basis, fused + CUDA graph",
+                               f"Z-basis, fused + CUDA graph" + (", shared x/z" if shared else ""),
                    "num_qubits": circ.num_qubits, "shots": shots, "gates_per_shot": gates,
                    "tableau_bytes": 3 * (2 * circ.num_qubits + 1) * circ.num_qubits * ((shots + 63) // 64) * 8,
                    "l2": "no flush needed: the 1.65 GB tableau is larger than the 129 MB L2",
@@ -417,10 +445,21 @@ def main():
                         "16 H2D bytes are the run parameters (seed, event base)"},
         "roofline": roofline,
         "profile_ms": {k: round(v["ms"], 3) for k, v in prof.items() if v["launches"]},
-        "algorithmic_bytes_per_step": {"segments": seg_bytes, "measurements": meas_bytes,
-                                        "whole_run_GBps": (seg_bytes + meas_bytes) / (ms / 1e3) / 1e9},
+        "plan": "shared x/z: x and z simulated once on the host, a sign program per shot-word on the device, "
+                "final x / z written to every shot" if shared else "per-shot tableau",
+        "algorithmic_bytes_per_step": {k: float(v) for k, v in kind_bytes.items()},
     }
 
+    if not args.no_plain and shared:
+        per_shot = CompiledCircuit(circ, st, fused=True, graph=True, shared_xz=False)
+        per_shot.run(reset=True)
+        k = max(1, min(3, args.steps))
+        qms = time_steps(per_shot, k)
+        qprof = per_shot.profile(reset=True)
+        line["per_shot_plan"] = {"ms_per_step": qms, "value": gates * shots * world / (qms / 1e3), "steps": k,
+                                 "profile_ms": {kk: round(v["ms"], 3) for kk, v in qprof.items() if v["launches"]},
+                                 "form": "fused segments and measurement phases over every shot's tableau"}
+        del per_shot
     if not args.no_plain:
         plain = CompiledCircuit(circ, st, fused=False, graph=True)
         plain.run(reset=True)

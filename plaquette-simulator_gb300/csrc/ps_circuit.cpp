@@ -793,15 +793,18 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
         return rc;
     };
     bool first = true;
+    // The one-pass sampler appends to per-word lists from a zero count (each
+    // sign kernel zeroes the lists it consumed; a per-shot run leaves counts).
+    if (c->d_entry_count) PS_CUDA(cudaMemsetAsync(c->d_entry_count, 0, (size_t)h->w * sizeof(int32_t), st));
     for (const FrameProgram::Launch &L : c->fprog.launches) {
         int rc = OK;
         if (L.seg >= 0)
-            rc = timed(P_SAMPLE, [&] { return launch_noise_sample(st, c->segs[(size_t)L.seg].dev, h->w, c->d_params, 1); });
+            rc = timed(P_SAMPLE, [&] { return launch_noise_sample_frame(st, c->segs[(size_t)L.seg].dev, h->w, c->d_params); });
         if (rc == OK)
             rc = timed(P_FRAME, [&] {
-                return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, c->d_fslot, c->d_meas,
-                                    c->d_entries, c->d_entry_count, c->entry_cap, (uint64_t)h->seed, c->d_params,
-                                    first ? 1 : 0);
+                return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, L.tab0, L.tab1,
+                                    c->d_fslot, c->d_meas, c->d_res_block, (int64_t)c->meas.size(), c->d_entries,
+                                    c->d_entry_count, c->entry_cap, (uint64_t)h->seed, c->d_params, first ? 1 : 0);
             });
         if (rc != OK) return rc;
         first = false;

@@ -23,6 +23,7 @@ FrameBuilder::FrameBuilder(int64_t n) : n_(n), W_(2 * n + 1), nw_((n + 63) / 64)
 
 void FrameBuilder::push_op(const FrameOp &op) {
     prog.ops.push_back(op);
+    op_tab_end_.push_back((uint32_t)prog.tab.size());
     prog.launches.back().op1 = (uint32_t)prog.ops.size();
 }
 
@@ -49,7 +50,9 @@ void FrameBuilder::flush_window() {
     ++stamp_;
 }
 
-void FrameBuilder::open_range() { prog.launches.push_back({-1, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size()}); }
+void FrameBuilder::open_range() {
+    prog.launches.push_back({-1, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size(), 0, 0});
+}
 
 // The gate functors of GateFunctors.hpp over all W rows (scratch included,
 // CliffordState.hpp:381-386): x / z updated here, the sign term folded into f.
@@ -121,12 +124,11 @@ void FrameBuilder::end_segment() {
     prog.slot_off.push_back((uint32_t)prog.tab.size());
     // A new launch: its sampling precedes it, then this segment's noise.
     if (prog.launches.back().op0 == prog.launches.back().op1) prog.launches.pop_back();
-    prog.launches.push_back({seg_, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size()});
+    prog.launches.push_back({seg_, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size(), 0, 0});
     FrameOp op{};
     op.kind = F_NOISE;
     op.arg = (int32_t)base;
-    prog.ops.push_back(op);
-    prog.launches.back().op1 = (uint32_t)prog.ops.size();
+    push_op(op);
     slot_rows_.clear();
     seg_ = -1;
 }
@@ -230,8 +232,17 @@ void FrameBuilder::finish() {
     for (int64_t i = 0; i < W_; ++i)
         if (f_[(size_t)i]) prog.tab.push_back((uint32_t)i);
     op.len = (uint32_t)prog.tab.size() - op.off;
-    prog.ops.push_back(op);
-    prog.launches.back().op1 = (uint32_t)prog.ops.size();
+    push_op(op);
+    for (FrameProgram::Launch &L : prog.launches) {  // tab range of the measurement ops
+        L.tab0 = L.tab1 = 0;
+        bool any = false;
+        for (uint32_t i = L.op0; i < L.op1; ++i) {
+            if ((prog.ops[i].kind & 0xFFu) == F_NOISE) continue;
+            if (!any) L.tab0 = prog.ops[i].off;
+            L.tab1 = op_tab_end_[i];
+            any = true;
+        }
+    }
     prog.xz.assign((size_t)(W_ * 2 * nw_), 0ull);
     for (int64_t i = 0; i < W_; ++i)
         for (int64_t t = 0; t < nw_; ++t) {

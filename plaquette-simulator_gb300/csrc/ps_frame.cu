@@ -15,25 +15,40 @@ namespace {
 // One warp per shot-word: its W signs live in shared memory while the warp
 // runs ops [op0, op1) in order.  Channel outcomes go one per lane (XORs
 // commute; shared atomics where two outcomes flip one row), a window's
-// measurements one per lane, the rows of other ops over the lanes.
+// measurements one per lane, the rows of other ops over the lanes.  When
+// `stage` is set the launch's ops and the tab range [tab0, tab0 + ntab) of
+// its measurement ops are first copied to shared memory, so the op stream
+// runs on shared-memory latency; channel rows stay in global memory (a word
+// uses few of them).  Record k of the circuit lives at rec + k*w (results)
+// and rec + (nm + k)*w (determined flags).
 __global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t n, int64_t w,
                                                    const FrameOp *__restrict__ ops, uint32_t op0, uint32_t op1,
-                                                   const uint32_t *__restrict__ tab,
-                                                   const uint32_t *__restrict__ slot_off,
-                                                   const MeasOp *__restrict__ meas,
-                                                   const NoiseEntry *__restrict__ entries,
-                                                   const int32_t *__restrict__ entry_count, int32_t cap,
-                                                   uint64_t seed, const RunParams *__restrict__ rp, int from_zero) {
+                                                   const uint32_t *__restrict__ tab, uint32_t tab0, uint32_t ntab,
+                                                   int stage, const uint32_t *__restrict__ slot_off,
+                                                   const MeasOp *__restrict__ meas, u64 *__restrict__ rec,
+                                                   int64_t nm, const NoiseEntry *__restrict__ entries,
+                                                   int32_t *__restrict__ entry_count, int32_t cap, uint64_t seed,
+                                                   const RunParams *__restrict__ rp, int from_zero) {
     extern __shared__ u64 sR[];
     const int64_t W = 2 * n + 1;
     const int lane = threadIdx.x;
     const int64_t k = blockIdx.x;
+    uint32_t *stab = reinterpret_cast<uint32_t *>(sR + W);
+    FrameOp *sops = reinterpret_cast<FrameOp *>(((uintptr_t)(stab + ntab) + 15) & ~(uintptr_t)15);
     for (int64_t i = lane; i < W; i += 32) sR[i] = from_zero ? 0ull : R[i * w + k];
+    if (stage) {
+        for (uint32_t i = lane; i < ntab; i += 32) stab[i] = tab[tab0 + i];
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(ops + op0);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(sops);
+        for (uint32_t i = lane; i < 4 * (op1 - op0); i += 32) dst[i] = src[i];
+    }
     __syncwarp();
+    const uint32_t *T = stage ? stab : tab;  // measurement-op tab, indexed x - tb
+    const uint32_t tb = stage ? tab0 : 0u;
     const uint64_t event_base = rp->event_base, word_base = rp->word_base;
     u64 last = 0ull;  // outcome of the latest measurement (its reset X)
     for (uint32_t oi = op0; oi < op1; ++oi) {
-        const FrameOp o = ops[oi];
+        const FrameOp o = stage ? sops[oi - op0] : ops[oi];
         const uint32_t kind = o.kind & 0xFFu;
         if (kind == F_NOISE) {
             const int cnt = entry_count[k];
@@ -41,72 +56,65 @@ __global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t 
             for (int e = lane; e < cnt; e += 32) {
                 const NoiseEntry en = ent[e];
                 const uint32_t t1 = slot_off[o.arg + en.layer + 1];
-                for (uint32_t t = slot_off[o.arg + en.layer]; t < t1; ++t) {
-                    const uint32_t v = tab[t], sel = v >> 28;
-                    u64 m = 0ull;
-                    if (sel & 1u) m ^= en.fxa;
-                    if (sel & 2u) m ^= en.fza;
-                    if (sel & 4u) m ^= en.fxb;
-                    if (sel & 8u) m ^= en.fzb;
-                    atomicXor(&sR[v & kFrameRowMask], m);
+                for (uint32_t t = slot_off[o.arg + en.layer]; t < t1; t += 4) {
+                    uint32_t v[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) v[u] = t + u < t1 ? tab[t + u] : 0u;  // a row entry is never 0 (sel != 0)
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (v[u] == 0u) continue;
+                        const uint32_t sel = v[u] >> 28;
+                        u64 m = 0ull;
+                        if (sel & 1u) m ^= en.fxa;
+                        if (sel & 2u) m ^= en.fza;
+                        if (sel & 4u) m ^= en.fxb;
+                        if (sel & 8u) m ^= en.fzb;
+                        atomicXor(&sR[v[u] & kFrameRowMask], m);
+                    }
                 }
             }
             __syncwarp();
+            if (lane == 0) entry_count[k] = 0;  // consumed: the next segment's sampling appends from 0
         } else if (kind == F_WINDOW) {
             u64 acc = 0ull;
-            uint32_t rec = 0, nrd = 0, nrs = 0;
+            uint32_t r0 = 0, nrd = 0, nrs = 0;
             if ((uint32_t)lane < o.len) {
-                rec = o.off + tab[o.off + lane];
-                const uint32_t m = tab[rec], hdr = tab[rec + 1];
+                r0 = o.off + T[o.off + lane - tb];
+                const uint32_t m = T[r0 - tb], hdr = T[r0 + 1 - tb];
                 nrd = hdr & 0xFFFFu;
                 nrs = (hdr >> 16) & 0x7FFFu;
                 acc = (hdr >> 31) ? ~0ull : 0ull;
-                for (uint32_t t = 0; t < nrd; ++t) acc ^= sR[tab[rec + 2 + t]];
-                const MeasOp &mo = meas[m];
-                mo.res[k] = acc;
-                mo.det[k] = ~0ull;
+                for (uint32_t t = 0; t < nrd; ++t) acc ^= sR[T[r0 + 2 + t - tb]];
+                rec[(int64_t)m * w + k] = acc;
+                rec[(nm + (int64_t)m) * w + k] = ~0ull;
                 if ((uint32_t)lane == o.len - 1) sR[2 * n] = acc;
             }
             __syncwarp();
-            for (uint32_t t = 0; t < nrs; ++t) atomicXor(&sR[tab[rec + 2 + nrd + t]], acc);
+            for (uint32_t t = 0; t < nrs; ++t) atomicXor(&sR[T[r0 + 2 + nrd + t - tb]], acc);
             last = __shfl_sync(0xffffffffu, acc, (int)o.len - 1);
             __syncwarp();
-        } else if (kind == F_MEAS_DET) {
-            u64 acc = 0ull;
-            for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) acc ^= sR[tab[t]];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, off);
-            if (o.kind >> 8) acc = ~acc;
-            if (lane == 0) {
-                const MeasOp &m = meas[o.arg];
-                m.res[k] = acc;
-                m.det[k] = ~0ull;
-                sR[2 * n] = acc;
-            }
-            last = acc;
-            __syncwarp();
         } else if (kind == F_MEAS_RAND) {
-            const MeasOp m = meas[o.arg];
+            const MeasOp &m = meas[o.arg];
             const u64 out = outcome_bits(m, lane, seed, event_base, k, word_base);
-            const uint32_t p = tab[o.off];
+            const uint32_t p = T[o.off - tb];
             const u64 rpv = sR[p + n];
             __syncwarp();
             if (lane == 0) {
                 sR[p] = rpv;
                 sR[p + n] = out;
-                m.res[k] = out;
-                m.det[k] = 0ull;
+                rec[(int64_t)o.arg * w + k] = out;
+                rec[(nm + (int64_t)o.arg) * w + k] = 0ull;
             }
             __syncwarp();
             for (uint32_t t = o.off + 1 + lane; t < o.off + o.len; t += 32) {
-                const uint32_t v = tab[t];
+                const uint32_t v = T[t - tb];
                 sR[v & 0x7FFFFFFFu] ^= rpv ^ ((v >> 31) ? ~0ull : 0ull);
             }
             last = out;
             __syncwarp();
         } else {  // F_RESET_X, F_FLIP
             const u64 m = kind == F_RESET_X ? last : ~0ull;
-            for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) sR[tab[t]] ^= m;
+            for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) sR[T[t - tb]] ^= m;
             __syncwarp();
         }
     }
@@ -140,15 +148,21 @@ int g_frame_sms = 0;
 size_t frame_smem_bytes(int64_t n) { return (size_t)(2 * n + 1) * sizeof(u64); }
 
 int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
-                 const uint32_t *tab, const uint32_t *slot_off, const MeasOp *meas, const NoiseEntry *entries,
-                 const int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero) {
-    const size_t smem = frame_smem_bytes(n);
+                 const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const MeasOp *meas,
+                 u64 *rec, int64_t nm, const NoiseEntry *entries, int32_t *entry_count, int32_t cap, uint64_t seed,
+                 const RunParams *rp, int from_zero) {
+    // Staging keeps a CTA's shared memory small enough for two per SM.
+    const size_t base = frame_smem_bytes(n);
+    const size_t staged = base + (size_t)(tab1 - tab0) * 4 + 16 + (size_t)(op1 - op0) * sizeof(FrameOp);
+    const int stage = staged <= kFrameStageMax ? 1 : 0;
+    const size_t smem = stage ? staged : base;
+    const uint32_t ntab = stage ? tab1 - tab0 : 0u;
     if (smem > 48 * 1024) {
         const int rc = allow_max_smem((const void *)frame_kernel);
         if (rc != OK) return rc;
     }
-    frame_kernel<<<(unsigned)w, 32, smem, st>>>(R, n, w, ops, op0, op1, tab, slot_off, meas, entries, entry_count, cap,
-                                                seed, rp, from_zero);
+    frame_kernel<<<(unsigned)w, 32, smem, st>>>(R, n, w, ops, op0, op1, tab, tab0, ntab, stage, slot_off, meas, rec,
+                                                nm, entries, entry_count, cap, seed, rp, from_zero);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

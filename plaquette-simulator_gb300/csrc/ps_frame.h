@@ -72,6 +72,7 @@ struct FrameProgram {
     struct Launch {
         int32_t seg;
         uint32_t op0, op1;
+        uint32_t tab0, tab1;  // tab range of the launch's measurement ops (staged in shared memory)
     };
     std::vector<Launch> launches;
 };
@@ -105,6 +106,7 @@ class FrameBuilder {
     std::vector<DetRecord> window_;
     std::vector<uint32_t> flipped_;  // row -> window stamp of a reset flip in the open window
     uint32_t stamp_ = 1;
+    std::vector<uint32_t> op_tab_end_;  // tab extent end of every op
     void flush_window();
     void push_op(const FrameOp &op);
     bool bit(const std::vector<uint64_t> &m, int64_t row, int64_t q) const {

@@ -152,6 +152,9 @@ constexpr size_t kSegSmemMax = 227 * 1024;
 // slot_tags: entries carry their slot index instead of their layer.
 int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
                         int slot_tags = 0);
+// Shared-x/z runs: one-pass sampling into unordered per-word lists (slot
+// tags; the counters must be zero before, the sign kernel zeroes them after).
+int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp);
 int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
                    int rows, int bw, int threads, const u64 *const *recs);
 
@@ -161,9 +164,13 @@ struct NoiseEntry;
 size_t frame_smem_bytes(int64_t n);
 // Ops [op0, op1) of a sign program over every shot-word's signs R (from_zero:
 // the signs start at 0, the tableau having just been reset).
+// tab[tab0, tab1): the measurement ops' rows, staged in shared memory when
+// they fit (kFrameStageMax); rec: the circuit's record block.
+constexpr size_t kFrameStageMax = 100 * 1024;
 int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
-                 const uint32_t *tab, const uint32_t *slot_off, const MeasOp *meas, const NoiseEntry *entries,
-                 const int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero);
+                 const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const MeasOp *meas,
+                 u64 *rec, int64_t nm, const NoiseEntry *entries, int32_t *entry_count, int32_t cap, uint64_t seed,
+                 const RunParams *rp, int from_zero);
 // X, Z of every shot := the shared bits xz ([2n+1][2][nw64]).
 int launch_broadcast_xz(cudaStream_t st, u64 *X, u64 *Z, int64_t n, int64_t w, const uint64_t *xz, int64_t nw64);
 

@@ -107,6 +107,51 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
     if (lane == 0) seg.entry_count[k] = count;
 }
 
+// Channel sampling for shared-x/z runs, in one pass: one thread per
+// (channel slot, word) draws the word's 16 Philox blocks (the same draws,
+// keyed by (seed, event, global word, block), as the two-pass sampler) and
+// appends a non-identity outcome to the word's list with an atomic counter.
+// The list is unordered -- outcomes are XORs tagged with their slot -- and
+// its counter is zeroed by the sign kernel that consumes it.
+__global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = (int)(t / w);
+    const int64_t k = t - (int64_t)s * w;
+    if (s >= seg.nslots) return;
+    const NoiseSlot sl = seg.slots[s];
+    const uint64_t *thr = seg.thr + sl.thr_off;
+    const uint64_t total = thr[sl.count - 1];
+    const uint64_t ev = rp->event_base + sl.event, word = rp->word_base + (uint64_t)k, seed = rp->seed;
+    u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
+    for (uint32_t sub = 0; sub < 16; ++sub) {
+        const u32x4 u = draw_block(seed, ev, word, sub, TAG_NOISE);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const uint64_t v = u.v[l];
+            if (v >= total) continue;  // identity, the common case
+            int idx = 1;
+            while (v >= thr[idx - 1]) ++idx;
+            const u64 bit = 1ull << (sub * 4 + l);
+            const int pa = sl.count == 3 ? idx : (idx >> 2), pb = sl.count == 3 ? 0 : (idx & 3);
+            if (pa == 1 || pa == 2) fxa |= bit;
+            if (pa == 2 || pa == 3) fza |= bit;
+            if (pb == 1 || pb == 2) fxb |= bit;
+            if (pb == 2 || pb == 3) fzb |= bit;
+        }
+    }
+    if ((fxa | fza | fxb | fzb) == 0ull) return;
+    const int pos = atomicAdd(&seg.entry_count[k], 1);
+    NoiseEntry e;
+    e.fxa = fxa;
+    e.fza = fza;
+    e.fxb = fxb;
+    e.fzb = fzb;
+    e.layer = s;
+    e.a = 0;
+    e.b = 0;
+    seg.entries[k * (int64_t)seg.cap + pos] = e;
+}
+
 // Tile cell: x and z of one (row, word, column) side by side, so a gate
 // reads / writes a column with one 16-byte shared-memory access.
 typedef ulonglong2 XZ;
@@ -742,6 +787,14 @@ int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, c
     PS_CUDA(cudaGetLastError());
     const int wpb = 4;
     noise_compact_kernel<<<(unsigned)((w + wpb - 1) / wpb), 32 * wpb, 0, stream>>>(seg, w, slot_tags);
+    PS_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp) {
+    if (seg.nslots == 0) return OK;
+    const int64_t threads = (int64_t)seg.nslots * w;
+    noise_frame_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(seg, w, rp);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

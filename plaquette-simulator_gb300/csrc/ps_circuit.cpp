@@ -799,7 +799,10 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
     for (const FrameProgram::Launch &L : c->fprog.launches) {
         int rc = OK;
         if (L.seg >= 0)
-            rc = timed(P_SAMPLE, [&] { return launch_noise_sample_frame(st, c->segs[(size_t)L.seg].dev, h->w, c->d_params); });
+            rc = timed(P_SAMPLE, [&] {
+                return launch_noise_sample_frame(st, c->segs[(size_t)L.seg].dev, h->w, c->d_params, c->d_fslot,
+                                                 (uint32_t)c->fprog.ops[L.op0].arg);
+            });
         if (rc == OK)
             rc = timed(P_FRAME, [&] {
                 return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, L.tab0, L.tab1,

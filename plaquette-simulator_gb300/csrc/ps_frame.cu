@@ -12,16 +12,20 @@ namespace ps {
 
 namespace {
 
-// One warp per shot-word: its W signs live in shared memory while the warp
-// runs ops [op0, op1) in order.  Channel outcomes go one per lane (XORs
-// commute; shared atomics where two outcomes flip one row), a window's
-// measurements one per lane, the rows of other ops over the lanes.  When
+// One CTA of FW warps per shot-word: its W signs live in shared memory while
+// it runs ops [op0, op1) in order.  Channel outcomes go one per thread over
+// all warps (XORs commute; shared atomics where two outcomes flip one row);
+// the measurement ops run on warp 0 -- a window's measurements one per
+// lane, the rows of other ops over the lanes -- with block barriers around
+// every channel op.  When
 // `stage` is set the launch's ops and the tab range [tab0, tab0 + ntab) of
 // its measurement ops are first copied to shared memory, so the op stream
 // runs on shared-memory latency; channel rows stay in global memory (a word
 // uses few of them).  Record k of the circuit lives at rec + k*w (results)
 // and rec + (nm + k)*w (determined flags).
-__global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t n, int64_t w,
+constexpr int FW = 4;  // warps per shot-word
+
+__global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, int64_t n, int64_t w,
                                                    const FrameOp *__restrict__ ops, uint32_t op0, uint32_t op1,
                                                    const uint32_t *__restrict__ tab, uint32_t tab0, uint32_t ntab,
                                                    int stage, const uint32_t *__restrict__ slot_off,
@@ -31,18 +35,18 @@ __global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t 
                                                    const RunParams *__restrict__ rp, int from_zero) {
     extern __shared__ u64 sR[];
     const int64_t W = 2 * n + 1;
-    const int lane = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int64_t k = blockIdx.x;
     uint32_t *stab = reinterpret_cast<uint32_t *>(sR + W);
     FrameOp *sops = reinterpret_cast<FrameOp *>(((uintptr_t)(stab + ntab) + 15) & ~(uintptr_t)15);
-    for (int64_t i = lane; i < W; i += 32) sR[i] = from_zero ? 0ull : R[i * w + k];
+    for (int64_t i = tid; i < W; i += 32 * FW) sR[i] = from_zero ? 0ull : R[i * w + k];
     if (stage) {
-        for (uint32_t i = lane; i < ntab; i += 32) stab[i] = tab[tab0 + i];
+        for (uint32_t i = tid; i < ntab; i += 32 * FW) stab[i] = tab[tab0 + i];
         const uint32_t *src = reinterpret_cast<const uint32_t *>(ops + op0);
         uint32_t *dst = reinterpret_cast<uint32_t *>(sops);
-        for (uint32_t i = lane; i < 4 * (op1 - op0); i += 32) dst[i] = src[i];
+        for (uint32_t i = tid; i < 4 * (op1 - op0); i += 32 * FW) dst[i] = src[i];
     }
-    __syncwarp();
+    __syncthreads();
     const uint32_t *T = stage ? stab : tab;  // measurement-op tab, indexed x - tb
     const uint32_t tb = stage ? tab0 : 0u;
     const uint64_t event_base = rp->event_base, word_base = rp->word_base;
@@ -51,12 +55,13 @@ __global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t 
         const FrameOp o = stage ? sops[oi - op0] : ops[oi];
         const uint32_t kind = o.kind & 0xFFu;
         if (kind == F_NOISE) {
+            __syncthreads();  // warp 0's measurement ops before
             const int cnt = entry_count[k];
             const NoiseEntry *ent = entries + k * (int64_t)cap;
-            for (int e = lane; e < cnt; e += 32) {
-                const NoiseEntry en = ent[e];
-                const uint32_t t1 = slot_off[o.arg + en.layer + 1];
-                for (uint32_t t = slot_off[o.arg + en.layer]; t < t1; t += 4) {
+            for (int e = tid; e < cnt; e += 32 * FW) {
+                const NoiseEntry en = ent[e];  // layer: first row entry, a: row count
+                const uint32_t t1 = (uint32_t)en.layer + en.a;
+                for (uint32_t t = (uint32_t)en.layer; t < t1; t += 4) {
                     uint32_t v[4];
 #pragma unroll
                     for (int u = 0; u < 4; ++u) v[u] = t + u < t1 ? tab[t + u] : 0u;  // a row entry is never 0 (sel != 0)
@@ -73,8 +78,10 @@ __global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t 
                     }
                 }
             }
-            __syncwarp();
-            if (lane == 0) entry_count[k] = 0;  // consumed: the next segment's sampling appends from 0
+            __syncthreads();
+            if (tid == 0) entry_count[k] = 0;  // consumed: the next segment's sampling appends from 0
+        } else if (wid != 0) {
+            continue;  // the measurement ops run on warp 0
         } else if (kind == F_WINDOW) {
             u64 acc = 0ull;
             uint32_t r0 = 0, nrd = 0, nrs = 0;
@@ -118,7 +125,8 @@ __global__ void __launch_bounds__(32) frame_kernel(u64 *__restrict__ R, int64_t 
             __syncwarp();
         }
     }
-    for (int64_t i = lane; i < W; i += 32) R[i * w + k] = sR[i];
+    __syncthreads();
+    for (int64_t i = tid; i < W; i += 32 * FW) R[i * w + k] = sR[i];
 }
 
 // x / z of every shot from the shared bits: one warp per (row, qubit), lanes
@@ -161,7 +169,7 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
         const int rc = allow_max_smem((const void *)frame_kernel);
         if (rc != OK) return rc;
     }
-    frame_kernel<<<(unsigned)w, 32, smem, st>>>(R, n, w, ops, op0, op1, tab, tab0, ntab, stage, slot_off, meas, rec,
+    frame_kernel<<<(unsigned)w, 32 * FW, smem, st>>>(R, n, w, ops, op0, op1, tab, tab0, ntab, stage, slot_off, meas, rec,
                                                 nm, entries, entry_count, cap, seed, rp, from_zero);
     PS_CUDA(cudaGetLastError());
     return OK;

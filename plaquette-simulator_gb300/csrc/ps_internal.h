@@ -152,9 +152,11 @@ constexpr size_t kSegSmemMax = 227 * 1024;
 // slot_tags: entries carry their slot index instead of their layer.
 int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
                         int slot_tags = 0);
-// Shared-x/z runs: one-pass sampling into unordered per-word lists (slot
-// tags; the counters must be zero before, the sign kernel zeroes them after).
-int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp);
+// Shared-x/z runs: one-pass sampling into unordered per-word lists, each
+// outcome tagged with its slot's rows slot_off[base + s] .. [base + s + 1]
+// (the counters must be zero before; the sign kernel zeroes them after).
+int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
+                              const uint32_t *slot_off, uint32_t base);
 int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
                    int rows, int bw, int threads, const u64 *const *recs);
 

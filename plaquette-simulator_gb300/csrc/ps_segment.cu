@@ -111,9 +111,12 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
 // (channel slot, word) draws the word's 16 Philox blocks (the same draws,
 // keyed by (seed, event, global word, block), as the two-pass sampler) and
 // appends a non-identity outcome to the word's list with an atomic counter.
-// The list is unordered -- outcomes are XORs tagged with their slot -- and
-// its counter is zeroed by the sign kernel that consumes it.
-__global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp) {
+// The list is unordered -- outcomes are XORs -- and carries, instead of the
+// slot, the slot's rows in the sign program: layer = first row entry
+// (slot_off[base + s]), a = their count.  Its counter is zeroed by the sign
+// kernel that consumes it.
+__global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp,
+                                                          const uint32_t *__restrict__ slot_off, uint32_t base) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int s = (int)(t / w);
     const int64_t k = t - (int64_t)s * w;
@@ -140,14 +143,15 @@ __global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_
         }
     }
     if ((fxa | fza | fxb | fzb) == 0ull) return;
+    const uint32_t t0 = slot_off[base + s], t1 = slot_off[base + s + 1];
     const int pos = atomicAdd(&seg.entry_count[k], 1);
     NoiseEntry e;
     e.fxa = fxa;
     e.fza = fza;
     e.fxb = fxb;
     e.fzb = fzb;
-    e.layer = s;
-    e.a = 0;
+    e.layer = (int32_t)t0;
+    e.a = (uint16_t)(t1 - t0);
     e.b = 0;
     seg.entries[k * (int64_t)seg.cap + pos] = e;
 }
@@ -791,10 +795,11 @@ int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, c
     return OK;
 }
 
-int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp) {
+int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
+                              const uint32_t *slot_off, uint32_t base) {
     if (seg.nslots == 0) return OK;
     const int64_t threads = (int64_t)seg.nslots * w;
-    noise_frame_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(seg, w, rp);
+    noise_frame_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(seg, w, rp, slot_off, base);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

@@ -1277,6 +1277,19 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             if (upload(h, c->owned, c->fprog.ops, &c->d_fops) || upload(h, c->owned, c->fprog.tab, &c->d_ftab) ||
                 upload(h, c->owned, c->fprog.slot_off, &c->d_fslot) || upload(h, c->owned, c->fprog.xz, &c->d_fxz))
                 return bail(E_CUDA);
+            // Outcome lists hold one entry per row chunk of a slot.
+            if (c->fprog.entry_cap > c->entry_cap) {
+                void *p = nullptr;
+                if (dev_alloc(h, &p, (size_t)c->fprog.entry_cap * h->w * sizeof(NoiseEntry)) != OK)
+                    return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
+                c->owned.push_back(p);
+                c->d_entries = (NoiseEntry *)p;
+                c->entry_cap = c->fprog.entry_cap;
+                for (SegHost &sg : c->segs) {
+                    sg.dev.entries = sg.slots.empty() ? nullptr : c->d_entries;
+                    sg.dev.cap = c->entry_cap;
+                }
+            }
             c->frame_ok = true;
         }
     }

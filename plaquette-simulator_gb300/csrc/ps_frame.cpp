@@ -117,10 +117,13 @@ void FrameBuilder::end_segment() {
         return;
     }
     const uint32_t base = (uint32_t)prog.slot_off.size();
+    int32_t chunks = 0;
     for (const auto &rows : slot_rows_) {
         prog.slot_off.push_back((uint32_t)prog.tab.size());
         prog.tab.insert(prog.tab.end(), rows.begin(), rows.end());
+        chunks += (int32_t)((rows.size() + kFrameChunk - 1) / kFrameChunk);
     }
+    prog.entry_cap = std::max(prog.entry_cap, chunks);
     prog.slot_off.push_back((uint32_t)prog.tab.size());
     // A new launch: its sampling precedes it, then this segment's noise.
     if (prog.launches.back().op0 == prog.launches.back().op1) prog.launches.pop_back();

@@ -59,23 +59,21 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
             const int cnt = entry_count[k];
             const NoiseEntry *ent = entries + k * (int64_t)cap;
             for (int e = tid; e < cnt; e += 32 * FW) {
-                const NoiseEntry en = ent[e];  // layer: first row entry, a: row count
-                const uint32_t t1 = (uint32_t)en.layer + en.a;
-                for (uint32_t t = (uint32_t)en.layer; t < t1; t += 4) {
-                    uint32_t v[4];
+                const NoiseEntry en = ent[e];  // layer: first row entry, a: row count (<= kFrameChunk)
+                const uint32_t t0 = (uint32_t)en.layer, len = en.a;
+                uint32_t v[kFrameChunk];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) v[u] = t + u < t1 ? tab[t + u] : 0u;  // a row entry is never 0 (sel != 0)
+                for (uint32_t u = 0; u < kFrameChunk; ++u) v[u] = u < len ? tab[t0 + u] : 0u;  // never 0 (sel != 0)
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        if (v[u] == 0u) continue;
-                        const uint32_t sel = v[u] >> 28;
-                        u64 m = 0ull;
-                        if (sel & 1u) m ^= en.fxa;
-                        if (sel & 2u) m ^= en.fza;
-                        if (sel & 4u) m ^= en.fxb;
-                        if (sel & 8u) m ^= en.fzb;
-                        atomicXor(&sR[v[u] & kFrameRowMask], m);
-                    }
+                for (uint32_t u = 0; u < kFrameChunk; ++u) {
+                    if (v[u] == 0u) continue;
+                    const uint32_t sel = v[u] >> 28;
+                    u64 m = 0ull;
+                    if (sel & 1u) m ^= en.fxa;
+                    if (sel & 2u) m ^= en.fza;
+                    if (sel & 4u) m ^= en.fxb;
+                    if (sel & 8u) m ^= en.fzb;
+                    atomicXor(&sR[v[u] & kFrameRowMask], m);
                 }
             }
             __syncthreads();

@@ -60,11 +60,14 @@ struct FrameOp {
 
 // Noise table entry: row | sel << 28, sel bit 0 fx(a), 1 fz(a), 2 fx(b), 3 fz(b).
 constexpr uint32_t kFrameRowMask = 0x0FFFFFFFu;
+// A sampled outcome is applied in chunks of at most this many rows.
+constexpr uint32_t kFrameChunk = 16;
 
 struct FrameProgram {
     std::vector<FrameOp> ops;
     std::vector<uint32_t> tab;
     std::vector<uint32_t> slot_off;  // per segment: nslots + 1 offsets into tab
+    int32_t entry_cap = 0;           // largest sum over a segment's slots of its row chunks
     std::vector<uint64_t> xz;        // final x / z bits: [W][2][nw64]
     int64_t nw64 = 0;
     // op ranges launched together: the ops of one segment's noise and the

@@ -14,6 +14,7 @@
 // bytes.
 #include <algorithm>
 
+#include "ps_frame.h"
 #include "ps_internal.h"
 #include "ps_segment.cuh"
 
@@ -112,9 +113,11 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
 // keyed by (seed, event, global word, block), as the two-pass sampler) and
 // appends a non-identity outcome to the word's list with an atomic counter.
 // The list is unordered -- outcomes are XORs -- and carries, instead of the
-// slot, the slot's rows in the sign program: layer = first row entry
-// (slot_off[base + s]), a = their count.  Its counter is zeroed by the sign
-// kernel that consumes it.
+// slot, the slot's rows in the sign program (slot_off[base + s] ..
+// [base + s + 1]) cut into chunks of at most kFrameChunk: one entry per
+// chunk, layer = its first row entry, a = its row count, so no consumer
+// walks a long list alone.  The counter is zeroed by the sign kernel that
+// consumes the list.
 __global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp,
                                                           const uint32_t *__restrict__ slot_off, uint32_t base) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -144,16 +147,20 @@ __global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_
     }
     if ((fxa | fza | fxb | fzb) == 0ull) return;
     const uint32_t t0 = slot_off[base + s], t1 = slot_off[base + s + 1];
-    const int pos = atomicAdd(&seg.entry_count[k], 1);
+    const int nch = (int)((t1 - t0 + kFrameChunk - 1) / kFrameChunk);
+    if (nch == 0) return;
+    int pos = atomicAdd(&seg.entry_count[k], nch);
     NoiseEntry e;
     e.fxa = fxa;
     e.fza = fza;
     e.fxb = fxb;
     e.fzb = fzb;
-    e.layer = (int32_t)t0;
-    e.a = (uint16_t)(t1 - t0);
     e.b = 0;
-    seg.entries[k * (int64_t)seg.cap + pos] = e;
+    for (uint32_t c0 = t0; c0 < t1; c0 += kFrameChunk, ++pos) {
+        e.layer = (int32_t)c0;
+        e.a = (uint16_t)min((uint32_t)kFrameChunk, t1 - c0);
+        seg.entries[k * (int64_t)seg.cap + pos] = e;
+    }
 }
 
 // Tile cell: x and z of one (row, word, column) side by side, so a gate

@@ -125,6 +125,10 @@ struct ps_circuit {
     FrameOp *d_fops = nullptr;
     uint32_t *d_ftab = nullptr, *d_fslot = nullptr;
     uint64_t *d_fxz = nullptr;
+    NoiseEntry *d_entries2 = nullptr;  // second outcome buffer: sampling runs one segment ahead
+    int32_t *d_entry_count2 = nullptr;
+    cudaStream_t fstream[2] = {nullptr, nullptr};  // sampling, x/z broadcast
+    std::vector<cudaEvent_t> fev;
     cudaGraph_t graph[2] = {nullptr, nullptr};      // [reset_state]
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
 };
@@ -782,8 +786,12 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
 }
 
 // The shared-x/z plan of a run from |0...0>: for each range of the sign
-// program, the channel sampling of its segment (entries tagged with their
-// slot) and the sign kernel; then the broadcast of the final x / z bits.
+// program, the channel sampling of its segment and the sign kernel; and the
+// broadcast of the final x / z bits (host-known, so it needs nothing else).
+// Unless profiled, the plan forks: the broadcast on one side stream, the
+// sampling on another running ahead of the sign kernels through two
+// alternating outcome buffers (sampling segment j+2 waits for the sign
+// kernel that consumed segment j), both joined back at the end.
 int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
     ps_state *h = c->h;
     auto timed = [&](int kind, auto &&launch) -> int {
@@ -792,27 +800,72 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
         if (prof && rc == OK && prof->end() != OK) return E_CUDA;
         return rc;
     };
-    bool first = true;
+    const bool fork = prof == nullptr && c->fstream[0] != nullptr;
+    cudaStream_t ss = fork ? c->fstream[0] : st, sb = fork ? c->fstream[1] : st;
+    size_t nev = 0;
+    auto record = [&](cudaStream_t s, cudaEvent_t *e) -> int {
+        if (nev >= c->fev.size()) return fail(E_ARG, "shared-x/z plan: out of events");
+        *e = c->fev[nev++];
+        PS_CUDA(cudaEventRecord(*e, s));
+        return OK;
+    };
+    NoiseEntry *ebuf[2] = {c->d_entries, c->d_entries2 ? c->d_entries2 : c->d_entries};
+    int32_t *cbuf[2] = {c->d_entry_count, c->d_entry_count2 ? c->d_entry_count2 : c->d_entry_count};
+    if (fork) {
+        cudaEvent_t e0;
+        int rc = record(st, &e0);
+        if (rc != OK) return rc;
+        PS_CUDA(cudaStreamWaitEvent(ss, e0, 0));
+        PS_CUDA(cudaStreamWaitEvent(sb, e0, 0));
+        rc = launch_broadcast_xz(sb, h->X, h->Z, h->n, h->w, c->d_fxz, c->fprog.nw64);
+        if (rc != OK) return rc;
+    }
     // The one-pass sampler appends to per-word lists from a zero count (each
     // sign kernel zeroes the lists it consumed; a per-shot run leaves counts).
-    if (c->d_entry_count) PS_CUDA(cudaMemsetAsync(c->d_entry_count, 0, (size_t)h->w * sizeof(int32_t), st));
+    for (int b = 0; b < 2; ++b)
+        if (cbuf[b] && (b == 0 || cbuf[1] != cbuf[0]))
+            PS_CUDA(cudaMemsetAsync(cbuf[b], 0, (size_t)h->w * sizeof(int32_t), ss));
+    std::vector<cudaEvent_t> consumed;  // sign kernel done with sampled segment j
+    bool first = true;
     for (const FrameProgram::Launch &L : c->fprog.launches) {
-        int rc = OK;
-        if (L.seg >= 0)
+        int rc = OK, b = 0;
+        const bool sampled = L.seg >= 0;
+        if (sampled) {
+            const size_t j = consumed.size();
+            b = (int)(j & 1);
+            if (fork && j >= 2) PS_CUDA(cudaStreamWaitEvent(ss, consumed[j - 2], 0));
+            SegmentDev d = c->segs[(size_t)L.seg].dev;
+            d.entries = ebuf[b];
+            d.entry_count = cbuf[b];
             rc = timed(P_SAMPLE, [&] {
-                return launch_noise_sample_frame(st, c->segs[(size_t)L.seg].dev, h->w, c->d_params, c->d_fslot,
-                                                 (uint32_t)c->fprog.ops[L.op0].arg);
+                return launch_noise_sample_frame(ss, d, h->w, c->d_params, c->d_fslot, (uint32_t)c->fprog.ops[L.op0].arg);
             });
+            if (rc == OK && fork) {
+                cudaEvent_t es;
+                rc = record(ss, &es);
+                if (rc == OK) PS_CUDA(cudaStreamWaitEvent(st, es, 0));
+            }
+        }
         if (rc == OK)
             rc = timed(P_FRAME, [&] {
                 return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, L.tab0, L.tab1,
-                                    c->d_fslot, c->d_meas, c->d_res_block, (int64_t)c->meas.size(), c->d_entries,
-                                    c->d_entry_count, c->entry_cap, (uint64_t)h->seed, c->d_params, first ? 1 : 0);
+                                    c->d_fslot, c->d_meas, c->d_res_block, (int64_t)c->meas.size(), ebuf[b], cbuf[b],
+                                    c->entry_cap, (uint64_t)h->seed, c->d_params, first ? 1 : 0);
             });
         if (rc != OK) return rc;
+        if (sampled) {
+            cudaEvent_t ef = nullptr;
+            if (fork && record(st, &ef) != OK) return E_ARG;
+            consumed.push_back(ef);
+        }
         first = false;
     }
-    return timed(P_BROADCAST, [&] { return launch_broadcast_xz(st, h->X, h->Z, h->n, h->w, c->d_fxz, c->fprog.nw64); });
+    if (!fork) return timed(P_BROADCAST, [&] { return launch_broadcast_xz(st, h->X, h->Z, h->n, h->w, c->d_fxz, c->fprog.nw64); });
+    cudaEvent_t es, eb;
+    if (record(ss, &es) != OK || record(sb, &eb) != OK) return E_ARG;
+    PS_CUDA(cudaStreamWaitEvent(st, es, 0));
+    PS_CUDA(cudaStreamWaitEvent(st, eb, 0));
+    return OK;
 }
 
 int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nullptr) {
@@ -1290,6 +1343,23 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                     sg.dev.cap = c->entry_cap;
                 }
             }
+            {
+                void *p = nullptr;
+                if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * sizeof(NoiseEntry)) != OK)
+                    return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
+                c->owned.push_back(p);
+                c->d_entries2 = (NoiseEntry *)p;
+                if (dev_alloc(h, &p, (size_t)h->w * sizeof(int32_t)) != OK) return bail(E_NOMEM);
+                c->owned.push_back(p);
+                c->d_entry_count2 = (int32_t *)p;
+            }
+            for (int k = 0; k < 2; ++k)
+                if (cudaStreamCreateWithFlags(&c->fstream[k], cudaStreamNonBlocking) != cudaSuccess)
+                    return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
+            c->fev.assign(3 + 2 * c->fprog.launches.size() + 2, nullptr);
+            for (cudaEvent_t &e : c->fev)
+                if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                    return bail(cuda_fail(cudaGetLastError(), "cudaEventCreate"));
             c->frame_ok = true;
         }
     }
@@ -1533,6 +1603,13 @@ ps_status ps_circuit_destroy(ps_circuit *c) {
         if (c->exec[k]) cudaGraphExecDestroy(c->exec[k]);
         if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
     }
+    for (cudaStream_t fs : c->fstream)
+        if (fs) {
+            cudaStreamSynchronize(fs);
+            cudaStreamDestroy(fs);
+        }
+    for (cudaEvent_t e : c->fev)
+        if (e) cudaEventDestroy(e);
     for (void *p : c->owned) dev_free(c->h, p);
     dev_free(c->h, c->d_forced);
     delete c;

@@ -1307,7 +1307,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                     const SegHost &sg = c->segs[(size_t)s.first];
                     std::map<size_t, uint32_t> slot_of;
                     for (size_t k = 0; k < sg.slot_op.size(); ++k) slot_of[(size_t)sg.slot_op[k]] = (uint32_t)k;
-                    fb.begin_segment(s.first, (uint32_t)sg.slots.size());
+                    fb.begin_segment(s.first, (uint32_t)sg.slots.size(), sg.op1 - sg.op0);
                     for (size_t i = sg.op0; i < sg.op1; ++i) {
                         const ps_op &o = ops[i];
                         if (is_channel(o.code))

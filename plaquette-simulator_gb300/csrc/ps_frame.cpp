@@ -8,10 +8,10 @@
 
 namespace ps {
 
-FrameBuilder::FrameBuilder(int64_t n) : n_(n), W_(2 * n + 1), nw_((n + 63) / 64) {
+FrameBuilder::FrameBuilder(int64_t n) : n_(n), W_(2 * n + 1), nw_((n + 63) / 64), ww_((2 * n + 1 + 63) / 64) {
     x_.assign((size_t)(W_ * nw_), 0ull);
     z_.assign((size_t)(W_ * nw_), 0ull);
-    f_.assign((size_t)W_, 0);
+    fb_.assign((size_t)ww_, 0ull);
     for (int64_t i = 0; i < n_; ++i) {  // |0...0>: destabilizer X_i, stabilizer Z_i (CliffordState.hpp:66-71)
         flip(x_, i, i);
         flip(z_, i + n_, i);
@@ -19,6 +19,34 @@ FrameBuilder::FrameBuilder(int64_t n) : n_(n), W_(2 * n + 1), nw_((n + 63) / 64)
     prog.nw64 = nw_;
     flipped_.assign((size_t)W_, 0);
     open_range();
+}
+
+void FrameBuilder::to_col() {
+    if (col_) return;
+    xc_.assign((size_t)(n_ * ww_), 0ull);
+    zc_.assign((size_t)(n_ * ww_), 0ull);
+    for (int64_t i = 0; i < W_; ++i)
+        for (int64_t t = 0; t < nw_; ++t) {
+            for (uint64_t v = x_[(size_t)(i * nw_ + t)]; v; v &= v - 1)
+                xc_[(size_t)((64 * t + __builtin_ctzll(v)) * ww_ + (i >> 6))] |= 1ull << (i & 63);
+            for (uint64_t v = z_[(size_t)(i * nw_ + t)]; v; v &= v - 1)
+                zc_[(size_t)((64 * t + __builtin_ctzll(v)) * ww_ + (i >> 6))] |= 1ull << (i & 63);
+        }
+    col_ = true;
+}
+
+void FrameBuilder::to_row() {
+    if (!col_) return;
+    std::fill(x_.begin(), x_.end(), 0ull);
+    std::fill(z_.begin(), z_.end(), 0ull);
+    for (int64_t q = 0; q < n_; ++q)
+        for (int64_t t = 0; t < ww_; ++t) {
+            for (uint64_t v = xc_[(size_t)(q * ww_ + t)]; v; v &= v - 1)
+                x_[(size_t)((64 * t + __builtin_ctzll(v)) * nw_ + (q >> 6))] |= 1ull << (q & 63);
+            for (uint64_t v = zc_[(size_t)(q * ww_ + t)]; v; v &= v - 1)
+                z_[(size_t)((64 * t + __builtin_ctzll(v)) * nw_ + (q >> 6))] |= 1ull << (q & 63);
+        }
+    col_ = false;
 }
 
 void FrameBuilder::push_op(const FrameOp &op) {
@@ -55,37 +83,79 @@ void FrameBuilder::open_range() {
 }
 
 // The gate functors of GateFunctors.hpp over all W rows (scratch included,
-// CliffordState.hpp:381-386): x / z updated here, the sign term folded into f.
+// CliffordState.hpp:381-386), 64 rows per word: x / z updated here, the sign
+// term folded into f.
 void FrameBuilder::gate(int32_t code, int64_t a, int64_t b) {
-    for (int64_t i = 0; i < W_; ++i) {
-        const int xa = bit(x_, i, a), za = bit(z_, i, a);
-        switch (code) {
-        case PS_OP_H:  // :89-93
-            f_[(size_t)i] ^= (uint8_t)(xa & za);
-            if (xa != za) {
-                flip(x_, i, a);
-                flip(z_, i, a);
+    if (!seg_col_) {  // a short segment: row by row on the row-major bits
+        to_row();
+        for (int64_t i = 0; i < W_; ++i) {
+            const int xa = bit(x_, i, a), za = bit(z_, i, a);
+            int fl = 0;
+            switch (code) {
+            case PS_OP_H:
+                fl = xa & za;
+                if (xa != za) {
+                    flip(x_, i, a);
+                    flip(z_, i, a);
+                }
+                break;
+            case PS_OP_S:
+                fl = xa & za;
+                if (xa) flip(z_, i, a);
+                break;
+            case PS_OP_X: fl = za; break;
+            case PS_OP_Y: fl = za ^ xa; break;
+            case PS_OP_Z: fl = xa; break;
+            case PS_OP_CX: {
+                const int xt = bit(x_, i, b), zt = bit(z_, i, b);
+                fl = xa & zt & (xt ^ za ^ 1);
+                if (xa) flip(x_, i, b);
+                if (zt) flip(z_, i, a);
+                break;
             }
+            case PS_OP_CZ: {
+                const int xt = bit(x_, i, b), zt = bit(z_, i, b);
+                fl = xa & xt & (zt ^ za);
+                if (xa) flip(z_, i, b);
+                if (xt) flip(z_, i, a);
+                break;
+            }
+            default: break;
+            }
+            if (fl) fset(i, !fget(i));
+        }
+        return;
+    }
+    to_col();
+    uint64_t *xa = &xc_[(size_t)(a * ww_)], *za = &zc_[(size_t)(a * ww_)];
+    uint64_t *xb = b >= 0 ? &xc_[(size_t)(b * ww_)] : nullptr, *zb = b >= 0 ? &zc_[(size_t)(b * ww_)] : nullptr;
+    for (int64_t t = 0; t < ww_; ++t) {
+        uint64_t &f = fb_[(size_t)t];
+        switch (code) {
+        case PS_OP_H: {  // :89-93
+            const uint64_t x = xa[t], z = za[t];
+            f ^= x & z;
+            xa[t] = z;
+            za[t] = x;
             break;
+        }
         case PS_OP_S:  // :164-169
-            f_[(size_t)i] ^= (uint8_t)(xa & za);
-            if (xa) flip(z_, i, a);
+            f ^= xa[t] & za[t];
+            za[t] ^= xa[t];
             break;
-        case PS_OP_X: f_[(size_t)i] ^= (uint8_t)za; break;         // :303-307
-        case PS_OP_Y: f_[(size_t)i] ^= (uint8_t)(za ^ xa); break;  // :323-327
-        case PS_OP_Z: f_[(size_t)i] ^= (uint8_t)xa; break;         // :372-376
+        case PS_OP_X: f ^= za[t]; break;          // :303-307
+        case PS_OP_Y: f ^= za[t] ^ xa[t]; break;  // :323-327
+        case PS_OP_Z: f ^= xa[t]; break;          // :372-376
         case PS_OP_CX: {  // :247-253, a = control
-            const int xt = bit(x_, i, b), zt = bit(z_, i, b);
-            f_[(size_t)i] ^= (uint8_t)(xa & zt & (xt ^ za ^ 1));
-            if (xa) flip(x_, i, b);
-            if (zt) flip(z_, i, a);
+            f ^= xa[t] & zb[t] & ~(xb[t] ^ za[t]);
+            xb[t] ^= xa[t];
+            za[t] ^= zb[t];
             break;
         }
         case PS_OP_CZ: {  // :29-35
-            const int xt = bit(x_, i, b), zt = bit(z_, i, b);
-            f_[(size_t)i] ^= (uint8_t)(xa & xt & (zt ^ za));
-            if (xa) flip(z_, i, b);
-            if (xt) flip(z_, i, a);
+            f ^= xa[t] & xb[t] & (zb[t] ^ za[t]);
+            zb[t] ^= xa[t];
+            za[t] ^= xb[t];
             break;
         }
         default: break;
@@ -93,8 +163,9 @@ void FrameBuilder::gate(int32_t code, int64_t a, int64_t b) {
     }
 }
 
-void FrameBuilder::begin_segment(int32_t seg, uint32_t nslots) {
+void FrameBuilder::begin_segment(int32_t seg, uint32_t nslots, size_t nops) {
     seg_ = seg;
+    seg_col_ = nops >= 64;
     slot_rows_.assign(nslots, {});
 }
 
@@ -103,10 +174,27 @@ void FrameBuilder::begin_segment(int32_t seg, uint32_t nslots) {
 void FrameBuilder::channel(int64_t a, int64_t b, uint32_t slot) {
     std::vector<uint32_t> &rows = slot_rows_[slot];
     rows.clear();
-    for (int64_t i = 0; i < W_; ++i) {
-        uint32_t sel = (uint32_t)bit(z_, i, a) | (uint32_t)bit(x_, i, a) << 1;
-        if (b >= 0) sel |= (uint32_t)bit(z_, i, b) << 2 | (uint32_t)bit(x_, i, b) << 3;
-        if (sel) rows.push_back((uint32_t)i | sel << 28);
+    if (!seg_col_) {
+        to_row();
+        for (int64_t i = 0; i < W_; ++i) {
+            uint32_t sel = (uint32_t)bit(z_, i, a) | (uint32_t)bit(x_, i, a) << 1;
+            if (b >= 0) sel |= (uint32_t)bit(z_, i, b) << 2 | (uint32_t)bit(x_, i, b) << 3;
+            if (sel) rows.push_back((uint32_t)i | sel << 28);
+        }
+        return;
+    }
+    to_col();
+    const uint64_t *xa = &xc_[(size_t)(a * ww_)], *za = &zc_[(size_t)(a * ww_)];
+    const uint64_t *xb = b >= 0 ? &xc_[(size_t)(b * ww_)] : nullptr, *zb = b >= 0 ? &zc_[(size_t)(b * ww_)] : nullptr;
+    for (int64_t t = 0; t < ww_; ++t) {
+        uint64_t m = za[t] | xa[t];
+        if (b >= 0) m |= zb[t] | xb[t];
+        for (; m; m &= m - 1) {
+            const int u = __builtin_ctzll(m);
+            uint32_t sel = (uint32_t)((za[t] >> u) & 1ull) | (uint32_t)((xa[t] >> u) & 1ull) << 1;
+            if (b >= 0) sel |= (uint32_t)((zb[t] >> u) & 1ull) << 2 | (uint32_t)((xb[t] >> u) & 1ull) << 3;
+            rows.push_back((uint32_t)(64 * t + u) | sel << 28);
+        }
     }
 }
 
@@ -161,6 +249,7 @@ void FrameBuilder::row_xor(int64_t dst, int64_t src) {
 // with x(p+n,q) = 1 takes the random branch, else the deterministic one; a
 // reset then flips the rows with z(., q) = 1 where the outcome is 1.
 void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
+    to_row();
     int64_t p = 0;
     while (p < n_ && !bit(x_, p + n_, q)) ++p;
     const int64_t s = 2 * n_;
@@ -178,11 +267,11 @@ void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
             z_[(size_t)((p + n_) * nw_ + t)] = 0ull;
         }
         flip(z_, p + n_, q);
-        f_[(size_t)p] = f_[(size_t)(p + n_)];
-        f_[(size_t)(p + n_)] = 0;
+        fset(p, fget(p + n_));
+        fset(p + n_, false);
         for (int64_t i = 0; i < 2 * n_; ++i)
             if (i != p && i != p + n_ && bit(x_, i, q)) {
-                const uint32_t c = (uint32_t)(phase_bit(i, p) ^ f_[(size_t)p]);
+                const uint32_t c = (uint32_t)(phase_bit(i, p) ^ (int)fget(p));
                 prog.tab.push_back((uint32_t)i | c << 31);
                 row_xor(i, p);
             }
@@ -210,13 +299,13 @@ void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
     bool hazard = false;
     for (int64_t i = 0; i < n_; ++i)
         if (bit(x_, i, q)) {
-            c ^= (uint32_t)(phase_bit(s, i + n_) ^ f_[(size_t)(i + n_)]);
+            c ^= (uint32_t)(phase_bit(s, i + n_) ^ (int)fget(i + n_));
             r.rd.push_back((uint32_t)(i + n_));
             hazard |= flipped_[(size_t)(i + n_)] == stamp_;
             row_xor(s, i + n_);
         }
     r.c = c;
-    f_[(size_t)s] = 0;
+    fset(s, false);
     if (hazard || window_.size() == 32) flush_window();
     if (reset)
         for (int64_t i = 0; i < W_; ++i)
@@ -228,12 +317,13 @@ void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
 }
 
 void FrameBuilder::finish() {
+    to_row();
     flush_window();
     FrameOp op{};
     op.kind = F_FLIP;
     op.off = (uint32_t)prog.tab.size();
     for (int64_t i = 0; i < W_; ++i)
-        if (f_[(size_t)i]) prog.tab.push_back((uint32_t)i);
+        if (fget(i)) prog.tab.push_back((uint32_t)i);
     op.len = (uint32_t)prog.tab.size() - op.off;
     push_op(op);
     for (FrameProgram::Launch &L : prog.launches) {  // tab range of the measurement ops

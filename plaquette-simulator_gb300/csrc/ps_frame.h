@@ -88,7 +88,8 @@ class FrameBuilder {
     void gate(int32_t code, int64_t a, int64_t b);  // H, S, X, Y, Z, CX, CZ
     // Pauli channel on a (and b >= 0): slot `slot` of the current segment.
     void channel(int64_t a, int64_t b, uint32_t slot);
-    void begin_segment(int32_t seg, uint32_t nslots);
+    // nops: the segment's op count (a long one is simulated column-major).
+    void begin_segment(int32_t seg, uint32_t nslots, size_t nops);
     void end_segment();
     void measure(int64_t q, int32_t meas_index, bool reset);
     void finish();
@@ -101,9 +102,22 @@ class FrameBuilder {
     };
 
   private:
-    int64_t n_, W_, nw_;
-    std::vector<uint64_t> x_, z_;  // row-major [W][nw]
-    std::vector<uint8_t> f_;       // pending constant flips per row
+    // x / z are kept column-major ([n][ww], word-parallel gates over rows)
+    // while a long segment is simulated and row-major ([W][nw], row
+    // products) otherwise; switching transposes by the set bits.
+    int64_t n_, W_, nw_, ww_;
+    std::vector<uint64_t> x_, z_;    // row-major [W][nw]
+    std::vector<uint64_t> xc_, zc_;  // column-major [n][ww]
+    bool col_ = false;
+    bool seg_col_ = false;  // the current segment runs column-major
+    std::vector<uint64_t> fb_;       // pending constant flips, a bit per row
+    bool fget(int64_t i) const { return (fb_[(size_t)(i >> 6)] >> (i & 63)) & 1ull; }
+    void fset(int64_t i, bool v) {
+        const uint64_t m = 1ull << (i & 63);
+        fb_[(size_t)(i >> 6)] = v ? (fb_[(size_t)(i >> 6)] | m) : (fb_[(size_t)(i >> 6)] & ~m);
+    }
+    void to_col();
+    void to_row();
     int32_t seg_ = -1;
     std::vector<std::vector<uint32_t>> slot_rows_;
     std::vector<DetRecord> window_;

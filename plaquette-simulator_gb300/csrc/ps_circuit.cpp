@@ -124,6 +124,7 @@ struct ps_circuit {
     FrameProgram fprog;
     FrameOp *d_fops = nullptr;
     uint32_t *d_ftab = nullptr, *d_fslot = nullptr;
+    int32_t *d_frand = nullptr;
     uint64_t *d_fxz = nullptr;
     NoiseEntry *d_entries2 = nullptr;  // second outcome buffer: sampling runs one segment ahead
     int32_t *d_entry_count2 = nullptr;
@@ -849,8 +850,9 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
         if (rc == OK)
             rc = timed(P_FRAME, [&] {
                 return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, L.tab0, L.tab1,
-                                    c->d_fslot, c->d_meas, c->d_res_block, (int64_t)c->meas.size(), ebuf[b], cbuf[b],
-                                    c->entry_cap, (uint64_t)h->seed, c->d_params, first ? 1 : 0);
+                                    c->d_fslot, c->d_frand + L.rand0, L.nrand, c->d_meas, c->d_res_block,
+                                    (int64_t)c->meas.size(), ebuf[b], cbuf[b], c->entry_cap, (uint64_t)h->seed,
+                                    c->d_params, first ? 1 : 0);
             });
         if (rc != OK) return rc;
         if (sampled) {
@@ -1327,8 +1329,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             c->fprog = std::move(fb.prog);
             if (c->fprog.tab.empty()) c->fprog.tab.push_back(0);
             if (c->fprog.slot_off.empty()) c->fprog.slot_off.push_back(0);
+            if (c->fprog.rand_meas.empty()) c->fprog.rand_meas.push_back(0);
             if (upload(h, c->owned, c->fprog.ops, &c->d_fops) || upload(h, c->owned, c->fprog.tab, &c->d_ftab) ||
-                upload(h, c->owned, c->fprog.slot_off, &c->d_fslot) || upload(h, c->owned, c->fprog.xz, &c->d_fxz))
+                upload(h, c->owned, c->fprog.slot_off, &c->d_fslot) || upload(h, c->owned, c->fprog.xz, &c->d_fxz) ||
+                upload(h, c->owned, c->fprog.rand_meas, &c->d_frand))
                 return bail(E_CUDA);
             // Outcome lists hold one entry per row chunk of a slot.
             if (c->fprog.entry_cap > c->entry_cap) {

@@ -33,4 +33,25 @@ __device__ __forceinline__ u64 outcome_bits(const MeasOp &op, int lane, uint64_t
     return bits;
 }
 
+// The same 64 outcomes computed by one thread (all 16 Philox blocks).
+__device__ __forceinline__ u64 outcome_word(const MeasOp &op, uint64_t seed, uint64_t event_base, int64_t k,
+                                            uint64_t word_base) {
+    u64 bits = 0ull;
+    if (op.forced) {
+        const u64 fw = op.forced[k];
+        for (int b = 0; b < 64; ++b) {
+            const float u = ((fw >> b) & 1ull) ? 0.25f : 0.75f;
+            if (u < op.bias) bits |= 1ull << b;
+        }
+        return bits;
+    }
+    for (uint32_t sub = 0; sub < 16; ++sub) {
+        const u32x4 u = draw_block(seed, event_base + op.event, word_base + (uint64_t)k, sub, TAG_MEASURE);
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+            if (unit_float(u.v[l]) < op.bias) bits |= 1ull << (sub * 4 + l);
+    }
+    return bits;
+}
+
 }  // namespace ps

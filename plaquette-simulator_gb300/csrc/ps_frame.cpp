@@ -79,7 +79,8 @@ void FrameBuilder::flush_window() {
 }
 
 void FrameBuilder::open_range() {
-    prog.launches.push_back({-1, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size(), 0, 0});
+    prog.launches.push_back(
+        {-1, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size(), 0, 0, (uint32_t)prog.rand_meas.size(), 0});
 }
 
 // The gate functors of GateFunctors.hpp over all W rows (scratch included,
@@ -215,7 +216,8 @@ void FrameBuilder::end_segment() {
     prog.slot_off.push_back((uint32_t)prog.tab.size());
     // A new launch: its sampling precedes it, then this segment's noise.
     if (prog.launches.back().op0 == prog.launches.back().op1) prog.launches.pop_back();
-    prog.launches.push_back({seg_, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size(), 0, 0});
+    prog.launches.push_back(
+        {seg_, (uint32_t)prog.ops.size(), (uint32_t)prog.ops.size(), 0, 0, (uint32_t)prog.rand_meas.size(), 0});
     FrameOp op{};
     op.kind = F_NOISE;
     op.arg = (int32_t)base;
@@ -256,8 +258,10 @@ void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
     if (p < n_) {  // MeasureRandom (:225-265), in program order after the open window
         flush_window();
         FrameOp op{};
-        op.kind = F_MEAS_RAND;
+        op.kind = F_MEAS_RAND | prog.launches.back().nrand << 8;
         op.arg = meas_index;
+        prog.rand_meas.push_back(meas_index);
+        prog.launches.back().nrand++;
         op.off = (uint32_t)prog.tab.size();
         prog.tab.push_back((uint32_t)p);
         for (int64_t t = 0; t < nw_; ++t) {  // row p := row p+n; row p+n := Z_q

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
                                                    const FrameOp *__restrict__ ops, uint32_t op0, uint32_t op1,
                                                    const uint32_t *__restrict__ tab, uint32_t tab0, uint32_t ntab,
                                                    int stage, const uint32_t *__restrict__ slot_off,
+                                                   const int32_t *__restrict__ rand_meas, uint32_t nrand,
                                                    const MeasOp *__restrict__ meas, u64 *__restrict__ rec,
                                                    int64_t nm, const NoiseEntry *__restrict__ entries,
                                                    int32_t *__restrict__ entry_count, int32_t cap, uint64_t seed,
@@ -37,7 +38,8 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
     const int64_t W = 2 * n + 1;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int64_t k = blockIdx.x;
-    uint32_t *stab = reinterpret_cast<uint32_t *>(sR + W);
+    u64 *sout = sR + W;  // the launch's random outcomes, drawn up front
+    uint32_t *stab = reinterpret_cast<uint32_t *>(sout + nrand);
     FrameOp *sops = reinterpret_cast<FrameOp *>(((uintptr_t)(stab + ntab) + 15) & ~(uintptr_t)15);
     for (int64_t i = tid; i < W; i += 32 * FW) sR[i] = from_zero ? 0ull : R[i * w + k];
     if (stage) {
@@ -46,10 +48,12 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
         uint32_t *dst = reinterpret_cast<uint32_t *>(sops);
         for (uint32_t i = tid; i < 4 * (op1 - op0); i += 32 * FW) dst[i] = src[i];
     }
+    const uint64_t event_base = rp->event_base, word_base = rp->word_base;
+    for (uint32_t j = tid; j < nrand; j += 32 * FW)
+        sout[j] = outcome_word(meas[rand_meas[j]], seed, event_base, k, word_base);
     __syncthreads();
     const uint32_t *T = stage ? stab : tab;  // measurement-op tab, indexed x - tb
     const uint32_t tb = stage ? tab0 : 0u;
-    const uint64_t event_base = rp->event_base, word_base = rp->word_base;
     u64 last = 0ull;  // outcome of the latest measurement (its reset X)
     for (uint32_t oi = op0; oi < op1; ++oi) {
         const FrameOp o = stage ? sops[oi - op0] : ops[oi];
@@ -99,8 +103,7 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
             last = __shfl_sync(0xffffffffu, acc, (int)o.len - 1);
             __syncwarp();
         } else if (kind == F_MEAS_RAND) {
-            const MeasOp &m = meas[o.arg];
-            const u64 out = outcome_bits(m, lane, seed, event_base, k, word_base);
+            const u64 out = sout[o.kind >> 8];
             const uint32_t p = T[o.off - tb];
             const u64 rpv = sR[p + n];
             __syncwarp();
@@ -154,11 +157,11 @@ int g_frame_sms = 0;
 size_t frame_smem_bytes(int64_t n) { return (size_t)(2 * n + 1) * sizeof(u64); }
 
 int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
-                 const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const MeasOp *meas,
-                 u64 *rec, int64_t nm, const NoiseEntry *entries, int32_t *entry_count, int32_t cap, uint64_t seed,
-                 const RunParams *rp, int from_zero) {
+                 const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,
+                 uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
+                 int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero) {
     // Staging keeps a CTA's shared memory small enough for two per SM.
-    const size_t base = frame_smem_bytes(n);
+    const size_t base = frame_smem_bytes(n) + (size_t)nrand * sizeof(u64);
     const size_t staged = base + (size_t)(tab1 - tab0) * 4 + 16 + (size_t)(op1 - op0) * sizeof(FrameOp);
     const int stage = staged <= kFrameStageMax ? 1 : 0;
     const size_t smem = stage ? staged : base;
@@ -167,7 +170,8 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
         const int rc = allow_max_smem((const void *)frame_kernel);
         if (rc != OK) return rc;
     }
-    frame_kernel<<<(unsigned)w, 32 * FW, smem, st>>>(R, n, w, ops, op0, op1, tab, tab0, ntab, stage, slot_off, meas, rec,
+    frame_kernel<<<(unsigned)w, 32 * FW, smem, st>>>(R, n, w, ops, op0, op1, tab, tab0, ntab, stage, slot_off,
+                                                     rand_meas, nrand, meas, rec,
                                                 nm, entries, entry_count, cap, seed, rp, from_zero);
     PS_CUDA(cudaGetLastError());
     return OK;

@@ -35,7 +35,7 @@ namespace ps {
 enum FrameKind : uint32_t {
     F_NOISE = 0,      // entries of segment `arg` (sampled just before): tab rows per slot
     F_MEAS_DET = 1,   // arg = MeasOp; tab[off..off+len) rows; kind bit 8 = constant
-    F_MEAS_RAND = 2,  // arg = MeasOp; tab[off] = p, then rows | c << 31
+    F_MEAS_RAND = 2,  // arg = MeasOp; tab[off] = p, then rows | c << 31; kind >> 8 = its index in the launch's random list
     F_RESET_X = 3,    // R[row] ^= outcome of the last measurement, rows tab[off..off+len)
     F_FLIP = 4,       // R[row] ^= ~0, rows tab[off..off+len)
     F_WINDOW = 5,     // len deterministic measurements, one per lane (below)
@@ -76,7 +76,11 @@ struct FrameProgram {
         int32_t seg;
         uint32_t op0, op1;
         uint32_t tab0, tab1;  // tab range of the launch's measurement ops (staged in shared memory)
+        uint32_t rand0, nrand;  // the launch's random measurements: rand_meas[rand0, rand0 + nrand)
     };
+    // MeasOp indices of the random measurements, launch by launch: their
+    // outcomes depend on no sign, so a launch draws them all up front.
+    std::vector<int32_t> rand_meas;
     std::vector<Launch> launches;
 };
 

@@ -61,17 +61,15 @@ void FrameBuilder::flush_window() {
     op.kind = F_WINDOW;
     op.off = (uint32_t)prog.tab.size();
     op.len = (uint32_t)window_.size();
-    prog.tab.resize(prog.tab.size() + window_.size());
-    const uint32_t s = (uint32_t)(2 * n_);
+    const uint32_t s = (uint32_t)(2 * n_), zero_row = (uint32_t)W_, sink_row = (uint32_t)W_ + 1;
     for (size_t j = 0; j < window_.size(); ++j) {
         DetRecord &r = window_[j];
         if (j + 1 < window_.size())  // the last measurement of the window overwrites the scratch row
             r.rs.erase(std::remove(r.rs.begin(), r.rs.end(), s), r.rs.end());
-        prog.tab[op.off + j] = (uint32_t)prog.tab.size() - op.off;
         prog.tab.push_back((uint32_t)r.meas);
-        prog.tab.push_back((uint32_t)r.rd.size() | (uint32_t)r.rs.size() << 16 | r.c << 31);
-        prog.tab.insert(prog.tab.end(), r.rd.begin(), r.rd.end());
-        prog.tab.insert(prog.tab.end(), r.rs.begin(), r.rs.end());
+        prog.tab.push_back(r.c | (uint32_t)r.rd.size() << 1 | (uint32_t)r.rs.size() << 4);
+        for (uint32_t t = 0; t < kWinRows; ++t) prog.tab.push_back(t < r.rd.size() ? r.rd[t] : zero_row);
+        for (uint32_t t = 0; t < kWinRows; ++t) prog.tab.push_back(t < r.rs.size() ? r.rs[t] : sink_row);
     }
     push_op(op);
     window_.clear();
@@ -300,23 +298,43 @@ void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
         z_[(size_t)(s * nw_ + t)] = 0ull;
     }
     uint32_t c = 0;
-    bool hazard = false;
     for (int64_t i = 0; i < n_; ++i)
         if (bit(x_, i, q)) {
             c ^= (uint32_t)(phase_bit(s, i + n_) ^ (int)fget(i + n_));
             r.rd.push_back((uint32_t)(i + n_));
-            hazard |= flipped_[(size_t)(i + n_)] == stamp_;
             row_xor(s, i + n_);
         }
     r.c = c;
     fset(s, false);
-    if (hazard || window_.size() == 32) flush_window();
     if (reset)
         for (int64_t i = 0; i < W_; ++i)
-            if (bit(z_, i, q)) {
-                r.rs.push_back((uint32_t)i);
-                flipped_[(size_t)i] = stamp_;
-            }
+            if (bit(z_, i, q)) r.rs.push_back((uint32_t)i);
+    if (r.rd.size() > kWinRows || r.rs.size() > kWinRows) {  // too long for a window record: alone
+        flush_window();
+        FrameOp op{};
+        op.kind = F_MEAS_DET | r.c << 8;
+        op.arg = meas_index;
+        op.off = (uint32_t)prog.tab.size();
+        prog.tab.insert(prog.tab.end(), r.rd.begin(), r.rd.end());
+        op.len = (uint32_t)r.rd.size();
+        push_op(op);
+        if (reset) {
+            FrameOp ro{};
+            ro.kind = F_RESET_X;
+            ro.off = (uint32_t)prog.tab.size();
+            prog.tab.insert(prog.tab.end(), r.rs.begin(), r.rs.end());
+            ro.len = (uint32_t)r.rs.size();
+            push_op(ro);
+        }
+        return;
+    }
+    bool hazard = window_.size() == 32;
+    for (uint32_t row : r.rd) hazard |= flipped_[row] == stamp_;  // reads a row a reset of the window flips
+    for (uint32_t row : r.rs)
+        if (row != (uint32_t)s) hazard |= flipped_[row] == stamp_;  // flips a row a reset of the window flips
+    if (hazard) flush_window();
+    for (uint32_t row : r.rs)
+        if (row != (uint32_t)s) flipped_[row] = stamp_;
     window_.push_back(std::move(r));
 }
 

@@ -38,10 +38,11 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
     const int64_t W = 2 * n + 1;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int64_t k = blockIdx.x;
-    u64 *sout = sR + W;  // the launch's random outcomes, drawn up front
+    u64 *sout = sR + W + 2;  // the launch's random outcomes, drawn up front
     uint32_t *stab = reinterpret_cast<uint32_t *>(sout + nrand);
     FrameOp *sops = reinterpret_cast<FrameOp *>(((uintptr_t)(stab + ntab) + 15) & ~(uintptr_t)15);
     for (int64_t i = tid; i < W; i += 32 * FW) sR[i] = from_zero ? 0ull : R[i * w + k];
+    if (tid < 2) sR[W + tid] = 0ull;  // zero row (unused window reads) and sink row (unused window writes)
     if (stage) {
         for (uint32_t i = tid; i < ntab; i += 32 * FW) stab[i] = tab[tab0 + i];
         const uint32_t *src = reinterpret_cast<const uint32_t *>(ops + op0);
@@ -86,21 +87,42 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
             continue;  // the measurement ops run on warp 0
         } else if (kind == F_WINDOW) {
             u64 acc = 0ull;
-            uint32_t r0 = 0, nrd = 0, nrs = 0;
+            uint32_t rs[kWinRows];
             if ((uint32_t)lane < o.len) {
-                r0 = o.off + T[o.off + lane - tb];
-                const uint32_t m = T[r0 - tb], hdr = T[r0 + 1 - tb];
-                nrd = hdr & 0xFFFFu;
-                nrs = (hdr >> 16) & 0x7FFFu;
-                acc = (hdr >> 31) ? ~0ull : 0ull;
-                for (uint32_t t = 0; t < nrd; ++t) acc ^= sR[T[r0 + 2 + t - tb]];
+                const uint32_t *rc = T + (o.off + kWinRec * lane - tb);
+                const uint32_t m = rc[0], hdr = rc[1];
+                uint32_t rd[kWinRows];
+#pragma unroll
+                for (uint32_t t = 0; t < kWinRows; ++t) {
+                    rd[t] = rc[2 + t];
+                    rs[t] = rc[2 + kWinRows + t];
+                }
+                acc = (hdr & 1u) ? ~0ull : 0ull;
+#pragma unroll
+                for (uint32_t t = 0; t < kWinRows; ++t) acc ^= sR[rd[t]];
                 rec[(int64_t)m * w + k] = acc;
                 rec[(nm + (int64_t)m) * w + k] = ~0ull;
                 if ((uint32_t)lane == o.len - 1) sR[2 * n] = acc;
             }
             __syncwarp();
-            for (uint32_t t = 0; t < nrs; ++t) atomicXor(&sR[T[r0 + 2 + nrd + t - tb]], acc);
+            if ((uint32_t)lane < o.len) {  // reset rows of a window are disjoint (the sink row aside)
+#pragma unroll
+                for (uint32_t t = 0; t < kWinRows; ++t) sR[rs[t]] ^= acc;
+            }
             last = __shfl_sync(0xffffffffu, acc, (int)o.len - 1);
+            __syncwarp();
+        } else if (kind == F_MEAS_DET) {
+            u64 acc = 0ull;
+            for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) acc ^= sR[T[t - tb]];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, off);
+            if (o.kind >> 8) acc = ~acc;
+            if (lane == 0) {
+                rec[(int64_t)o.arg * w + k] = acc;
+                rec[(nm + (int64_t)o.arg) * w + k] = ~0ull;
+                sR[2 * n] = acc;
+            }
+            last = acc;
             __syncwarp();
         } else if (kind == F_MEAS_RAND) {
             const u64 out = sout[o.kind >> 8];
@@ -154,7 +176,7 @@ int g_frame_sms = 0;
 
 }  // namespace
 
-size_t frame_smem_bytes(int64_t n) { return (size_t)(2 * n + 1) * sizeof(u64); }
+size_t frame_smem_bytes(int64_t n) { return (size_t)(2 * n + 3) * sizeof(u64); }  // rows, zero row, sink row
 
 int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
                  const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,

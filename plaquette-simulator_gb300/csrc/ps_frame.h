@@ -34,7 +34,7 @@ namespace ps {
 
 enum FrameKind : uint32_t {
     F_NOISE = 0,      // entries of segment `arg` (sampled just before): tab rows per slot
-    F_MEAS_DET = 1,   // arg = MeasOp; tab[off..off+len) rows; kind bit 8 = constant
+    F_MEAS_DET = 1,   // arg = MeasOp; tab[off..off+len) rows; kind bit 8 = constant (more rows than a window record holds)
     F_MEAS_RAND = 2,  // arg = MeasOp; tab[off] = p, then rows | c << 31; kind >> 8 = its index in the launch's random list
     F_RESET_X = 3,    // R[row] ^= outcome of the last measurement, rows tab[off..off+len)
     F_FLIP = 4,       // R[row] ^= ~0, rows tab[off..off+len)
@@ -43,13 +43,17 @@ enum FrameKind : uint32_t {
 
 // A window of deterministic measurements (each with its reset X) that run
 // at once, one per lane: every lane reads its rows first, the last one
-// writes the scratch row, then the resets XOR their outcomes in (shared
-// atomics; XORs commute).  The builder closes a window before a measurement
-// that reads a row an earlier reset of the window flips (a reset that flips
-// a row an earlier measurement read is fine: reads come first), and drops
-// the scratch row from every reset but the last one's (the last measurement
-// overwrites it).  tab[off + j] = offset of record j from off; a record is
-// [MeasOp index][nread | nreset << 16 | c << 31][read rows][reset rows].
+// writes the scratch row, then the resets XOR their outcomes in.  The
+// builder closes a window before a measurement that reads a row an earlier
+// reset of the window flips, or whose reset flips a row an earlier reset
+// flips (so the XORs need no atomics; a reset that flips a row an earlier
+// measurement read is fine: reads come first), and drops the scratch row
+// from every reset but the last one's (the last measurement overwrites it).
+// Record j sits at tab[off + kWinRec * j]: [MeasOp index][c | nread << 1 |
+// nreset << 4][kWinRows read rows][kWinRows reset rows], unused read rows
+// pointing at the zero row W and unused reset rows at the sink row W + 1.
+constexpr uint32_t kWinRows = 4;
+constexpr uint32_t kWinRec = 2 + 2 * kWinRows;
 
 struct FrameOp {
     uint32_t kind;  // FrameKind | constant bit << 8

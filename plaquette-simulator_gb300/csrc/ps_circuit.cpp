@@ -126,8 +126,10 @@ struct ps_circuit {
     uint32_t *d_ftab = nullptr, *d_fslot = nullptr;
     int32_t *d_frand = nullptr;
     uint64_t *d_fxz = nullptr;
-    NoiseEntry *d_entries2 = nullptr;  // second outcome buffer: sampling runs one segment ahead
-    int32_t *d_entry_count2 = nullptr;
+    // Outcome buffers of the shared-x/z plan (the first is d_entries /
+    // d_entry_count): sampling runs up to fent.size() - 1 segments ahead.
+    std::vector<NoiseEntry *> fent;
+    std::vector<int32_t *> fcnt;
     cudaStream_t fstream[2] = {nullptr, nullptr};  // sampling, x/z broadcast
     std::vector<cudaEvent_t> fev;
     cudaGraph_t graph[2] = {nullptr, nullptr};      // [reset_state]
@@ -790,9 +792,9 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
 // program, the channel sampling of its segment and the sign kernel; and the
 // broadcast of the final x / z bits (host-known, so it needs nothing else).
 // Unless profiled, the plan forks: the broadcast on one side stream, the
-// sampling on another running ahead of the sign kernels through two
-// alternating outcome buffers (sampling segment j+2 waits for the sign
-// kernel that consumed segment j), both joined back at the end.
+// sampling on another running ahead of the sign kernels through NB rotating
+// outcome buffers (sampling segment j+NB waits for the sign kernel that
+// consumed segment j), both joined back at the end.
 int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
     ps_state *h = c->h;
     auto timed = [&](int kind, auto &&launch) -> int {
@@ -810,8 +812,9 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
         PS_CUDA(cudaEventRecord(*e, s));
         return OK;
     };
-    NoiseEntry *ebuf[2] = {c->d_entries, c->d_entries2 ? c->d_entries2 : c->d_entries};
-    int32_t *cbuf[2] = {c->d_entry_count, c->d_entry_count2 ? c->d_entry_count2 : c->d_entry_count};
+    const size_t nb = c->fent.size();
+    const std::vector<NoiseEntry *> &ebuf = c->fent;
+    const std::vector<int32_t *> &cbuf = c->fcnt;
     if (fork) {
         cudaEvent_t e0;
         int rc = record(st, &e0);
@@ -823,18 +826,18 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
     }
     // The one-pass sampler appends to per-word lists from a zero count (each
     // sign kernel zeroes the lists it consumed; a per-shot run leaves counts).
-    for (int b = 0; b < 2; ++b)
-        if (cbuf[b] && (b == 0 || cbuf[1] != cbuf[0]))
-            PS_CUDA(cudaMemsetAsync(cbuf[b], 0, (size_t)h->w * sizeof(int32_t), ss));
+    for (size_t b = 0; b < nb; ++b)
+        if (cbuf[b]) PS_CUDA(cudaMemsetAsync(cbuf[b], 0, (size_t)h->w * sizeof(int32_t), ss));
     std::vector<cudaEvent_t> consumed;  // sign kernel done with sampled segment j
     bool first = true;
     for (const FrameProgram::Launch &L : c->fprog.launches) {
-        int rc = OK, b = 0;
+        int rc = OK;
+        size_t b = 0;
         const bool sampled = L.seg >= 0;
         if (sampled) {
             const size_t j = consumed.size();
-            b = (int)(j & 1);
-            if (fork && j >= 2) PS_CUDA(cudaStreamWaitEvent(ss, consumed[j - 2], 0));
+            b = j % nb;
+            if (fork && j >= nb) PS_CUDA(cudaStreamWaitEvent(ss, consumed[j - nb], 0));
             SegmentDev d = c->segs[(size_t)L.seg].dev;
             d.entries = ebuf[b];
             d.entry_count = cbuf[b];
@@ -1347,15 +1350,21 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                     sg.dev.cap = c->entry_cap;
                 }
             }
-            {
-                void *p = nullptr;
-                if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * sizeof(NoiseEntry)) != OK)
-                    return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
-                c->owned.push_back(p);
-                c->d_entries2 = (NoiseEntry *)p;
-                if (dev_alloc(h, &p, (size_t)h->w * sizeof(int32_t)) != OK) return bail(E_NOMEM);
-                c->owned.push_back(p);
-                c->d_entry_count2 = (int32_t *)p;
+            {  // four outcome buffers where they take at most 1 GiB, else two
+                const size_t per = (size_t)c->entry_cap * h->w * sizeof(NoiseEntry);
+                const size_t nb = 4 * per <= ((size_t)1 << 30) ? 4 : 2;
+                c->fent.assign(1, c->d_entries);
+                c->fcnt.assign(1, c->d_entry_count);
+                for (size_t b = 1; b < nb; ++b) {
+                    void *p = nullptr;
+                    if (dev_alloc(h, &p, per) != OK)
+                        return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
+                    c->owned.push_back(p);
+                    c->fent.push_back((NoiseEntry *)p);
+                    if (dev_alloc(h, &p, (size_t)h->w * sizeof(int32_t)) != OK) return bail(E_NOMEM);
+                    c->owned.push_back(p);
+                    c->fcnt.push_back((int32_t *)p);
+                }
             }
             for (int k = 0; k < 2; ++k)
                 if (cudaStreamCreateWithFlags(&c->fstream[k], cudaStreamNonBlocking) != cudaSuccess)

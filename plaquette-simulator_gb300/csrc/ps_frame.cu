@@ -173,6 +173,7 @@ __global__ void __launch_bounds__(256) broadcast_xz_kernel(u64 *__restrict__ X, 
 }
 
 int g_frame_sms = 0;
+int g_prio_greatest = 1;  // 1: not looked up yet (priorities are <= 0)
 
 }  // namespace
 
@@ -192,9 +193,26 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
         const int rc = allow_max_smem((const void *)frame_kernel);
         if (rc != OK) return rc;
     }
-    frame_kernel<<<(unsigned)w, 32 * FW, smem, st>>>(R, n, w, ops, op0, op1, tab, tab0, ntab, stage, slot_off,
-                                                     rand_meas, nrand, meas, rec,
-                                                nm, entries, entry_count, cap, seed, rp, from_zero);
+    // The sign kernels are the plan's critical path: launched at the highest
+    // priority, their CTAs go ahead of the side streams' queued sampling and
+    // broadcast CTAs.
+    if (g_prio_greatest == 1) {
+        int least = 0, greatest = 0;
+        PS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        g_prio_greatest = greatest;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)w);
+    cfg.blockDim = dim3(32 * FW);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = g_prio_greatest;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PS_CUDA(cudaLaunchKernelEx(&cfg, frame_kernel, R, n, w, ops, op0, op1, tab, tab0, ntab, stage, slot_off, rand_meas,
+                               nrand, meas, rec, nm, entries, entry_count, cap, seed, rp, from_zero));
     PS_CUDA(cudaGetLastError());
     return OK;
 }

@@ -129,20 +129,25 @@ __global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_
     const uint64_t total = thr[sl.count - 1];
     const uint64_t ev = rp->event_base + sl.event, word = rp->word_base + (uint64_t)k, seed = rp->seed;
     u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
-    for (uint32_t sub = 0; sub < 16; ++sub) {
-        const u32x4 u = draw_block(seed, ev, word, sub, TAG_NOISE);
+    for (uint32_t sub0 = 0; sub0 < 16; sub0 += 2) {
+        // two independent Philox chains in flight per thread
+        const u32x4 uu[2] = {draw_block(seed, ev, word, sub0, TAG_NOISE), draw_block(seed, ev, word, sub0 + 1, TAG_NOISE)};
 #pragma unroll
-        for (int l = 0; l < 4; ++l) {
-            const uint64_t v = u.v[l];
-            if (v >= total) continue;  // identity, the common case
-            int idx = 1;
-            while (v >= thr[idx - 1]) ++idx;
-            const u64 bit = 1ull << (sub * 4 + l);
-            const int pa = sl.count == 3 ? idx : (idx >> 2), pb = sl.count == 3 ? 0 : (idx & 3);
-            if (pa == 1 || pa == 2) fxa |= bit;
-            if (pa == 2 || pa == 3) fza |= bit;
-            if (pb == 1 || pb == 2) fxb |= bit;
-            if (pb == 2 || pb == 3) fzb |= bit;
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t sub = sub0 + q;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const uint64_t v = uu[q].v[l];
+                if (v >= total) continue;  // identity, the common case
+                int idx = 1;
+                while (v >= thr[idx - 1]) ++idx;
+                const u64 bit = 1ull << (sub * 4 + l);
+                const int pa = sl.count == 3 ? idx : (idx >> 2), pb = sl.count == 3 ? 0 : (idx & 3);
+                if (pa == 1 || pa == 2) fxa |= bit;
+                if (pa == 2 || pa == 3) fza |= bit;
+                if (pb == 1 || pb == 2) fxb |= bit;
+                if (pb == 2 || pb == 3) fzb |= bit;
+            }
         }
     }
     if ((fxa | fza | fxb | fzb) == 0ull) return;

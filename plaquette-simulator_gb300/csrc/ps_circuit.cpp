@@ -1330,7 +1330,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             }
             fb.finish();
             c->fprog = std::move(fb.prog);
-            if (c->fprog.tab.empty()) c->fprog.tab.push_back(0);
+            c->fprog.tab.insert(c->fprog.tab.end(), 4, 0u);  // padding: staged ranges round up to 16 bytes
             if (c->fprog.slot_off.empty()) c->fprog.slot_off.push_back(0);
             if (c->fprog.rand_meas.empty()) c->fprog.rand_meas.push_back(0);
             if (upload(h, c->owned, c->fprog.ops, &c->d_fops) || upload(h, c->owned, c->fprog.tab, &c->d_ftab) ||

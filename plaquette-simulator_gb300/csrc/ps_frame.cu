@@ -25,9 +25,18 @@ namespace {
 // and rec + (nm + k)*w (determined flags).
 constexpr int FW = 4;  // warps per shot-word
 
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
+                 : "memory");
+}
+
 __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, int64_t n, int64_t w,
                                                    const FrameOp *__restrict__ ops, uint32_t op0, uint32_t op1,
-                                                   const uint32_t *__restrict__ tab, uint32_t tab0, uint32_t ntab,
+                                                   const uint32_t *__restrict__ tab, uint32_t tab0, uint32_t ntab16,
                                                    int stage, const uint32_t *__restrict__ slot_off,
                                                    const int32_t *__restrict__ rand_meas, uint32_t nrand,
                                                    const MeasOp *__restrict__ meas, u64 *__restrict__ rec,
@@ -39,19 +48,26 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int64_t k = blockIdx.x;
     u64 *sout = sR + W + 2;  // the launch's random outcomes, drawn up front
-    uint32_t *stab = reinterpret_cast<uint32_t *>(sout + nrand);
-    FrameOp *sops = reinterpret_cast<FrameOp *>(((uintptr_t)(stab + ntab) + 15) & ~(uintptr_t)15);
-    for (int64_t i = tid; i < W; i += 32 * FW) sR[i] = from_zero ? 0ull : R[i * w + k];
+    uint32_t *stab = reinterpret_cast<uint32_t *>(((uintptr_t)(sout + nrand) + 15) & ~(uintptr_t)15);
+    FrameOp *sops = reinterpret_cast<FrameOp *>(stab + 4 * ntab16);
+    // Signs, the tab range (16-byte chunks from the aligned tab0) and the ops
+    // are copied asynchronously, all in flight at once, while the random
+    // outcomes are drawn.
+    if (from_zero) {
+        for (int64_t i = tid; i < W; i += 32 * FW) sR[i] = 0ull;
+    } else {
+        for (int64_t i = tid; i < W; i += 32 * FW) cp_async8(&sR[i], R + i * w + k);
+    }
     if (tid < 2) sR[W + tid] = 0ull;  // zero row (unused window reads) and sink row (unused window writes)
     if (stage) {
-        for (uint32_t i = tid; i < ntab; i += 32 * FW) stab[i] = tab[tab0 + i];
-        const uint32_t *src = reinterpret_cast<const uint32_t *>(ops + op0);
-        uint32_t *dst = reinterpret_cast<uint32_t *>(sops);
-        for (uint32_t i = tid; i < 4 * (op1 - op0); i += 32 * FW) dst[i] = src[i];
+        for (uint32_t i = tid; i < ntab16; i += 32 * FW) cp_async16(stab + 4 * i, tab + tab0 + 4 * i);
+        for (uint32_t i = tid; i < op1 - op0; i += 32 * FW) cp_async16(sops + i, ops + op0 + i);
     }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
     const uint64_t event_base = rp->event_base, word_base = rp->word_base;
     for (uint32_t j = tid; j < nrand; j += 32 * FW)
         sout[j] = outcome_word(meas[rand_meas[j]], seed, event_base, k, word_base);
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
     const uint32_t *T = stage ? stab : tab;  // measurement-op tab, indexed x - tb
     const uint32_t tb = stage ? tab0 : 0u;
@@ -183,12 +199,15 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
                  const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,
                  uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
                  int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero) {
-    // Staging keeps a CTA's shared memory small enough for two per SM.
-    const size_t base = frame_smem_bytes(n) + (size_t)nrand * sizeof(u64);
-    const size_t staged = base + (size_t)(tab1 - tab0) * 4 + 16 + (size_t)(op1 - op0) * sizeof(FrameOp);
+    // Staging keeps a CTA's shared memory small enough for two per SM.  The
+    // staged tab range starts at tab0 rounded down to 16 bytes (tab holds
+    // padding after its last word for the rounded-up end).
+    const size_t base = ((frame_smem_bytes(n) + (size_t)nrand * sizeof(u64)) + 15) / 16 * 16;
+    const uint32_t tab0a = tab0 & ~3u, tab1a = (tab1 + 3u) & ~3u;
+    const size_t staged = base + (size_t)(tab1a - tab0a) * 4 + (size_t)(op1 - op0) * sizeof(FrameOp);
     const int stage = staged <= kFrameStageMax ? 1 : 0;
     const size_t smem = stage ? staged : base;
-    const uint32_t ntab = stage ? tab1 - tab0 : 0u;
+    const uint32_t ntab16 = stage ? (tab1a - tab0a) / 4 : 0u;
     if (smem > 48 * 1024) {
         const int rc = allow_max_smem((const void *)frame_kernel);
         if (rc != OK) return rc;
@@ -211,7 +230,7 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
     attr[0].val.priority = g_prio_greatest;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    PS_CUDA(cudaLaunchKernelEx(&cfg, frame_kernel, R, n, w, ops, op0, op1, tab, tab0, ntab, stage, slot_off, rand_meas,
+    PS_CUDA(cudaLaunchKernelEx(&cfg, frame_kernel, R, n, w, ops, op0, op1, tab, tab0a, ntab16, stage, slot_off, rand_meas,
                                nrand, meas, rec, nm, entries, entry_count, cap, seed, rp, from_zero));
     PS_CUDA(cudaGetLastError());
     return OK;

@@ -855,7 +855,7 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
                 return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, L.tab0, L.tab1,
                                     c->d_fslot, c->d_frand + L.rand0, L.nrand, c->d_meas, c->d_res_block,
                                     (int64_t)c->meas.size(), ebuf[b], cbuf[b], c->entry_cap, (uint64_t)h->seed,
-                                    c->d_params, first ? 1 : 0);
+                                    c->d_params, first ? 1 : 0, sampled ? 1 : 0);
             });
         if (rc != OK) return rc;
         if (sampled) {

@@ -61,7 +61,7 @@ void FrameBuilder::flush_window() {
     op.kind = F_WINDOW;
     op.off = (uint32_t)prog.tab.size();
     op.len = (uint32_t)window_.size();
-    const uint32_t s = (uint32_t)(2 * n_), zero_row = (uint32_t)W_, sink_row = (uint32_t)W_ + 1;
+    const uint32_t s = (uint32_t)(2 * n_), zero_row = (uint32_t)W_;
     for (size_t j = 0; j < window_.size(); ++j) {
         DetRecord &r = window_[j];
         if (j + 1 < window_.size())  // the last measurement of the window overwrites the scratch row
@@ -69,7 +69,7 @@ void FrameBuilder::flush_window() {
         prog.tab.push_back((uint32_t)r.meas);
         prog.tab.push_back(r.c | (uint32_t)r.rd.size() << 1 | (uint32_t)r.rs.size() << 4);
         for (uint32_t t = 0; t < kWinRows; ++t) prog.tab.push_back(t < r.rd.size() ? r.rd[t] : zero_row);
-        for (uint32_t t = 0; t < kWinRows; ++t) prog.tab.push_back(t < r.rs.size() ? r.rs[t] : sink_row);
+        for (uint32_t t = 0; t < kWinRows; ++t) prog.tab.push_back(t < r.rs.size() ? r.rs[t] : (uint32_t)W_ + 1 + t);
     }
     push_op(op);
     window_.clear();

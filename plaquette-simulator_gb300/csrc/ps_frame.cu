@@ -42,12 +42,13 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
                                                    const MeasOp *__restrict__ meas, u64 *__restrict__ rec,
                                                    int64_t nm, const NoiseEntry *__restrict__ entries,
                                                    int32_t *__restrict__ entry_count, int32_t cap, uint64_t seed,
-                                                   const RunParams *__restrict__ rp, int from_zero) {
+                                                   const RunParams *__restrict__ rp, int from_zero,
+                                                   int noise_first) {
     extern __shared__ u64 sR[];
     const int64_t W = 2 * n + 1;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int64_t k = blockIdx.x;
-    u64 *sout = sR + W + 2;  // the launch's random outcomes, drawn up front
+    u64 *sout = sR + W + 1 + kWinRows;  // the launch's random outcomes, drawn up front
     uint32_t *stab = reinterpret_cast<uint32_t *>(((uintptr_t)(sout + nrand) + 15) & ~(uintptr_t)15);
     FrameOp *sops = reinterpret_cast<FrameOp *>(stab + 4 * ntab16);
     // Signs, the tab range (16-byte chunks from the aligned tab0) and the ops
@@ -58,12 +59,24 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
     } else {
         for (int64_t i = tid; i < W; i += 32 * FW) cp_async8(&sR[i], R + i * w + k);
     }
-    if (tid < 2) sR[W + tid] = 0ull;  // zero row (unused window reads) and sink row (unused window writes)
+    if (tid < 1 + (int)kWinRows) sR[W + tid] = 0ull;  // zero row (unused window reads), sinks (unused writes)
     if (stage) {
         for (uint32_t i = tid; i < ntab16; i += 32 * FW) cp_async16(stab + 4 * i, tab + tab0 + 4 * i);
         for (uint32_t i = tid; i < op1 - op0; i += 32 * FW) cp_async16(sops + i, ops + op0 + i);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
+    // A launch that starts with its segment's channel outcomes: each thread's
+    // first outcome and its rows are fetched now, under the copies' latency.
+    int pcnt = 0;
+    NoiseEntry pen;
+    pen.a = 0;
+    uint32_t pv[kFrameChunk];
+    if (noise_first) {
+        pcnt = entry_count[k];
+        if (tid < pcnt) pen = entries[k * (int64_t)cap + tid];
+#pragma unroll
+        for (uint32_t u = 0; u < kFrameChunk; ++u) pv[u] = u < pen.a ? tab[(uint32_t)pen.layer + u] : 0u;
+    }
     const uint64_t event_base = rp->event_base, word_base = rp->word_base;
     for (uint32_t j = tid; j < nrand; j += 32 * FW)
         sout[j] = outcome_word(meas[rand_meas[j]], seed, event_base, k, word_base);
@@ -77,17 +90,10 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
         const uint32_t kind = o.kind & 0xFFu;
         if (kind == F_NOISE) {
             __syncthreads();  // warp 0's measurement ops before
-            const int cnt = entry_count[k];
-            const NoiseEntry *ent = entries + k * (int64_t)cap;
-            for (int e = tid; e < cnt; e += 32 * FW) {
-                const NoiseEntry en = ent[e];  // layer: first row entry, a: row count (<= kFrameChunk)
-                const uint32_t t0 = (uint32_t)en.layer, len = en.a;
-                uint32_t v[kFrameChunk];
-#pragma unroll
-                for (uint32_t u = 0; u < kFrameChunk; ++u) v[u] = u < len ? tab[t0 + u] : 0u;  // never 0 (sel != 0)
+            auto apply = [&](const NoiseEntry &en, const uint32_t (&v)[kFrameChunk]) {
 #pragma unroll
                 for (uint32_t u = 0; u < kFrameChunk; ++u) {
-                    if (v[u] == 0u) continue;
+                    if (v[u] == 0u) continue;  // a row entry is never 0 (sel != 0)
                     const uint32_t sel = v[u] >> 28;
                     u64 m = 0ull;
                     if (sel & 1u) m ^= en.fxa;
@@ -96,6 +102,17 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
                     if (sel & 8u) m ^= en.fzb;
                     atomicXor(&sR[v[u] & kFrameRowMask], m);
                 }
+            };
+            const bool pre = noise_first && oi == op0;
+            const int cnt = pre ? pcnt : entry_count[k];
+            const NoiseEntry *ent = entries + k * (int64_t)cap;
+            if (pre && tid < cnt) apply(pen, pv);
+            for (int e = tid + (pre ? 32 * FW : 0); e < cnt; e += 32 * FW) {
+                const NoiseEntry en = ent[e];  // layer: first row entry, a: row count (<= kFrameChunk)
+                uint32_t v[kFrameChunk];
+#pragma unroll
+                for (uint32_t u = 0; u < kFrameChunk; ++u) v[u] = u < en.a ? tab[(uint32_t)en.layer + u] : 0u;
+                apply(en, v);
             }
             __syncthreads();
             if (tid == 0) entry_count[k] = 0;  // consumed: the next segment's sampling appends from 0
@@ -121,9 +138,12 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
                 if ((uint32_t)lane == o.len - 1) sR[2 * n] = acc;
             }
             __syncwarp();
-            if ((uint32_t)lane < o.len) {  // reset rows of a window are disjoint (the sink row aside)
+            if ((uint32_t)lane < o.len) {  // a lane's reset rows are distinct, and disjoint from other lanes' (sinks aside)
+                u64 v[kWinRows];
 #pragma unroll
-                for (uint32_t t = 0; t < kWinRows; ++t) sR[rs[t]] ^= acc;
+                for (uint32_t t = 0; t < kWinRows; ++t) v[t] = sR[rs[t]];
+#pragma unroll
+                for (uint32_t t = 0; t < kWinRows; ++t) sR[rs[t]] = v[t] ^ acc;
             }
             last = __shfl_sync(0xffffffffu, acc, (int)o.len - 1);
             __syncwarp();
@@ -151,7 +171,7 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
                 rec[(int64_t)o.arg * w + k] = out;
                 rec[(nm + (int64_t)o.arg) * w + k] = 0ull;
             }
-            __syncwarp();
+            // the multiplied rows exclude p and p+n (and are distinct): no barrier needed before them
             for (uint32_t t = o.off + 1 + lane; t < o.off + o.len; t += 32) {
                 const uint32_t v = T[t - tb];
                 sR[v & 0x7FFFFFFFu] ^= rpv ^ ((v >> 31) ? ~0ull : 0ull);
@@ -193,12 +213,15 @@ int g_prio_greatest = 1;  // 1: not looked up yet (priorities are <= 0)
 
 }  // namespace
 
-size_t frame_smem_bytes(int64_t n) { return (size_t)(2 * n + 3) * sizeof(u64); }  // rows, zero row, sink row
+size_t frame_smem_bytes(int64_t n) {  // rows, the zero row, kWinRows sink rows
+    return (size_t)(2 * n + 2 + kWinRows) * sizeof(u64);
+}
 
 int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
                  const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,
                  uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
-                 int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero) {
+                 int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero,
+                 int noise_first) {
     // Staging keeps a CTA's shared memory small enough for two per SM.  The
     // staged tab range starts at tab0 rounded down to 16 bytes (tab holds
     // padding after its last word for the rounded-up end).
@@ -231,7 +254,7 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     PS_CUDA(cudaLaunchKernelEx(&cfg, frame_kernel, R, n, w, ops, op0, op1, tab, tab0a, ntab16, stage, slot_off, rand_meas,
-                               nrand, meas, rec, nm, entries, entry_count, cap, seed, rp, from_zero));
+                               nrand, meas, rec, nm, entries, entry_count, cap, seed, rp, from_zero, noise_first));
     PS_CUDA(cudaGetLastError());
     return OK;
 }

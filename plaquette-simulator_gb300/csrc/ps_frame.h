@@ -51,7 +51,8 @@ enum FrameKind : uint32_t {
 // from every reset but the last one's (the last measurement overwrites it).
 // Record j sits at tab[off + kWinRec * j]: [MeasOp index][c | nread << 1 |
 // nreset << 4][kWinRows read rows][kWinRows reset rows], unused read rows
-// pointing at the zero row W and unused reset rows at the sink row W + 1.
+// pointing at the zero row W and unused reset row t at the sink row W+1+t
+// (a lane's reset rows are then distinct).
 constexpr uint32_t kWinRows = 4;
 constexpr uint32_t kWinRec = 2 + 2 * kWinRows;
 

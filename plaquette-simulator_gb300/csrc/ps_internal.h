@@ -173,7 +173,8 @@ constexpr size_t kFrameStageMax = 100 * 1024;
 int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
                  const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,
                  uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
-                 int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero);
+                 int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero,
+                 int noise_first);
 // X, Z of every shot := the shared bits xz ([2n+1][2][nw64]).
 int launch_broadcast_xz(cudaStream_t st, u64 *X, u64 *Z, int64_t n, int64_t w, const uint64_t *xz, int64_t nw64);
 

@@ -815,19 +815,37 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
     const size_t nb = c->fent.size();
     const std::vector<NoiseEntry *> &ebuf = c->fent;
     const std::vector<int32_t *> &cbuf = c->fcnt;
+    // The x / z broadcast rides on the sampling launches (their Philox
+    // arithmetic leaves HBM idle): sampling launch j writes (row, qubit)
+    // pairs [j*P/S, (j+1)*P/S) of the P = W*n; without sampling launches it
+    // is a kernel of its own on the side stream.
+    XZBroadcast bc;
+    bc.X = h->X;
+    bc.Z = h->Z;
+    bc.xz = c->d_fxz;
+    bc.n = h->n;
+    bc.w = h->w;
+    bc.nw64 = c->fprog.nw64;
+    const int64_t P = h->W * h->n;
+    int64_t nsamp = 0;
+    for (const FrameProgram::Launch &L : c->fprog.launches) nsamp += L.seg >= 0 ? 1 : 0;
     if (fork) {
         cudaEvent_t e0;
         int rc = record(st, &e0);
         if (rc != OK) return rc;
         PS_CUDA(cudaStreamWaitEvent(ss, e0, 0));
         PS_CUDA(cudaStreamWaitEvent(sb, e0, 0));
-        rc = launch_broadcast_xz(sb, h->X, h->Z, h->n, h->w, c->d_fxz, c->fprog.nw64);
-        if (rc != OK) return rc;
+        if (nsamp == 0) {
+            XZBroadcast all = bc;
+            all.rq0 = 0;
+            all.rq1 = P;
+            rc = launch_broadcast_xz(sb, all);
+            if (rc != OK) return rc;
+        }
     }
-    // The one-pass sampler appends to per-word lists from a zero count (each
-    // sign kernel zeroes the lists it consumed; a per-shot run leaves counts).
-    for (size_t b = 0; b < nb; ++b)
-        if (cbuf[b]) PS_CUDA(cudaMemsetAsync(cbuf[b], 0, (size_t)h->w * sizeof(int32_t), ss));
+    // The one-pass sampler appends to per-word lists from a zero count: the
+    // counters of this plan are zeroed at compile time, and every sign
+    // kernel zeroes the ones it consumed, so each run finds them zero.
     std::vector<cudaEvent_t> consumed;  // sign kernel done with sampled segment j
     bool first = true;
     for (const FrameProgram::Launch &L : c->fprog.launches) {
@@ -841,8 +859,12 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
             SegmentDev d = c->segs[(size_t)L.seg].dev;
             d.entries = ebuf[b];
             d.entry_count = cbuf[b];
+            XZBroadcast share = bc;
+            share.rq0 = P * (int64_t)j / nsamp;
+            share.rq1 = P * (int64_t)(j + 1) / nsamp;
             rc = timed(P_SAMPLE, [&] {
-                return launch_noise_sample_frame(ss, d, h->w, c->d_params, c->d_fslot, (uint32_t)c->fprog.ops[L.op0].arg);
+                return launch_noise_sample_frame(ss, d, h->w, c->d_params, c->d_fslot, (uint32_t)c->fprog.ops[L.op0].arg,
+                                                 share);
             });
             if (rc == OK && fork) {
                 cudaEvent_t es;
@@ -865,7 +887,13 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
         }
         first = false;
     }
-    if (!fork) return timed(P_BROADCAST, [&] { return launch_broadcast_xz(st, h->X, h->Z, h->n, h->w, c->d_fxz, c->fprog.nw64); });
+    if (!fork) {
+        if (nsamp > 0) return OK;
+        XZBroadcast all = bc;
+        all.rq0 = 0;
+        all.rq1 = P;
+        return timed(P_BROADCAST, [&] { return launch_broadcast_xz(st, all); });
+    }
     cudaEvent_t es, eb;
     if (record(ss, &es) != OK || record(sb, &eb) != OK) return E_ARG;
     PS_CUDA(cudaStreamWaitEvent(st, es, 0));
@@ -1350,20 +1378,24 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                     sg.dev.cap = c->entry_cap;
                 }
             }
-            {  // four outcome buffers where they take at most 1 GiB, else two
+            {  // four outcome buffers where they take at most 1 GiB, else two; own zeroed counters
                 const size_t per = (size_t)c->entry_cap * h->w * sizeof(NoiseEntry);
                 const size_t nb = 4 * per <= ((size_t)1 << 30) ? 4 : 2;
                 c->fent.assign(1, c->d_entries);
-                c->fcnt.assign(1, c->d_entry_count);
-                for (size_t b = 1; b < nb; ++b) {
+                c->fcnt.clear();
+                for (size_t b = 0; b < nb; ++b) {
                     void *p = nullptr;
-                    if (dev_alloc(h, &p, per) != OK)
-                        return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
-                    c->owned.push_back(p);
-                    c->fent.push_back((NoiseEntry *)p);
+                    if (b > 0) {
+                        if (dev_alloc(h, &p, per) != OK)
+                            return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
+                        c->owned.push_back(p);
+                        c->fent.push_back((NoiseEntry *)p);
+                    }
                     if (dev_alloc(h, &p, (size_t)h->w * sizeof(int32_t)) != OK) return bail(E_NOMEM);
                     c->owned.push_back(p);
                     c->fcnt.push_back((int32_t *)p);
+                    if (cudaMemsetAsync(p, 0, (size_t)h->w * sizeof(int32_t), h->stream) != cudaSuccess)
+                        return bail(cuda_fail(cudaGetLastError(), "cudaMemsetAsync"));
                 }
             }
             for (int k = 0; k < 2; ++k)

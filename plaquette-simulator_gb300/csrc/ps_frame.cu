@@ -189,23 +189,12 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
 }
 
 // x / z of every shot from the shared bits: one warp per (row, qubit), lanes
-// over 16-byte word pairs (w is even).
-__global__ void __launch_bounds__(256) broadcast_xz_kernel(u64 *__restrict__ X, u64 *__restrict__ Z, int64_t n,
-                                                           int64_t W, int64_t w, const uint64_t *__restrict__ xz,
-                                                           int64_t nw64) {
+// over 16-byte word pairs.
+__global__ void __launch_bounds__(256) broadcast_xz_kernel(XZBroadcast bc) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t rq = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rq < W * n; rq += warps) {
-        const int64_t row = rq / n, q = rq - row * n;
-        const u64 xb = (xz[(row * 2 + 0) * nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-        const u64 zb = (xz[(row * 2 + 1) * nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-        const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
-        u64 *xo = X + rq * w, *zo = Z + rq * w;
-        for (int64_t kp = lane; kp < w / 2; kp += 32) {
-            *reinterpret_cast<ulonglong2 *>(xo + 2 * kp) = xv;
-            *reinterpret_cast<ulonglong2 *>(zo + 2 * kp) = zv;
-        }
-    }
+    for (int64_t rq = bc.rq0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rq < bc.rq1; rq += warps)
+        broadcast_row_column(bc, rq, lane);
 }
 
 int g_frame_sms = 0;
@@ -259,15 +248,15 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
     return OK;
 }
 
-int launch_broadcast_xz(cudaStream_t st, u64 *X, u64 *Z, int64_t n, int64_t w, const uint64_t *xz, int64_t nw64) {
+int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc) {
+    if (bc.rq1 <= bc.rq0) return OK;
     if (g_frame_sms == 0) {
         int dev = 0;
         PS_CUDA(cudaGetDevice(&dev));
         PS_CUDA(cudaDeviceGetAttribute(&g_frame_sms, cudaDevAttrMultiProcessorCount, dev));
     }
-    const int64_t W = 2 * n + 1;
-    const int64_t blocks = std::min<int64_t>((W * n + 7) / 8, (int64_t)g_frame_sms * 8);
-    broadcast_xz_kernel<<<(unsigned)blocks, 256, 0, st>>>(X, Z, n, W, w, xz, nw64);
+    const int64_t blocks = std::min<int64_t>((bc.rq1 - bc.rq0 + 7) / 8, (int64_t)g_frame_sms * 8);
+    broadcast_xz_kernel<<<(unsigned)blocks, 256, 0, st>>>(bc);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

@@ -89,6 +89,31 @@ struct FrameProgram {
     std::vector<Launch> launches;
 };
 
+// A range [rq0, rq1) of (row, qubit) pairs of the x / z broadcast: X and Z
+// of every shot-word := the shared bits xz ([W][2][nw64]).  The sampling
+// launches of a run share the broadcast out between them.
+struct XZBroadcast {
+    unsigned long long *X = nullptr, *Z = nullptr;
+    const uint64_t *xz = nullptr;
+    int64_t n = 0, w = 0, nw64 = 0, rq0 = 0, rq1 = 0;
+};
+
+#ifdef __CUDACC__
+// One warp writes (row, qubit) rq of X and Z for every shot-word, 16 bytes
+// per lane and store (w is even).
+__device__ __forceinline__ void broadcast_row_column(const XZBroadcast &bc, int64_t rq, int lane) {
+    const int64_t row = rq / bc.n, q = rq - row * bc.n;
+    const unsigned long long xb = (bc.xz[(row * 2 + 0) * bc.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+    const unsigned long long zb = (bc.xz[(row * 2 + 1) * bc.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+    const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
+    unsigned long long *xo = bc.X + rq * bc.w, *zo = bc.Z + rq * bc.w;
+    for (int64_t kp = lane; kp < bc.w / 2; kp += 32) {
+        *reinterpret_cast<ulonglong2 *>(xo + 2 * kp) = xv;
+        *reinterpret_cast<ulonglong2 *>(zo + 2 * kp) = zv;
+    }
+}
+#endif
+
 // Host-side simulation of the shared x / z bits and emission of the sign
 // program.  Calls follow the circuit's program order.
 class FrameBuilder {

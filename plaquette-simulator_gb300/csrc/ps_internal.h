@@ -155,8 +155,10 @@ int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, c
 // Shared-x/z runs: one-pass sampling into unordered per-word lists, each
 // outcome tagged with its slot's rows slot_off[base + s] .. [base + s + 1]
 // (the counters must be zero before; the sign kernel zeroes them after).
+// bc: the share of the x / z broadcast this launch writes (bc.X null: none).
+struct XZBroadcast;
 int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
-                              const uint32_t *slot_off, uint32_t base);
+                              const uint32_t *slot_off, uint32_t base, const XZBroadcast &bc);
 int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
                    int rows, int bw, int threads, const u64 *const *recs);
 
@@ -175,8 +177,8 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
                  uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
                  int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero,
                  int noise_first);
-// X, Z of every shot := the shared bits xz ([2n+1][2][nw64]).
-int launch_broadcast_xz(cudaStream_t st, u64 *X, u64 *Z, int64_t n, int64_t w, const uint64_t *xz, int64_t nw64);
+// X, Z of every shot := the shared bits, (row, qubit) pairs [bc.rq0, bc.rq1).
+int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc);
 
 // ps_gates.cu (compiled-circuit form of the per-op kernels)
 int launch_channel_rp(cudaStream_t stream, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,

@@ -119,7 +119,16 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
 // walks a long list alone.  The counter is zeroed by the sign kernel that
 // consumes the list.
 __global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp,
-                                                          const uint32_t *__restrict__ slot_off, uint32_t base) {
+                                                          const uint32_t *__restrict__ slot_off, uint32_t base,
+                                                          XZBroadcast bc) {
+    // A share of the x / z broadcast first: its stores drain to HBM while
+    // the Philox arithmetic below keeps the ALUs busy.
+    if (bc.X) {
+        const int lane = threadIdx.x & 31;
+        const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+        for (int64_t rq = bc.rq0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rq < bc.rq1; rq += warps)
+            broadcast_row_column(bc, rq, lane);
+    }
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int s = (int)(t / w);
     const int64_t k = t - (int64_t)s * w;
@@ -808,10 +817,10 @@ int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, c
 }
 
 int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
-                              const uint32_t *slot_off, uint32_t base) {
+                              const uint32_t *slot_off, uint32_t base, const XZBroadcast &bc) {
     if (seg.nslots == 0) return OK;
     const int64_t threads = (int64_t)seg.nslots * w;
-    noise_frame_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(seg, w, rp, slot_off, base);
+    noise_frame_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(seg, w, rp, slot_off, base, bc);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

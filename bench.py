@@ -388,17 +388,19 @@ def main():
         #  sign program: every launch reads and writes the signs of all rows
         #    and shot-words (the first starts from zero), plus the records
         #    (result + determined words per measurement);
-        #  x/z broadcast: the x and z words of every row, qubit and shot-word;
-        #  channel sampling: 4 outcome words written and read back per
-        #    (channel, shot-word).
+        #  channel sampling: the sampling launches also write the x/z
+        #    broadcast -- the x and z words of every row, qubit and shot-word
+        #    -- counted here; their outcome entries (tens of MB) are not.
         nl = max(1, prof["sign_program"]["launches"])
         kind_bytes = {
             "sign_program": (2 * nl - 1) * W * w_words * 8 + 2 * nm * w_words * 8,
-            "xz_broadcast": 2 * W * n_q * w_words * 8,
-            "channel_sample": 2 * 4 * 8 * int(fused.stats["num_channels"]) * w_words,
+            "channel_sample": 2 * W * n_q * w_words * 8,
         }
+        if prof.get("xz_broadcast", {}).get("launches"):
+            kind_bytes["xz_broadcast"] = 2 * W * n_q * w_words * 8
+            kind_bytes["channel_sample"] = 0
         kernel_of = {"sign_program": "frame_kernel", "xz_broadcast": "broadcast_xz_kernel",
-                     "channel_sample": "noise_dense_kernel + noise_compact_kernel"}
+                     "channel_sample": "noise_frame_kernel (one-pass channel sampling + its share of the x/z broadcast)"}
     else:
         meas_bytes = fused.measure_bytes(reset=True)
         seg_bytes = float(fused.stats["segment_bytes"])
@@ -423,8 +425,11 @@ def main():
                               "algorithmic_GBps": kind_bytes[k] / max(1e-9, prof[k]["ms"] / 1e3) / 1e9}
                           for k in kind_bytes}}
     if dom == "sign_program":
-        roofline["note"] = ("latency-bound: one warp per shot-word runs the sign program's ops in order on "
+        roofline["note"] = ("latency-bound: one CTA per shot-word runs the sign program's ops in order on "
                             "signs held in shared memory; it moves little HBM data by design")
+    elif dom == "channel_sample":
+        roofline["note"] = ("the sampling launches carry the Philox work (16 blocks per channel and shot-word, "
+                            "integer-bound) and write the x/z broadcast under it; achieved counts the broadcast only")
 
     line = {
         "metric": METRIC, "value": value, "unit": "shot-gates/s", "n_gpus": world, "steps": args.steps,

@@ -121,24 +121,33 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
 __global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp,
                                                           const uint32_t *__restrict__ slot_off, uint32_t base,
                                                           XZBroadcast bc) {
-    // A share of the x / z broadcast first: its stores drain to HBM while
-    // the Philox arithmetic below keeps the ALUs busy.
-    if (bc.X) {
-        const int lane = threadIdx.x & 31;
-        const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-        for (int64_t rq = bc.rq0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rq < bc.rq1; rq += warps)
-            broadcast_row_column(bc, rq, lane);
-    }
+    // A share of the x / z broadcast, interleaved with the Philox arithmetic
+    // (a (row, qubit) pair after every other pair of blocks, the rest at the
+    // end) so that its stores drain to HBM while the ALUs stay busy.  Every
+    // thread stays to the end: the broadcast is written by whole warps.
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    int64_t rq = bc.X ? bc.rq0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) : bc.rq1;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int s = (int)(t / w);
     const int64_t k = t - (int64_t)s * w;
-    if (s >= seg.nslots) return;
-    const NoiseSlot sl = seg.slots[s];
-    const uint64_t *thr = seg.thr + sl.thr_off;
-    const uint64_t total = thr[sl.count - 1];
+    const bool active = s < seg.nslots;
+    NoiseSlot sl{};
+    const uint64_t *thr = seg.thr;
+    uint64_t total = 0;  // no draw is below 0: an inactive thread samples nothing
+    if (active) {
+        sl = seg.slots[s];
+        thr = seg.thr + sl.thr_off;
+        total = thr[sl.count - 1];
+    }
     const uint64_t ev = rp->event_base + sl.event, word = rp->word_base + (uint64_t)k, seed = rp->seed;
     u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
     for (uint32_t sub0 = 0; sub0 < 16; sub0 += 2) {
+        if ((sub0 & 2) && rq < bc.rq1) {
+            broadcast_row_column(bc, rq, lane);
+            rq += warps;
+        }
+        if (!active) continue;
         // two independent Philox chains in flight per thread
         const u32x4 uu[2] = {draw_block(seed, ev, word, sub0, TAG_NOISE), draw_block(seed, ev, word, sub0 + 1, TAG_NOISE)};
 #pragma unroll
@@ -159,6 +168,7 @@ __global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_
             }
         }
     }
+    for (; rq < bc.rq1; rq += warps) broadcast_row_column(bc, rq, lane);
     if ((fxa | fza | fxb | fzb) == 0ull) return;
     const uint32_t t0 = slot_off[base + s], t1 = slot_off[base + s + 1];
     const int nch = (int)((t1 - t0 + kFrameChunk - 1) / kFrameChunk);

@@ -16,6 +16,9 @@ FrameBuilder::FrameBuilder(int64_t n) : n_(n), W_(2 * n + 1), nw_((n + 63) / 64)
         flip(x_, i, i);
         flip(z_, i + n_, i);
     }
+    // and r(i) = [i == 2n] (MiscFunctors.hpp:8-28): the device starts every
+    // sign at 0, so the scratch row's 1 is a pending flip
+    fset(2 * n_, true);
     prog.nw64 = nw_;
     flipped_.assign((size_t)W_, 0);
     open_range();

@@ -208,3 +208,43 @@ def test_shared_xz_large_register(ps, O):
         assert not x[i, :m].any() and not z[n + i, :m].any() and not r[i].any() and not r[n + i].any()
     with pytest.raises(Exception):
         cc.run(reset=False)  # the per-shot plan does not take 3,100 qubits
+
+
+def _edge_circuits():
+    from plaquette_simulator import circuits as C
+    no_meas = C.Circuit(6)
+    for q in range(6):
+        no_meas.h(q)
+        no_meas.pauli1(q, 0.1, 0.05, 0.2)
+    for q in range(5):
+        no_meas.cx(q, q + 1)
+        no_meas.pauli2(q, q + 1, [0.01 * (j + 1) for j in range(15)])
+    one = C.Circuit(1)
+    for _ in range(20):
+        one.h(0)
+        one.pauli1(0, 0.1, 0.1, 0.1)
+        one.m(0)
+        one.s(0)
+        one.r(0)
+    return {
+        "no_measurements": (no_meas, 130),
+        "no_noise": (random_mixed_circuit(8, 300, seed=58, noise=False, flags=False), 70),
+        "empty": (C.Circuit(3), 64),
+        "one_qubit": (one, 100),
+        "one_shot": (random_mixed_circuit(10, 300, seed=59, flags=False), 1),
+        "word_and_one": (random_mixed_circuit(10, 300, seed=60, flags=False), 65),
+    }
+
+
+@pytest.mark.parametrize("name", list(_edge_circuits().keys()))
+def test_shared_xz_edge_cases(ps, O, name):
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ, B = _edge_circuits()[name]
+    st = ps.CliffordState(circ.num_qubits, B, 31, True)
+    cc = CompiledCircuit(circ, st, fused=True, graph=True)
+    assert cc.stats["shared_xz"] == 1
+    cc.run(reset=True)
+    st.synchronize()
+    o = O.Oracle(circ.num_qubits, B, seed=31)
+    o.run(circ.op_array(), circ.param_array())
+    _check(st, o, cc.first_record, circ.num_measurements())

@@ -150,8 +150,8 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
         } else if (kind == F_MEAS_DET) {
             u64 acc = 0ull;
             for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) acc ^= sR[T[t - tb]];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, off);
+            acc = (u64)__reduce_xor_sync(0xffffffffu, (unsigned)(acc >> 32)) << 32 |
+                  (u64)__reduce_xor_sync(0xffffffffu, (unsigned)acc);
             if (o.kind >> 8) acc = ~acc;
             if (lane == 0) {
                 rec[(int64_t)o.arg * w + k] = acc;

@@ -23,6 +23,9 @@ LIB = os.path.join(LIBDIR, "libps_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 CU_FLAGS = ARCH + COMMON + ["-lineinfo", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+# .cpp sources without device code, handed to the host compiler as they are
+# (the others use CUDA language extensions and compile as CUDA)
+HOST_CPP = {"ps_frame.cpp"}
 
 
 def nvcc() -> str:
@@ -53,7 +56,7 @@ def _compile(src: str, force: bool) -> str:
     obj = os.path.join(BUILD, src + ".o")
     path = os.path.join(CSRC, src)
     if force or _newer(obj, [path] + _headers()):
-        flags = CU_FLAGS if src.endswith(".cu") else ARCH + COMMON + ["-x", "cu"]
+        flags = CU_FLAGS if src.endswith(".cu") else ARCH + COMMON + ([] if src in HOST_CPP else ["-x", "cu"])
         cmd = [nvcc()] + flags + ["-c", path, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

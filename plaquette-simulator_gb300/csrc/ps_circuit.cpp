@@ -877,7 +877,7 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
                 return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, L.tab0, L.tab1,
                                     c->d_fslot, c->d_frand + L.rand0, L.nrand, c->d_meas, c->d_res_block,
                                     (int64_t)c->meas.size(), ebuf[b], cbuf[b], c->entry_cap, (uint64_t)h->seed,
-                                    c->d_params, first ? 1 : 0, sampled ? 1 : 0);
+                                    c->d_params, first ? 1 : 0, sampled ? 1 : 0, L.scratch);
             });
         if (rc != OK) return rc;
         if (sampled) {
@@ -1357,6 +1357,11 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 }
             }
             fb.finish();
+            // F_LINEAR scratch: what shared memory leaves beside the signs
+            // and up to n random outcomes of a launch
+            const size_t fixed = frame_smem_bytes(h->n) + (size_t)h->n * sizeof(u64) + 16;
+            fb.linearize(fixed < kSegSmemMax ? (uint32_t)std::min<size_t>((kSegSmemMax - fixed) / sizeof(u64), 1u << 20)
+                                             : 0u);
             c->fprog = std::move(fb.prog);
             c->fprog.tab.insert(c->fprog.tab.end(), 4, 0u);  // padding: staged ranges round up to 16 bytes
             if (c->fprog.slot_off.empty()) c->fprog.slot_off.push_back(0);

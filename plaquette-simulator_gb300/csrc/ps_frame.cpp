@@ -369,4 +369,293 @@ void FrameBuilder::finish() {
         }
 }
 
+namespace {
+
+// An affine form over GF(2): sorted input indices (shared-memory sign
+// indices, see F_LINEAR) and a constant.
+struct Form {
+    std::vector<uint32_t> t;
+    bool c = false;
+};
+
+void xor_into(Form &a, const Form &b) {
+    a.c ^= b.c;
+    if (b.t.empty()) return;
+    std::vector<uint32_t> out;
+    out.reserve(a.t.size() + b.t.size());
+    std::set_symmetric_difference(a.t.begin(), a.t.end(), b.t.begin(), b.t.end(), std::back_inserter(out));
+    a.t.swap(out);
+}
+
+// Largest F_LINEAR record (words of tab; a launch stages its measurement
+// rows in shared memory) and the terms a run may cost per op it replaces:
+// one op on one warp is a chain of a few dependent shared-memory steps,
+// while the CTA's 128 threads evaluate about that many terms in the same
+// time.
+constexpr size_t kLinWordsMax = 16384;
+constexpr size_t kLinTermsPerOp = 512;
+
+// The sign program's measurement ops executed on forms instead of signs,
+// exactly as frame_kernel runs them: the signs at the start of a run are
+// the inputs (row i = {i}), a random outcome r is {kLinRand0(W) + r}.  Every
+// op can be taken back, so a run is cut where its map outgrows the budget.
+class PhaseMap {
+  public:
+    PhaseMap(int64_t n, const std::vector<uint32_t> &tab)
+        : n_((uint32_t)n), W_((uint32_t)(2 * n + 1)), tab_(tab), stamp_(W_, 0), logged_(W_, 0), form_(W_) {}
+
+    void reset() {
+        ++cur_;
+        touched_.clear();
+        recs_.clear();
+        has_last_ = false;
+        last_ = Form{};
+        rec_terms_ = row_terms_ = 0;
+        nops_ = 0;
+    }
+    size_t nops() const { return nops_; }
+
+    // false (and nothing applied) for a reset X whose outcome the run does not hold
+    bool apply(const FrameOp &o) {
+        const uint32_t kind = o.kind & 0xFFu;
+        if (kind == F_RESET_X && !has_last_) return false;
+        sv_ = {recs_.size(), touched_.size(), rec_terms_, row_terms_, has_last_};
+        sv_last_ = last_;
+        ++op_;
+        log_.clear();
+        const uint32_t s = 2 * n_;
+        if (kind == F_WINDOW) {
+            std::vector<Form> acc(o.len);
+            for (uint32_t j = 0; j < o.len; ++j) {
+                const uint32_t *rc = &tab_[o.off + kWinRec * j];
+                acc[j].c = rc[1] & 1u;
+                for (uint32_t t = 0; t < kWinRows; ++t) xor_into(acc[j], get(rc[2 + t]));
+                record(rc[0] | kLinDet, acc[j]);
+            }
+            mut(s) = acc[o.len - 1];
+            for (uint32_t j = 0; j < o.len; ++j)
+                for (uint32_t t = 0; t < kWinRows; ++t) {
+                    const uint32_t r = tab_[o.off + kWinRec * j + 2 + kWinRows + t];
+                    if (r < W_) xor_into(mut(r), acc[j]);
+                }
+            set_last(acc[o.len - 1]);
+        } else if (kind == F_MEAS_DET) {
+            Form a;
+            a.c = (o.kind >> 8) != 0u;
+            for (uint32_t t = o.off; t < o.off + o.len; ++t) xor_into(a, get(tab_[t]));
+            record((uint32_t)o.arg | kLinDet, a);
+            mut(s) = a;
+            set_last(a);
+        } else if (kind == F_MEAS_RAND) {
+            const uint32_t p = tab_[o.off];
+            const Form rpv = get(p + n_);
+            Form out;
+            out.t.push_back(kLinRand0(W_) + (o.kind >> 8));
+            mut(p) = rpv;
+            mut(p + n_) = out;
+            record((uint32_t)o.arg, out);
+            for (uint32_t t = o.off + 1; t < o.off + o.len; ++t) {
+                Form &f = mut(tab_[t] & 0x7FFFFFFFu);
+                xor_into(f, rpv);
+                f.c ^= (tab_[t] >> 31) != 0u;
+            }
+            set_last(out);
+        } else {  // F_RESET_X, F_FLIP
+            for (uint32_t t = o.off; t < o.off + o.len; ++t) {
+                const uint32_t r = tab_[t];
+                if (r >= W_) continue;
+                if (kind == F_RESET_X)
+                    xor_into(mut(r), last_);
+                else
+                    mut(r).c ^= true;
+            }
+        }
+        for (const Log &l : log_) row_terms_ += form_[l.row].t.size() - (l.was ? l.old.t.size() : 0);
+        ++nops_;
+        return true;
+    }
+
+    void undo() {
+        for (size_t i = log_.size(); i-- > 0;) {
+            const Log &l = log_[i];
+            form_[l.row] = l.old;
+            if (!l.was) stamp_[l.row] = 0;
+        }
+        log_.clear();
+        recs_.resize(sv_.nrec);
+        touched_.resize(sv_.ntouched);
+        rec_terms_ = sv_.rec_terms;
+        row_terms_ = sv_.row_terms;
+        has_last_ = sv_.has_last;
+        last_ = sv_last_;
+        --nops_;
+    }
+
+    bool over(uint32_t max_rows, size_t ops) const {
+        const size_t terms = rec_terms_ + row_terms_ + last_.t.size();
+        const size_t nout = recs_.size() + touched_.size() + 1;
+        return touched_.size() + 1 > max_rows || 5 + 2 * nout + terms > kLinWordsMax ||
+               terms > kLinTermsPerOp * (ops + 1);
+    }
+
+    // The run as one F_LINEAR op (appended to tab); scratch: its new-row words.
+    FrameOp emit(std::vector<uint32_t> &tab, uint32_t *scratch) const {
+        std::vector<uint32_t> rows;
+        for (uint32_t r : touched_) {
+            const Form &f = form_[r];
+            if (!(f.c == false && f.t.size() == 1 && f.t[0] == r)) rows.push_back(r);
+        }
+        std::sort(rows.begin(), rows.end());
+        const uint32_t nrec = (uint32_t)recs_.size(), nrow = (uint32_t)rows.size(), nlast = has_last_ ? 1u : 0u;
+        const uint32_t nout = nrec + nrow + nlast;
+        FrameOp op{};
+        op.kind = F_LINEAR;
+        op.off = (uint32_t)tab.size();
+        tab.push_back(nrec);
+        tab.push_back(nrow);
+        tab.push_back(nlast);
+        tab.push_back(0u);
+        for (const Rec &r : recs_) tab.push_back(r.dst | (r.f.c ? kLinConst : 0u));
+        for (uint32_t r : rows) tab.push_back(r | (form_[r].c ? kLinConst : 0u));
+        if (nlast) tab.push_back(last_.c ? kLinConst : 0u);
+        uint32_t b = 0;
+        tab.push_back(b);
+        for (const Rec &r : recs_) tab.push_back(b += (uint32_t)r.f.t.size());
+        for (uint32_t r : rows) tab.push_back(b += (uint32_t)form_[r].t.size());
+        if (nlast) tab.push_back(b += (uint32_t)last_.t.size());
+        for (const Rec &r : recs_) tab.insert(tab.end(), r.f.t.begin(), r.f.t.end());
+        for (uint32_t r : rows) tab.insert(tab.end(), form_[r].t.begin(), form_[r].t.end());
+        if (nlast) tab.insert(tab.end(), last_.t.begin(), last_.t.end());
+        op.len = (uint32_t)tab.size() - op.off;
+        *scratch = nrow + nlast;
+        (void)nout;
+        return op;
+    }
+
+  private:
+    struct Rec {
+        uint32_t dst;
+        Form f;
+    };
+    struct Log {
+        uint32_t row;
+        bool was;  // touched before this op
+        Form old;
+    };
+    struct Saved {
+        size_t nrec, ntouched, rec_terms, row_terms;
+        bool has_last;
+    };
+    uint32_t n_, W_;
+    const std::vector<uint32_t> &tab_;
+    std::vector<uint32_t> stamp_, logged_;  // row -> run that touched it, op that logged it
+    std::vector<Form> form_;
+    std::vector<uint32_t> touched_;
+    std::vector<Rec> recs_;
+    std::vector<Log> log_;
+    Form last_, sv_last_;
+    bool has_last_ = false;
+    size_t rec_terms_ = 0, row_terms_ = 0, nops_ = 0;
+    uint32_t cur_ = 0, op_ = 0;
+    Saved sv_{};
+
+    Form get(uint32_t r) const {  // the zero row and the sinks read as 0
+        if (r >= W_) return Form{};
+        if (stamp_[r] != cur_) return Form{{r}, false};
+        return form_[r];
+    }
+    Form &mut(uint32_t r) {
+        const bool was = stamp_[r] == cur_;
+        if (logged_[r] != op_) {
+            logged_[r] = op_;
+            log_.push_back({r, was, was ? form_[r] : Form{}});
+        }
+        if (!was) {
+            stamp_[r] = cur_;
+            form_[r] = Form{{r}, false};
+            touched_.push_back(r);
+        }
+        return form_[r];
+    }
+    void record(uint32_t dst, const Form &f) {
+        recs_.push_back({dst, f});
+        rec_terms_ += f.t.size();
+    }
+    void set_last(const Form &f) {
+        last_ = f;
+        has_last_ = true;
+    }
+};
+
+}  // namespace
+
+void FrameBuilder::linearize(uint32_t max_rows) {
+    if (max_rows < 2) return;
+    const std::vector<FrameOp> old = prog.ops;
+    std::vector<uint32_t> &tab = prog.tab;
+    std::vector<FrameOp> ops;
+    PhaseMap pm(n_, tab);
+    for (FrameProgram::Launch &L : prog.launches) {
+        // The launch's measurement ops, linear or kept, get a fresh
+        // contiguous tab range (the staged one).
+        const uint32_t new0 = (uint32_t)ops.size(), t0 = (uint32_t)tab.size();
+        std::vector<uint32_t> run;  // old indices of the ops in pm
+        L.scratch = 0;
+        auto keep = [&](uint32_t i) {
+            FrameOp o = old[i];
+            if ((o.kind & 0xFFu) != F_NOISE) {
+                const uint32_t a = o.off, b = op_tab_end_[i];
+                o.off = (uint32_t)tab.size();
+                for (uint32_t t = a; t < b; ++t) {
+                    const uint32_t v = tab[t];
+                    tab.push_back(v);
+                }
+            }
+            ops.push_back(o);
+        };
+        auto flush = [&]() {
+            if (pm.nops() >= 2) {
+                uint32_t s = 0;
+                ops.push_back(pm.emit(tab, &s));
+                L.scratch = std::max(L.scratch, s);
+            } else {
+                for (uint32_t i : run) keep(i);
+            }
+            run.clear();
+            pm.reset();
+        };
+        pm.reset();
+        for (uint32_t i = L.op0; i < L.op1; ++i) {
+            if ((old[i].kind & 0xFFu) == F_NOISE) {
+                flush();
+                keep(i);
+                continue;
+            }
+            bool applied = pm.apply(old[i]);
+            if (applied && pm.over(max_rows, run.size() + 1)) {
+                pm.undo();
+                flush();
+                applied = pm.apply(old[i]);
+                if (applied && pm.over(max_rows, 1)) {
+                    pm.undo();
+                    applied = false;
+                }
+            }
+            if (applied) {
+                run.push_back(i);
+            } else {  // on its own, between the runs before and after it
+                flush();
+                keep(i);
+            }
+        }
+        flush();
+        L.op0 = new0;
+        L.op1 = (uint32_t)ops.size();
+        L.tab0 = t0;
+        L.tab1 = (uint32_t)tab.size();
+    }
+    prog.ops.swap(ops);
+    op_tab_end_.clear();
+}
+
 }  // namespace ps

@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
     u64 *sout = sR + W + 1 + kWinRows;  // the launch's random outcomes, drawn up front
     uint32_t *stab = reinterpret_cast<uint32_t *>(((uintptr_t)(sout + nrand) + 15) & ~(uintptr_t)15);
     FrameOp *sops = reinterpret_cast<FrameOp *>(stab + 4 * ntab16);
+    u64 *snew = reinterpret_cast<u64 *>(sops + (stage ? op1 - op0 : 0u));  // F_LINEAR's new rows
     // Signs, the tab range (16-byte chunks from the aligned tab0) and the ops
     // are copied asynchronously, all in flight at once, while the random
     // outcomes are drawn.
@@ -116,6 +117,29 @@ __global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, 
             }
             __syncthreads();
             if (tid == 0) entry_count[k] = 0;  // consumed: the next segment's sampling appends from 0
+        } else if (kind == F_LINEAR) {
+            // every output from the signs as they were, then the new rows
+            __syncthreads();  // warp 0's measurement ops before
+            const uint32_t *L = T + (o.off - tb);
+            const uint32_t nrec = L[0], nrow = L[1], nlast = L[2], nout = nrec + nrow + nlast;
+            const uint32_t *dst = L + 4, *beg = dst + nout, *term = beg + nout + 1;
+            for (uint32_t j = tid; j < nout; j += 32 * FW) {
+                const uint32_t d = dst[j], t1 = beg[j + 1];
+                u64 v = (d & kLinConst) ? ~0ull : 0ull;
+#pragma unroll 4
+                for (uint32_t t = beg[j]; t < t1; ++t) v ^= sR[term[t]];
+                if (j < nrec) {
+                    const int64_t m = (int64_t)(d & kLinIndex);
+                    rec[m * w + k] = v;
+                    rec[(nm + m) * w + k] = (d & kLinDet) ? ~0ull : 0ull;
+                } else {
+                    snew[j - nrec] = v;
+                }
+            }
+            __syncthreads();
+            for (uint32_t j = tid; j < nrow; j += 32 * FW) sR[dst[nrec + j] & kLinIndex] = snew[j];
+            if (nlast) last = snew[nrow];
+            __syncthreads();
         } else if (wid != 0) {
             continue;  // the measurement ops run on warp 0
         } else if (kind == F_WINDOW) {
@@ -210,15 +234,18 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
                  const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,
                  uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
                  int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero,
-                 int noise_first) {
+                 int noise_first, uint32_t scratch) {
     // Staging keeps a CTA's shared memory small enough for two per SM.  The
     // staged tab range starts at tab0 rounded down to 16 bytes (tab holds
-    // padding after its last word for the rounded-up end).
+    // padding after its last word for the rounded-up end).  The F_LINEAR
+    // scratch (new rows) comes last.
     const size_t base = ((frame_smem_bytes(n) + (size_t)nrand * sizeof(u64)) + 15) / 16 * 16;
     const uint32_t tab0a = tab0 & ~3u, tab1a = (tab1 + 3u) & ~3u;
-    const size_t staged = base + (size_t)(tab1a - tab0a) * 4 + (size_t)(op1 - op0) * sizeof(FrameOp);
+    const size_t scr = (size_t)scratch * sizeof(u64);
+    const size_t staged = base + (size_t)(tab1a - tab0a) * 4 + (size_t)(op1 - op0) * sizeof(FrameOp) + scr;
     const int stage = staged <= kFrameStageMax ? 1 : 0;
-    const size_t smem = stage ? staged : base;
+    const size_t smem = stage ? staged : base + scr;
+    if (smem > kSegSmemMax) return E_ARG;
     const uint32_t ntab16 = stage ? (tab1a - tab0a) / 4 : 0u;
     if (smem > 48 * 1024) {
         const int rc = allow_max_smem((const void *)frame_kernel);

@@ -39,6 +39,7 @@ enum FrameKind : uint32_t {
     F_RESET_X = 3,    // R[row] ^= outcome of the last measurement, rows tab[off..off+len)
     F_FLIP = 4,       // R[row] ^= ~0, rows tab[off..off+len)
     F_WINDOW = 5,     // len deterministic measurements, one per lane (below)
+    F_LINEAR = 6,     // a run of the ops above as one linear map over the signs (below); arg unused
 };
 
 // A window of deterministic measurements (each with its reset X) that run
@@ -55,6 +56,23 @@ enum FrameKind : uint32_t {
 // (a lane's reset rows are then distinct).
 constexpr uint32_t kWinRows = 4;
 constexpr uint32_t kWinRec = 2 + 2 * kWinRows;
+
+// Between two channel ops every op above is affine over GF(2) in the signs
+// it starts from and the launch's random outcomes (drawn up front), so a run
+// of them is, for every record it writes, every row it changes and the
+// latest outcome (read by a later reset X), a constant XOR a set of inputs.
+// An F_LINEAR op holds those sets; all threads of the CTA evaluate them at
+// once, then write the changed rows, instead of one warp stepping through the
+// run.  tab[off..off+len): [nrec][nrow][nlast][0], dst[nout], beg[nout + 1],
+// terms, nout = nrec + nrow + nlast (records, changed rows, the latest
+// outcome), output j = const XOR sR[terms[beg[j] .. beg[j+1])], a term being
+// a shared-memory sign index (rows < W, random outcome r at kLinRand0(W) + r).
+// dst: record MeasOp index | kLinConst | kLinDet (determined), or row |
+// kLinConst.
+constexpr uint32_t kLinIndex = 0x3FFFFFFFu;
+constexpr uint32_t kLinConst = 1u << 30;
+constexpr uint32_t kLinDet = 1u << 31;
+inline uint32_t kLinRand0(int64_t W) { return (uint32_t)W + 1 + kWinRows; }
 
 struct FrameOp {
     uint32_t kind;  // FrameKind | constant bit << 8
@@ -82,6 +100,7 @@ struct FrameProgram {
         uint32_t op0, op1;
         uint32_t tab0, tab1;  // tab range of the launch's measurement ops (staged in shared memory)
         uint32_t rand0, nrand;  // the launch's random measurements: rand_meas[rand0, rand0 + nrand)
+        uint32_t scratch = 0;   // shared-memory words its F_LINEAR ops stage new rows in (nrow + nlast)
     };
     // MeasOp indices of the random measurements, launch by launch: their
     // outcomes depend on no sign, so a launch draws them all up front.
@@ -127,6 +146,10 @@ class FrameBuilder {
     void end_segment();
     void measure(int64_t q, int32_t meas_index, bool reset);
     void finish();
+    // After finish(): every run of two or more measurement-phase ops becomes
+    // F_LINEAR ops whose new rows take at most max_rows words of shared
+    // memory (0: none), where that costs the device fewer steps.
+    void linearize(uint32_t max_rows);
     FrameProgram prog;
 
     struct DetRecord {

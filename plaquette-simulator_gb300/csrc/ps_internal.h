@@ -176,7 +176,7 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
                  const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,
                  uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
                  int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero,
-                 int noise_first);
+                 int noise_first, uint32_t scratch);
 // X, Z of every shot := the shared bits, (row, qubit) pairs [bc.rq0, bc.rq1).
 int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc);
 

@@ -442,7 +442,8 @@ def main():
                    "tableau_bytes": 3 * (2 * circ.num_qubits + 1) * circ.num_qubits * ((shots + 63) // 64) * 8,
                    "l2": "no flush needed: the 1.65 GB tableau is larger than the 129 MB L2",
                    "parallelism": f"shots split over {world} GPU(s), {shots} per GPU"},
-        "gpu_launches": int(fused.stats["launches_per_run"]) + 1,
+        # the per-shot plan's reset adds init_zero_kernel; shared-x/z runs start from zero signs in the sign kernel
+        "gpu_launches": int(fused.stats["launches_per_run"]) + (0 if shared else 1),
         "clocks": clocks,
         "e2e": {"value": gates * shots * world / (e2e_ms / 1e3), "unit": "shot-gates/s",
                 "h2d_bytes_per_step": 16, "d2h_bytes_per_step": d2h,

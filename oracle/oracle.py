@@ -78,6 +78,7 @@ def lib():
             "ora_run": (C.c_int, [_vp, _vp, _i64, _vp, _vp]),
             "ora_threshold": (_u64, [C.c_double]),
             "ora_draw_u32": (C.c_uint32, [_i64, _u64, _i64, C.c_uint32]),
+            "ora_channel_paulis": (None, [_i64, _u64, _i64, _i64, _vp, C.c_int, _vp]),
             "ora_philox4x32_10": (None, [_vp, _vp, _vp]),
             "ora_row_product_sign": (_i32, [_vp, _i64, _i64, _i64]),
             "ora_row_multiply": (None, [_vp, _i64, _i64, _i64]),

@@ -39,9 +39,11 @@ void ora_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 
 enum { TAG_MEASURE = 1, TAG_NOISE = 2 };
 
-/* One 32-bit draw for (seed, event, global shot, tag).  Shot g lives in
- * 64-shot word g>>6; the word's 64 draws come from 16 Philox blocks with
- * counter (sub, word, event, tag), sub = (g&63)>>2, lane = g&3. */
+/* One 32-bit draw for (seed, event, global shot, tag), the draw of a
+ * random measurement's shot.  Shot g lives in 64-shot word g>>6; the word's
+ * 64 draws come from 16 Philox blocks with counter (sub, word, event, tag),
+ * sub = (g&63)>>2, lane = g&3.  (Pauli channels draw per word instead:
+ * ora_channel_paulis.) */
 uint32_t ora_draw_u32(int64_t seed, uint64_t event, int64_t gshot, uint32_t tag) {
     uint32_t key[2] = {(uint32_t)((uint64_t)seed & 0xffffffffu), (uint32_t)((uint64_t)seed >> 32)};
     uint64_t word = (uint64_t)gshot >> 6;
@@ -451,46 +453,109 @@ static void apply_flag_paulis(ora_state *s, int64_t q, const int32_t *fx, const 
     ora_s_flag(s, q, fz);
 }
 
-static int pick_index(uint32_t u, const uint64_t *thr, int count) {
-    for (int k = 0; k < count; ++k)
-        if ((uint64_t)u < thr[k]) return k + 1;
-    return 0;
+/* Pauli-channel sampling (this library's own scheme; the reference has no
+ * channel op).  thr[k] = ora_threshold of the cumulative probability of
+ * Paulis 1..k+1, total = thr[count-1]: a shot is hit with probability
+ * total / 2^32 and a hit takes Pauli k+1 with probability
+ * (thr[k] - thr[k-1]) / total.  The 64 shots of a global word are sampled by
+ * gaps: with S_0 = 2^32 and S_{j+1} = floor(S_j (2^32 - total) / 2^32), a
+ * draw u puts the next hit g shots on, g the first with u >= S_{g+1}; one
+ * more draw v picks the hit's Pauli, the first k with
+ * floor(v total / 2^32) < thr[k].  Draw i of the word is lane i%4 of Philox
+ * block (i/4, word, event, TAG_NOISE). */
+static uint64_t surv64(uint64_t total) {
+    if (total == 0) return (uint64_t)1 << 32;
+    const uint64_t q = ((uint64_t)1 << 32) - total;
+    uint64_t s = (uint64_t)1 << 32;
+    for (int j = 0; j < 64; ++j) s = (s * q) >> 32;
+    return s;
 }
 
-void ora_pauli_channel_1(ora_state *s, int64_t q, const float p[3]) {
-    uint64_t thr[3];
+static void channel_word(int64_t seed, uint64_t event, uint64_t word, const uint64_t *thr, int count, uint64_t s64,
+                         int32_t idx[64]) {
+    memset(idx, 0, 64 * sizeof(int32_t));
+    const uint64_t total = thr[count - 1];
+    if (total == 0) return;
+    const uint32_t key[2] = {(uint32_t)((uint64_t)seed & 0xffffffffu), (uint32_t)((uint64_t)seed >> 32)};
+    uint32_t ctr[4] = {0u, (uint32_t)word, (uint32_t)event, TAG_NOISE}, blk[4];
+    ora_philox4x32_10(ctr, key, blk);
+    uint32_t u = blk[0];
+    if ((uint64_t)u < s64) return;
+    const uint64_t q = ((uint64_t)1 << 32) - total;
+    uint32_t i = 1;
+    int pos = 0;
+    for (;;) {
+        uint64_t s = (uint64_t)1 << 32;
+        for (;;) {
+            s = (s * q) >> 32;
+            if ((uint64_t)u >= s) break;
+            if (++pos == 64) return;
+        }
+        if ((i & 3u) == 0u) {
+            ctr[0] = i >> 2;
+            ora_philox4x32_10(ctr, key, blk);
+        }
+        const uint64_t v = ((uint64_t)blk[i & 3u] * total) >> 32;
+        ++i;
+        int k = 1;
+        while (v >= thr[k - 1]) ++k;
+        idx[pos] = k;
+        if (++pos == 64) return;
+        if ((i & 3u) == 0u) {
+            ctr[0] = i >> 2;
+            ora_philox4x32_10(ctr, key, blk);
+        }
+        u = blk[i & 3u];
+        ++i;
+    }
+}
+
+void ora_channel_paulis(int64_t seed, uint64_t event, int64_t shot_base, int64_t batch, const float *p, int count,
+                        int32_t *out) {
+    uint64_t thr[15];
     double cum = 0.0;
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < count; ++k) {
         cum += (double)p[k];
         thr[k] = ora_threshold(cum);
     }
+    const uint64_t s64 = surv64(thr[count - 1]);
+    int32_t idx[64];
+    int64_t cur = -1;
+    for (int64_t b = 0; b < batch; ++b) {
+        const int64_t g = shot_base + b;
+        if ((g >> 6) != cur) {
+            cur = g >> 6;
+            channel_word(seed, event, (uint64_t)cur, thr, count, s64, idx);
+        }
+        out[b] = idx[g & 63];
+    }
+}
+
+void ora_pauli_channel_1(ora_state *s, int64_t q, const float p[3]) {
     const uint64_t event = s->events++;
+    int32_t *k = (int32_t *)calloc((size_t)s->batch + 1, sizeof(int32_t));
     int32_t *fx = (int32_t *)calloc((size_t)s->batch + 1, sizeof(int32_t));
     int32_t *fz = (int32_t *)calloc((size_t)s->batch + 1, sizeof(int32_t));
+    ora_channel_paulis(s->seed, event, s->shot_base, s->batch, p, 3, k);
     for (int64_t b = 0; b < s->batch; ++b) {
-        int k = pick_index(ora_draw_u32(s->seed, event, s->shot_base + b, TAG_NOISE), thr, 3);
-        fx[b] = (k == 1 || k == 2);
-        fz[b] = (k == 2 || k == 3);
+        fx[b] = (k[b] == 1 || k[b] == 2);
+        fz[b] = (k[b] == 2 || k[b] == 3);
     }
     apply_flag_paulis(s, q, fx, fz);
+    free(k);
     free(fx);
     free(fz);
 }
 
 void ora_pauli_channel_2(ora_state *s, int64_t a, int64_t bq, const float p[15]) {
-    uint64_t thr[15];
-    double cum = 0.0;
-    for (int k = 0; k < 15; ++k) {
-        cum += (double)p[k];
-        thr[k] = ora_threshold(cum);
-    }
     const uint64_t event = s->events++;
     size_t sz = (size_t)s->batch + 1;
+    int32_t *k = (int32_t *)calloc(sz, 4);
     int32_t *fxa = (int32_t *)calloc(sz, 4), *fza = (int32_t *)calloc(sz, 4);
     int32_t *fxb = (int32_t *)calloc(sz, 4), *fzb = (int32_t *)calloc(sz, 4);
+    ora_channel_paulis(s->seed, event, s->shot_base, s->batch, p, 15, k);
     for (int64_t b = 0; b < s->batch; ++b) {
-        int k = pick_index(ora_draw_u32(s->seed, event, s->shot_base + b, TAG_NOISE), thr, 15);
-        int pa = k >> 2, pb = k & 3;
+        int pa = k[b] >> 2, pb = k[b] & 3;
         fxa[b] = (pa == 1 || pa == 2);
         fza[b] = (pa == 2 || pa == 3);
         fxb[b] = (pb == 1 || pb == 2);
@@ -498,6 +563,7 @@ void ora_pauli_channel_2(ora_state *s, int64_t a, int64_t bq, const float p[15])
     }
     apply_flag_paulis(s, a, fxa, fza);
     apply_flag_paulis(s, bq, fxb, fzb);
+    free(k);
     free(fxa);
     free(fza);
     free(fxb);

@@ -112,6 +112,11 @@ int ora_run(ora_state *s, const ora_op *ops, int64_t nops, const float *params,
 
 /* Threshold used for Pauli-channel sampling: u32 < T means "inside". */
 uint64_t ora_threshold(double cumulative);
+/* The Pauli a channel event puts on shots [shot_base, shot_base + batch):
+ * out[b] = 0 (identity) or the index into p plus 1, drawn word by word by
+ * the gap sampling described in ps_oracle.c. */
+void ora_channel_paulis(int64_t seed, uint64_t event, int64_t shot_base, int64_t batch, const float *p, int count,
+                        int32_t *out);
 /* One 32-bit Philox draw for (seed, event, global shot, tag); tag 1 =
  * measurement outcome, 2 = Pauli channel. */
 uint32_t ora_draw_u32(int64_t seed, uint64_t event, int64_t gshot, uint32_t tag);

@@ -49,14 +49,6 @@ void cond_paulis(RefHandle *h, size_t q, const std::vector<int> &fx, const std::
     h->st->ApplyPhaseGateWithApplyFlag(q, vz);
 }
 
-int pick(std::uint32_t u, const float *p, int count) {
-    double cum = 0.0;
-    for (int k = 0; k < count; ++k) {
-        cum += static_cast<double>(p[k]);
-        if (static_cast<std::uint64_t>(u) < ora_threshold(cum)) return k + 1;
-    }
-    return 0;
-}
 } // namespace
 
 extern "C" {
@@ -182,9 +174,9 @@ std::int32_t ref_pauli_product_phase(std::int32_t x1, std::int32_t z1, std::int3
     return Plaquette::PauliProductPhase<int>(x1, z1, x2, z2);
 }
 
-// Circuit replay with the same op encoding as ora_run.  Pauli channels draw
-// the same Philox numbers as the oracle and apply them through the
-// reference's own flag gates.
+// Circuit replay with the same op encoding as ora_run.  Pauli channels take
+// the oracle's outcomes (ora_channel_paulis: the reference has no channel op)
+// and apply them through the reference's own flag gates.
 int ref_run(void *p, const std::int32_t *ops, std::int64_t nops, const float *params, const std::uint8_t *forced_all) {
     auto *h = static_cast<RefHandle *>(p);
     const size_t B = h->st->GetBatchSize();
@@ -212,8 +204,10 @@ int ref_run(void *p, const std::int32_t *ops, std::int64_t nops, const float *pa
         case ORA_OP_PAULI1: {
             const std::uint64_t ev = h->events++;
             std::vector<int> fx(B), fz(B);
+            std::vector<std::int32_t> pk(B + 1);
+            ora_channel_paulis(h->seed, ev, h->shot_base, (std::int64_t)B, params + c, 3, pk.data());
             for (size_t s = 0; s < B; ++s) {
-                int kk = pick(ora_draw_u32(h->seed, ev, h->shot_base + s, 2), params + c, 3);
+                int kk = pk[s];
                 fx[s] = (kk == 1 || kk == 2);
                 fz[s] = (kk == 2 || kk == 3);
             }
@@ -223,8 +217,10 @@ int ref_run(void *p, const std::int32_t *ops, std::int64_t nops, const float *pa
         case ORA_OP_PAULI2: {
             const std::uint64_t ev = h->events++;
             std::vector<int> fxa(B), fza(B), fxb(B), fzb(B);
+            std::vector<std::int32_t> pk(B + 1);
+            ora_channel_paulis(h->seed, ev, h->shot_base, (std::int64_t)B, params + c, 15, pk.data());
             for (size_t s = 0; s < B; ++s) {
-                int kk = pick(ora_draw_u32(h->seed, ev, h->shot_base + s, 2), params + c, 15);
+                int kk = pk[s];
                 int pa = kk >> 2, pb = kk & 3;
                 fxa[s] = (pa == 1 || pa == 2);
                 fza[s] = (pa == 2 || pa == 3);

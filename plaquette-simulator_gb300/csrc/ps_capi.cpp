@@ -426,7 +426,7 @@ ps_status ps_pauli_channel_1(ps_state *h, uint64_t q, const float p[3]) {
     CHECK_HANDLE(h);
     CHECK_QUBIT(h, q);
     if (!p) return fail(E_ARG, "null probabilities");
-    uint64_t thr[3];
+    uint64_t thr[4];
     channel_thresholds(p, 3, thr);
     return launch_pauli_channel(h, (int64_t)q, 0, thr, 3);
 }
@@ -436,7 +436,7 @@ ps_status ps_pauli_channel_1_noalloc(ps_state *h, uint64_t q, const float p[3]) 
     CHECK_HANDLE(h);
     CHECK_QUBIT(h, q);
     if (!p) return fail(E_ARG, "null probabilities");
-    uint64_t thr[3];
+    uint64_t thr[4];
     channel_thresholds(p, 3, thr);
     return launch_pauli_channel_noalloc(h, (int64_t)q, thr);
 }
@@ -448,7 +448,7 @@ ps_status ps_pauli_channel_2(ps_state *h, uint64_t a, uint64_t b, const float p[
     CHECK_QUBIT(h, b);
     if (a == b) return fail(E_ARG, "two-qubit channel needs distinct qubits");
     if (!p) return fail(E_ARG, "null probabilities");
-    uint64_t thr[15];
+    uint64_t thr[16];
     channel_thresholds(p, 15, thr);
     return launch_pauli_channel(h, (int64_t)a, (int64_t)b, thr, 15);
 }

@@ -815,10 +815,11 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
     const size_t nb = c->fent.size();
     const std::vector<NoiseEntry *> &ebuf = c->fent;
     const std::vector<int32_t *> &cbuf = c->fcnt;
-    // The x / z broadcast rides on the sampling launches (their Philox
-    // arithmetic leaves HBM idle): sampling launch j writes (row, qubit)
-    // pairs [j*P/S, (j+1)*P/S) of the P = W*n; without sampling launches it
-    // is a kernel of its own on the side stream.
+    // The x / z broadcast rides on the sampling launches: sampling launch j
+    // writes (row, qubit) pairs [j*P/S, (j+1)*P/S) of the P = W*n.  (As a
+    // kernel of its own beside the run it was slower, at every grid size and
+    // priority tried.)  Without sampling launches it is a kernel of its own
+    // on the side stream.
     XZBroadcast bc;
     bc.X = h->X;
     bc.Z = h->Z;
@@ -839,7 +840,7 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
             XZBroadcast all = bc;
             all.rq0 = 0;
             all.rq1 = P;
-            rc = launch_broadcast_xz(sb, all);
+            rc = launch_broadcast_xz(sb, all, true);
             if (rc != OK) return rc;
         }
     }
@@ -892,7 +893,7 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
         XZBroadcast all = bc;
         all.rq0 = 0;
         all.rq1 = P;
-        return timed(P_BROADCAST, [&] { return launch_broadcast_xz(st, all); });
+        return timed(P_BROADCAST, [&] { return launch_broadcast_xz(st, all, false); });
     }
     cudaEvent_t es, eb;
     if (record(ss, &es) != OK || record(sb, &eb) != OK) return E_ARG;
@@ -1148,10 +1149,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             const int cnt = o.code == OP_PAULI2 ? 15 : 3;
             if (o.c < 0 || (uint64_t)o.c + cnt > nparams)
                 return bail(fail(E_ARG, "op " + std::to_string(i) + ": channel parameters out of range"));
-            uint64_t t[15];
+            uint64_t t[16];
             channel_thresholds(params + o.c, cnt, t);
             thr_off[i] = (int32_t)thr.size();
-            thr.insert(thr.end(), t, t + cnt);
+            thr.insert(thr.end(), t, t + cnt + 1);
         }
         if (is_meas(o.code)) rec_of[i] = nrec++;
         if (is_meas(o.code) || is_channel(o.code)) event_of[i] = ev++;
@@ -1437,10 +1438,15 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         }
     }
     st.launches_per_run += 1;  // run-parameter update
-    if (c->frame_ok) {  // runs from |0...0>: sampling (2), sign kernel per range, broadcast, parameters
+    if (c->frame_ok) {  // runs from |0...0>: per range its sampling kernel (if any) and sign kernel, the parameters
         st.shared_xz = 1;
-        st.launches_per_run = 2;
-        for (const FrameProgram::Launch &L : c->fprog.launches) st.launches_per_run += L.seg >= 0 ? 3 : 1;
+        st.launches_per_run = 1;
+        bool sampled = false;
+        for (const FrameProgram::Launch &L : c->fprog.launches) {
+            st.launches_per_run += L.seg >= 0 ? 2 : 1;
+            sampled |= L.seg >= 0;
+        }
+        if (!sampled) st.launches_per_run += 1;  // the broadcast, on the sampling launches otherwise
     }
     st.seg_rows = c->opts.seg_rows;
     st.seg_words = c->opts.seg_words;

@@ -64,8 +64,9 @@ PS_HD u32x4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, ui
 
 enum : uint32_t { TAG_MEASURE = 1, TAG_NOISE = 2 };
 
-// Draws for the 64 shots of global word `word`: block `sub` (0..15) covers
-// shots 4*sub .. 4*sub+3 of the word.
+// Philox block `sub` of global word `word` for event `event`.  A random
+// measurement's draws: block sub (0..15) covers shots 4*sub .. 4*sub+3 of
+// the word; a Pauli channel's: see channel_word.
 PS_HD u32x4 draw_block(uint64_t seed, uint64_t event, uint64_t word, uint32_t sub, uint32_t tag) {
     return philox4x32_10(sub, (uint32_t)word, (uint32_t)event, tag, (uint32_t)(seed & 0xffffffffu),
                          (uint32_t)(seed >> 32));
@@ -73,6 +74,76 @@ PS_HD u32x4 draw_block(uint64_t seed, uint64_t event, uint64_t word, uint32_t su
 
 // 24-bit uniform in [0,1), exact in binary32.
 PS_HD float unit_float(uint32_t u) { return (float)(u >> 8) * (1.0f / 16777216.0f); }
+
+// ------------------------------------------------------ Pauli channels
+// A channel's table: thr[0..count) cumulative thresholds of its Paulis
+// (Pauli k+1 takes draws in [thr[k-1], thr[k]) of [0, 2^32), count 3 for
+// X, Y, Z on one qubit, 15 for IX .. ZZ on two), total = thr[count-1] the
+// probability p = total / 2^32 that a shot is hit, and thr[count] =
+// channel_surv64(total).
+//
+// A shot is hit with probability p, independently of the others, and a hit
+// shot takes Pauli k+1 with probability (thr[k] - thr[k-1]) / total.  The
+// 64 shots of a word are sampled by their gaps: the survival products
+// S_0 = 2^32, S_{j+1} = floor(S_j (2^32 - total) / 2^32) (the chance that j
+// shots in a row are missed, in 32-bit fixed point: integer arithmetic, so
+// every platform computes the same bits); a draw u puts the next hit g
+// shots on, g the first with u >= S_{g+1}, and one more draw v picks the
+// hit's Pauli as the first k with floor(v total / 2^32) < thr[k].  Draw i of
+// a word is lane i%4 of Philox block i/4 keyed by (seed, event, word,
+// TAG_NOISE).  A word with no hit -- u < S_64 -- costs one block.
+PS_HD uint64_t channel_surv64(uint64_t total) {
+    if (total == 0) return 1ull << 32;
+    const uint64_t q = (1ull << 32) - total;  // < 2^32, so S * q < 2^64
+    uint64_t s = 1ull << 32;
+    for (int j = 0; j < 64; ++j) s = (s * q) >> 32;
+    return s;
+}
+
+// Lane j of a block, without indexing the block by a variable (which would
+// put it in local memory).
+PS_HD uint32_t block_lane(const u32x4 &b, uint32_t j) {
+    return j == 0u ? b.v[0] : j == 1u ? b.v[1] : j == 2u ? b.v[2] : b.v[3];
+}
+
+struct ChannelWord {
+    u64 fxa, fza, fxb, fzb;  // shots with X or Y / Y or Z on qubit a, and on qubit b
+};
+
+PS_HD ChannelWord channel_word(uint64_t seed, uint64_t event, uint64_t word, const uint64_t *thr, int count) {
+    ChannelWord m{0ull, 0ull, 0ull, 0ull};
+    const uint64_t total = thr[count - 1];
+    if (total == 0) return m;
+    u32x4 blk = draw_block(seed, event, word, 0u, TAG_NOISE);
+    uint32_t u = blk.v[0];
+    if ((uint64_t)u < thr[count]) return m;  // no shot of the word is hit
+    const uint64_t q = (1ull << 32) - total;
+    uint32_t i = 1;  // the next draw
+    int pos = 0;     // the first shot not sampled yet
+    for (;;) {
+        uint64_t s = 1ull << 32;
+        for (;;) {  // the gap to the next hit
+            s = (s * q) >> 32;
+            if ((uint64_t)u >= s) break;
+            if (++pos == 64) return m;
+        }
+        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
+        const uint64_t v = ((uint64_t)block_lane(blk, i & 3u) * total) >> 32;
+        ++i;
+        int idx = 1;
+        while (v >= thr[idx - 1]) ++idx;
+        const u64 bit = 1ull << pos;
+        const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
+        if (pa == 1 || pa == 2) m.fxa |= bit;
+        if (pa == 2 || pa == 3) m.fza |= bit;
+        if (pb == 1 || pb == 2) m.fxb |= bit;
+        if (pb == 2 || pb == 3) m.fzb |= bit;
+        if (++pos == 64) return m;
+        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
+        u = block_lane(blk, i & 3u);
+        ++i;
+    }
+}
 
 // ----------------------------------------------------------- sign math
 // Bit-sliced mod-4 accumulation of the reference's PauliProductPhase

@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(256) broadcast_xz_kernel(XZBroadcast bc) {
 
 int g_frame_sms = 0;
 int g_prio_greatest = 1;  // 1: not looked up yet (priorities are <= 0)
+int g_prio_least = 1;
 
 }  // namespace
 
@@ -275,15 +276,34 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
     return OK;
 }
 
-int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc) {
+int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc, bool yield) {
     if (bc.rq1 <= bc.rq0) return OK;
     if (g_frame_sms == 0) {
         int dev = 0;
         PS_CUDA(cudaGetDevice(&dev));
         PS_CUDA(cudaDeviceGetAttribute(&g_frame_sms, cudaDevAttrMultiProcessorCount, dev));
     }
-    const int64_t blocks = std::min<int64_t>((bc.rq1 - bc.rq0 + 7) / 8, (int64_t)g_frame_sms * 8);
-    broadcast_xz_kernel<<<(unsigned)blocks, 256, 0, st>>>(bc);
+    if (g_prio_least == 1) {
+        int least = 0, greatest = 0;
+        PS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        g_prio_least = least;
+    }
+    // yield: one (row, qubit) pair per warp, so that CTAs retire within
+    // microseconds and the kernels beside it (the sign program, launched at
+    // the highest priority) get every SM slot that frees up; otherwise a
+    // grid of 8 CTAs per SM walking the pairs.
+    const int64_t pairs = bc.rq1 - bc.rq0;
+    const int64_t blocks = yield ? (pairs + 7) / 8 : std::min<int64_t>((pairs + 7) / 8, (int64_t)g_frame_sms * 8);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = g_prio_least;
+    cfg.attrs = attr;
+    cfg.numAttrs = yield ? 1 : 0;
+    PS_CUDA(cudaLaunchKernelEx(&cfg, broadcast_xz_kernel, bc));
     PS_CUDA(cudaGetLastError());
     return OK;
 }

@@ -104,53 +104,23 @@ __global__ void __launch_bounds__(256) gate2_kernel(u64 *__restrict__ X, u64 *__
     st2(R + i * w + k, r.a, r.b);
 }
 
-// Pauli-channel sampling: one thread per (shot-word, qubit slot).  For each
-// shot one Philox draw u picks Pauli k = first index with u < thr[k]
-// (0 = identity).  Output masks: fx = shots with X or Y, fz = Y or Z, for
-// qubit a (slot 0) and b (slot 1).
-// 16 threads per 64-shot word: thread `sub` computes Philox block `sub`
-// (shots 4*sub .. 4*sub+3); the four masks are OR-reduced over the 16 lanes.
+// Pauli-channel sampling: one thread per shot-word draws the word's
+// outcomes (channel_word) and writes its masks: fx = shots with X or Y,
+// fz = Y or Z, for qubit a (masks[0..w), [w..2w)) and b ([2w..3w), [3w..4w)).
 __global__ void __launch_bounds__(256) channel_sample_kernel(u64 *__restrict__ masks, int64_t w, uint64_t seed_arg,
                                                             uint64_t event_arg, uint64_t word_base_arg,
                                                             const RunParams *__restrict__ rp,
                                                             int count, const uint64_t *__restrict__ thr) {
-    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t k = gt >> 4;
-    const uint32_t sub = (uint32_t)(gt & 15);
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= w) return;
     const uint64_t seed = rp ? rp->seed : seed_arg;
     const uint64_t event = (rp ? rp->event_base : 0ull) + event_arg;
     const uint64_t word_base = rp ? rp->word_base : word_base_arg;
-    u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
-    if (k < w) {
-        const uint64_t total = thr[count - 1];
-        const u32x4 u = draw_block(seed, event, word_base + (uint64_t)k, sub, TAG_NOISE);
-#pragma unroll
-        for (int l = 0; l < 4; ++l) {
-            const uint64_t v = u.v[l];
-            if (v >= total) continue;  // identity, the common case
-            int idx = 1;
-            while (v >= thr[idx - 1]) ++idx;
-            const u64 bit = 1ull << (sub * 4 + l);
-            const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
-            if (pa == 1 || pa == 2) fxa |= bit;
-            if (pa == 2 || pa == 3) fza |= bit;
-            if (pb == 1 || pb == 2) fxb |= bit;
-            if (pb == 2 || pb == 3) fzb |= bit;
-        }
-    }
-#pragma unroll
-    for (int off = 8; off > 0; off >>= 1) {
-        fxa |= __shfl_xor_sync(0xffffffffu, fxa, off);
-        fza |= __shfl_xor_sync(0xffffffffu, fza, off);
-        fxb |= __shfl_xor_sync(0xffffffffu, fxb, off);
-        fzb |= __shfl_xor_sync(0xffffffffu, fzb, off);
-    }
-    if (sub == 0 && k < w) {
-        masks[k] = fxa;
-        masks[w + k] = fza;
-        masks[2 * w + k] = fxb;
-        masks[3 * w + k] = fzb;
-    }
+    const ChannelWord m = channel_word(seed, event, word_base + (uint64_t)k, thr, count);
+    masks[k] = m.fxa;
+    masks[w + k] = m.fza;
+    masks[2 * w + k] = m.fxb;
+    masks[3 * w + k] = m.fzb;
 }
 
 // r ^= (fx & z_q) ^ (fz & x_q) over all rows: X flips rows with Z on q, Z
@@ -202,7 +172,7 @@ int launch_gate(ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag
 
 int launch_channel_rp(cudaStream_t st, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,
                       uint32_t event_off, const RunParams *rp, u64 *masks) {
-    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, st>>>(masks, h->w, (uint64_t)h->seed, event_off, (uint64_t)h->word_base, rp, count,
+    channel_sample_kernel<<<blocks_for(h->w), 256, 0, st>>>(masks, h->w, (uint64_t)h->seed, event_off, (uint64_t)h->word_base, rp, count,
                                                              dev_thr);
     PS_CUDA(cudaGetLastError());
     const int64_t work = h->W * (h->w >> 1);
@@ -227,14 +197,15 @@ void channel_thresholds(const float *p, int count, uint64_t *thr) {
         else
             thr[k] = (uint64_t)std::floor(cum * 4294967296.0);
     }
+    thr[count] = channel_surv64(thr[count - 1]);
 }
 
 int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thr, int count) {
     const uint64_t event = h->events++;
     uint64_t *dthr = nullptr;
-    PS_CUDA(cudaMallocAsync(&dthr, 15 * sizeof(uint64_t), h->stream));
-    PS_CUDA(cudaMemcpyAsync(dthr, thr, (size_t)count * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
-    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, h->stream>>>(h->mask_buf, h->w, (uint64_t)h->seed, event, (uint64_t)h->word_base,
+    PS_CUDA(cudaMallocAsync(&dthr, 16 * sizeof(uint64_t), h->stream));
+    PS_CUDA(cudaMemcpyAsync(dthr, thr, (size_t)(count + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+    channel_sample_kernel<<<blocks_for(h->w), 256, 0, h->stream>>>(h->mask_buf, h->w, (uint64_t)h->seed, event, (uint64_t)h->word_base,
                                                                     nullptr, count, dthr);
     PS_CUDA(cudaGetLastError());
     const int64_t work = h->W * (h->w >> 1);
@@ -278,10 +249,11 @@ constexpr int NOALLOC_THR = 16;  // threshold slots in front of the masks
 
 static __device__ __align__(256) u64 g_noalloc_scratch[NOALLOC_THR + 4 * NOALLOC_MAX_WORDS];
 
-__global__ void noalloc_set_thresholds(uint64_t *thr, uint64_t t0, uint64_t t1, uint64_t t2) {
+__global__ void noalloc_set_thresholds(uint64_t *thr, uint64_t t0, uint64_t t1, uint64_t t2, uint64_t s64) {
     thr[0] = t0;
     thr[1] = t1;
     thr[2] = t2;
+    thr[3] = s64;
 }
 
 // Device address of the array, looked up once per device on the first call
@@ -318,8 +290,8 @@ int launch_pauli_channel_noalloc(ps_state *h, int64_t q, const uint64_t *thr3) {
     u64 *masks = scratch + NOALLOC_THR;
     const uint64_t event = h->events++;
     // Thresholds travel as kernel arguments (no host copy, no allocation).
-    noalloc_set_thresholds<<<1, 1, 0, h->stream>>>(thr, thr3[0], thr3[1], thr3[2]);
-    channel_sample_kernel<<<blocks_for(16 * h->w), 256, 0, h->stream>>>(masks, h->w, (uint64_t)h->seed, event, (uint64_t)h->word_base,
+    noalloc_set_thresholds<<<1, 1, 0, h->stream>>>(thr, thr3[0], thr3[1], thr3[2], thr3[3]);
+    channel_sample_kernel<<<blocks_for(h->w), 256, 0, h->stream>>>(masks, h->w, (uint64_t)h->seed, event, (uint64_t)h->word_base,
                                                                         nullptr, 3, thr);
     PS_CUDA(cudaGetLastError());
     const int64_t work = h->W * (h->w >> 1);

@@ -132,7 +132,8 @@ int upload_forced(ps_state *h, const uint8_t *forced, const u64 **dev);
 // ps_gates.cu
 int launch_gate(ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag);
 int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thresholds, int count);
-// Sampling thresholds for a Pauli channel from float probabilities.
+// A Pauli channel's table (channel_word) from its float probabilities:
+// count + 1 entries.
 void channel_thresholds(const float *p, int count, uint64_t *thr);
 
 // ps_measure.cu
@@ -177,8 +178,9 @@ int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *o
                  uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
                  int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero,
                  int noise_first, uint32_t scratch);
-// X, Z of every shot := the shared bits, (row, qubit) pairs [bc.rq0, bc.rq1).
-int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc);
+// X, Z of every shot := the shared bits, (row, qubit) pairs [bc.rq0, bc.rq1);
+// yield: short CTAs at the lowest priority, for a launch beside other work.
+int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc, bool yield);
 
 // ps_gates.cu (compiled-circuit form of the per-op kernels)
 int launch_channel_rp(cudaStream_t stream, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,

@@ -22,50 +22,21 @@ namespace ps {
 
 namespace {
 
-// Pauli-channel sampling for one segment, pass 1: 16 threads per (word,
-// channel); thread `sub` draws Philox block `sub` (shots 4*sub..4*sub+3 of
-// the word) and the X/Z component masks are OR-reduced over the 16 lanes into
-// dense[word][slot].
+// Pauli-channel sampling for one segment, pass 1: one thread per (word,
+// channel) draws the word's outcomes (channel_word) into dense[word][slot].
 __global__ void __launch_bounds__(256) noise_dense_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp) {
-    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t pair = gt >> 4;
-    const uint32_t sub = (uint32_t)(gt & 15);
+    const int64_t pair = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t k = pair / seg.nslots;
     const int s = (int)(pair - k * seg.nslots);
-    u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
-    if (k < w) {
-        const NoiseSlot sl = seg.slots[s];
-        const uint64_t *thr = seg.thr + sl.thr_off;
-        const uint64_t total = thr[sl.count - 1];
-        const u32x4 u = draw_block(rp->seed, rp->event_base + sl.event, rp->word_base + (uint64_t)k, sub, TAG_NOISE);
-#pragma unroll
-        for (int l = 0; l < 4; ++l) {
-            const uint64_t v = u.v[l];
-            if (v >= total) continue;  // identity, the common case
-            int idx = 1;
-            while (v >= thr[idx - 1]) ++idx;
-            const u64 bit = 1ull << (sub * 4 + l);
-            const int pa = sl.count == 3 ? idx : (idx >> 2), pb = sl.count == 3 ? 0 : (idx & 3);
-            if (pa == 1 || pa == 2) fxa |= bit;
-            if (pa == 2 || pa == 3) fza |= bit;
-            if (pb == 1 || pb == 2) fxb |= bit;
-            if (pb == 2 || pb == 3) fzb |= bit;
-        }
-    }
-#pragma unroll
-    for (int off = 8; off > 0; off >>= 1) {
-        fxa |= __shfl_xor_sync(0xffffffffu, fxa, off);
-        fza |= __shfl_xor_sync(0xffffffffu, fza, off);
-        fxb |= __shfl_xor_sync(0xffffffffu, fxb, off);
-        fzb |= __shfl_xor_sync(0xffffffffu, fzb, off);
-    }
-    if (sub == 0 && k < w) {
-        u64 *d = seg.dense + pair * 4;
-        d[0] = fxa;
-        d[1] = fza;
-        d[2] = fxb;
-        d[3] = fzb;
-    }
+    if (k >= w) return;
+    const NoiseSlot sl = seg.slots[s];
+    const ChannelWord m = channel_word(rp->seed, rp->event_base + sl.event, rp->word_base + (uint64_t)k,
+                                       seg.thr + sl.thr_off, sl.count);
+    u64 *d = seg.dense + pair * 4;
+    d[0] = m.fxa;
+    d[1] = m.fza;
+    d[2] = m.fxb;
+    d[3] = m.fzb;
 }
 
 // Pass 2: one warp per word appends the non-identity outcomes to the word's
@@ -109,82 +80,47 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
 }
 
 // Channel sampling for shared-x/z runs, in one pass: one thread per
-// (channel slot, word) draws the word's 16 Philox blocks (the same draws,
-// keyed by (seed, event, global word, block), as the two-pass sampler) and
-// appends a non-identity outcome to the word's list with an atomic counter.
-// The list is unordered -- outcomes are XORs -- and carries, instead of the
-// slot, the slot's rows in the sign program (slot_off[base + s] ..
-// [base + s + 1]) cut into chunks of at most kFrameChunk: one entry per
-// chunk, layer = its first row entry, a = its row count, so no consumer
-// walks a long list alone.  The counter is zeroed by the sign kernel that
-// consumes the list.
+// (channel slot, word) draws the word's outcomes (channel_word, the same
+// draws as the two-pass sampler) and appends a non-identity outcome to the
+// word's list with an atomic counter.  The list is unordered -- outcomes are
+// XORs -- and carries, instead of the slot, the slot's rows in the sign
+// program (slot_off[base + s] .. [base + s + 1]) cut into chunks of at most
+// kFrameChunk: one entry per chunk, layer = its first row entry, a = its row
+// count, so no consumer walks a long list alone.  The counter is zeroed by
+// the sign kernel that consumes the list.  Every warp then writes its share
+// of the x / z broadcast (one (row, qubit) pair at a time, all lanes).
 __global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp,
                                                           const uint32_t *__restrict__ slot_off, uint32_t base,
                                                           XZBroadcast bc) {
-    // A share of the x / z broadcast, interleaved with the Philox arithmetic
-    // (a (row, qubit) pair after every other pair of blocks, the rest at the
-    // end) so that its stores drain to HBM while the ALUs stay busy.  Every
-    // thread stays to the end: the broadcast is written by whole warps.
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    int64_t rq = bc.X ? bc.rq0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) : bc.rq1;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int s = (int)(t / w);
     const int64_t k = t - (int64_t)s * w;
-    const bool active = s < seg.nslots;
-    NoiseSlot sl{};
-    const uint64_t *thr = seg.thr;
-    uint64_t total = 0;  // no draw is below 0: an inactive thread samples nothing
-    if (active) {
-        sl = seg.slots[s];
-        thr = seg.thr + sl.thr_off;
-        total = thr[sl.count - 1];
-    }
-    const uint64_t ev = rp->event_base + sl.event, word = rp->word_base + (uint64_t)k, seed = rp->seed;
-    u64 fxa = 0, fza = 0, fxb = 0, fzb = 0;
-    for (uint32_t sub0 = 0; sub0 < 16; sub0 += 2) {
-        if ((sub0 & 2) && rq < bc.rq1) {
-            broadcast_row_column(bc, rq, lane);
-            rq += warps;
-        }
-        if (!active) continue;
-        // two independent Philox chains in flight per thread
-        const u32x4 uu[2] = {draw_block(seed, ev, word, sub0, TAG_NOISE), draw_block(seed, ev, word, sub0 + 1, TAG_NOISE)};
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const uint32_t sub = sub0 + q;
-#pragma unroll
-            for (int l = 0; l < 4; ++l) {
-                const uint64_t v = uu[q].v[l];
-                if (v >= total) continue;  // identity, the common case
-                int idx = 1;
-                while (v >= thr[idx - 1]) ++idx;
-                const u64 bit = 1ull << (sub * 4 + l);
-                const int pa = sl.count == 3 ? idx : (idx >> 2), pb = sl.count == 3 ? 0 : (idx & 3);
-                if (pa == 1 || pa == 2) fxa |= bit;
-                if (pa == 2 || pa == 3) fza |= bit;
-                if (pb == 1 || pb == 2) fxb |= bit;
-                if (pb == 2 || pb == 3) fzb |= bit;
+    if (s < seg.nslots) {
+        const NoiseSlot sl = seg.slots[s];
+        const ChannelWord m = channel_word(rp->seed, rp->event_base + sl.event, rp->word_base + (uint64_t)k,
+                                           seg.thr + sl.thr_off, sl.count);
+        const uint32_t t0 = slot_off[base + s], t1 = slot_off[base + s + 1];
+        const int nch = (int)((t1 - t0 + kFrameChunk - 1) / kFrameChunk);
+        if ((m.fxa | m.fza | m.fxb | m.fzb) != 0ull && nch > 0) {
+            int pos = atomicAdd(&seg.entry_count[k], nch);
+            NoiseEntry e;
+            e.fxa = m.fxa;
+            e.fza = m.fza;
+            e.fxb = m.fxb;
+            e.fzb = m.fzb;
+            e.b = 0;
+            for (uint32_t c0 = t0; c0 < t1; c0 += kFrameChunk, ++pos) {
+                e.layer = (int32_t)c0;
+                e.a = (uint16_t)min((uint32_t)kFrameChunk, t1 - c0);
+                seg.entries[k * (int64_t)seg.cap + pos] = e;
             }
         }
     }
-    for (; rq < bc.rq1; rq += warps) broadcast_row_column(bc, rq, lane);
-    if ((fxa | fza | fxb | fzb) == 0ull) return;
-    const uint32_t t0 = slot_off[base + s], t1 = slot_off[base + s + 1];
-    const int nch = (int)((t1 - t0 + kFrameChunk - 1) / kFrameChunk);
-    if (nch == 0) return;
-    int pos = atomicAdd(&seg.entry_count[k], nch);
-    NoiseEntry e;
-    e.fxa = fxa;
-    e.fza = fza;
-    e.fxb = fxb;
-    e.fzb = fzb;
-    e.b = 0;
-    for (uint32_t c0 = t0; c0 < t1; c0 += kFrameChunk, ++pos) {
-        e.layer = (int32_t)c0;
-        e.a = (uint16_t)min((uint32_t)kFrameChunk, t1 - c0);
-        seg.entries[k * (int64_t)seg.cap + pos] = e;
-    }
+    if (!bc.X) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t rq = bc.rq0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rq < bc.rq1; rq += warps)
+        broadcast_row_column(bc, rq, lane);
 }
 
 // Tile cell: x and z of one (row, word, column) side by side, so a gate
@@ -817,7 +753,7 @@ size_t segment_launch_smem(int nlayers, int nruns, int ngates, int nsigns, int n
 
 int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp, int slot_tags) {
     if (seg.nslots == 0) return OK;
-    const int64_t threads = 16 * (int64_t)seg.nslots * w;
+    const int64_t threads = (int64_t)seg.nslots * w;
     noise_dense_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(seg, w, rp);
     PS_CUDA(cudaGetLastError());
     const int wpb = 4;

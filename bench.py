@@ -428,8 +428,9 @@ def main():
         roofline["note"] = ("latency-bound: one CTA per shot-word runs the sign program's ops in order on "
                             "signs held in shared memory; it moves little HBM data by design")
     elif dom == "channel_sample":
-        roofline["note"] = ("the sampling launches carry the Philox work (16 blocks per channel and shot-word, "
-                            "integer-bound) and write the x/z broadcast under it; achieved counts the broadcast only")
+        roofline["note"] = ("the sampling launches draw the channel outcomes (one Philox block per channel and "
+                            "shot-word without hits) and write the x/z broadcast; achieved counts the broadcast only, "
+                            "over event times that include each launch's submit gap (a lower bound)")
 
     line = {
         "metric": METRIC, "value": value, "unit": "shot-gates/s", "n_gpus": world, "steps": args.steps,

@@ -441,7 +441,7 @@ def main():
                                f"Z-basis, fused + CUDA graph" + (", shared x/z" if shared else ""),
                    "num_qubits": circ.num_qubits, "shots": shots, "gates_per_shot": gates,
                    "tableau_bytes": 3 * (2 * circ.num_qubits + 1) * circ.num_qubits * ((shots + 63) // 64) * 8,
-                   "l2": "no flush needed: the 1.65 GB tableau is larger than the 129 MB L2",
+                   "l2": "no flush needed: the 2.48 GB tableau (1.65 GB of it the x/z rewritten every step) is larger than the 129 MB L2",
                    "parallelism": f"shots split over {world} GPU(s), {shots} per GPU"},
         # the per-shot plan's reset adds init_zero_kernel; shared-x/z runs start from zero signs in the sign kernel
         "gpu_launches": int(fused.stats["launches_per_run"]) + (0 if shared else 1),

@@ -92,11 +92,21 @@ PS_HD float unit_float(uint32_t u) { return (float)(u >> 8) * (1.0f / 16777216.0
 // hit's Pauli as the first k with floor(v total / 2^32) < thr[k].  Draw i of
 // a word is lane i%4 of Philox block i/4 keyed by (seed, event, word,
 // TAG_NOISE).  A word with no hit -- u < S_64 -- costs one block.
+// floor(a b / 2^32) for a, b < 2^32: the survival step S_{j+1} from S_j,
+// exact for j >= 1 (S_1 = 2^32 - total < 2^32).
+PS_HD uint32_t mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
 PS_HD uint64_t channel_surv64(uint64_t total) {
     if (total == 0) return 1ull << 32;
-    const uint64_t q = (1ull << 32) - total;  // < 2^32, so S * q < 2^64
-    uint64_t s = 1ull << 32;
-    for (int j = 0; j < 64; ++j) s = (s * q) >> 32;
+    const uint32_t q = (uint32_t)((1ull << 32) - total);
+    uint32_t s = q;  // S_1
+    for (int j = 1; j < 64; ++j) s = mulhi32(s, q);
     return s;
 }
 
@@ -117,15 +127,15 @@ PS_HD ChannelWord channel_word(uint64_t seed, uint64_t event, uint64_t word, con
     u32x4 blk = draw_block(seed, event, word, 0u, TAG_NOISE);
     uint32_t u = blk.v[0];
     if ((uint64_t)u < thr[count]) return m;  // no shot of the word is hit
-    const uint64_t q = (1ull << 32) - total;
+    const uint32_t q = (uint32_t)((1ull << 32) - total);
     uint32_t i = 1;  // the next draw
     int pos = 0;     // the first shot not sampled yet
     for (;;) {
-        uint64_t s = 1ull << 32;
-        for (;;) {  // the gap to the next hit
-            s = (s * q) >> 32;
-            if ((uint64_t)u >= s) break;
+        uint32_t s = q;  // S_1
+        for (;;) {       // the gap to the next hit
+            if (u >= s) break;
             if (++pos == 64) return m;
+            s = mulhi32(s, q);
         }
         if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
         const uint64_t v = ((uint64_t)block_lane(blk, i & 3u) * total) >> 32;

@@ -14,10 +14,11 @@ namespace {
 
 // One CTA of FW warps per shot-word: its W signs live in shared memory while
 // it runs ops [op0, op1) in order.  Channel outcomes go one per thread over
-// all warps (XORs commute; shared atomics where two outcomes flip one row);
-// the measurement ops run on warp 0 -- a window's measurements one per
-// lane, the rows of other ops over the lanes -- with block barriers around
-// every channel op.  When
+// all warps (XORs commute; shared atomics where two outcomes flip one row),
+// and so do the outputs of an F_LINEAR op; the other measurement ops (those
+// the builder left out of its linear maps) run on warp 0 -- a window's
+// measurements one per lane, the rows of other ops over the lanes -- with
+// block barriers around every all-warp op.  When
 // `stage` is set the launch's ops and the tab range [tab0, tab0 + ntab) of
 // its measurement ops are first copied to shared memory, so the op stream
 // runs on shared-memory latency; channel rows stay in global memory (a word

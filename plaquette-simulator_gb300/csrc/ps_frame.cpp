@@ -26,6 +26,17 @@ FrameBuilder::FrameBuilder(int64_t n) : n_(n), W_(2 * n + 1), nw_((n + 63) / 64)
 
 void FrameBuilder::to_col() {
     if (col_) return;
+    if (colok_) {  // the copy is exact but for the scratch row
+        const int64_t s = 2 * n_;
+        const uint64_t m = 1ull << (s & 63);
+        for (int64_t q = 0; q < n_; ++q) {
+            uint64_t &xw = xc_[(size_t)(q * ww_ + (s >> 6))], &zw = zc_[(size_t)(q * ww_ + (s >> 6))];
+            xw = bit(x_, s, q) ? (xw | m) : (xw & ~m);
+            zw = bit(z_, s, q) ? (zw | m) : (zw & ~m);
+        }
+        col_ = true;
+        return;
+    }
     xc_.assign((size_t)(n_ * ww_), 0ull);
     zc_.assign((size_t)(n_ * ww_), 0ull);
     for (int64_t i = 0; i < W_; ++i)
@@ -36,6 +47,7 @@ void FrameBuilder::to_col() {
                 zc_[(size_t)((64 * t + __builtin_ctzll(v)) * ww_ + (i >> 6))] |= 1ull << (i & 63);
         }
     col_ = true;
+    colok_ = true;
 }
 
 void FrameBuilder::to_row() {
@@ -50,7 +62,37 @@ void FrameBuilder::to_row() {
                 z_[(size_t)((64 * t + __builtin_ctzll(v)) * nw_ + (q >> 6))] |= 1ull << (q & 63);
         }
     col_ = false;
+    colok_ = true;
 }
+
+namespace {
+// Rows [lo, hi) of a column-major bit column: the first set one (hi if
+// none), and each set one in increasing order.
+int64_t first_set(const uint64_t *col, int64_t lo, int64_t hi) {
+    for (int64_t t = lo >> 6; (t << 6) < hi; ++t) {
+        uint64_t v = col[t];
+        if ((t << 6) < lo) v &= ~0ull << (lo & 63);
+        if (v) {
+            const int64_t i = (t << 6) + __builtin_ctzll(v);
+            return i < hi ? i : hi;
+        }
+    }
+    return hi;
+}
+
+template <class F>
+void each_set(const uint64_t *col, int64_t lo, int64_t hi, F &&f) {
+    for (int64_t t = lo >> 6; (t << 6) < hi; ++t) {
+        uint64_t v = col[t];
+        if ((t << 6) < lo) v &= ~0ull << (lo & 63);
+        for (; v; v &= v - 1) {
+            const int64_t i = (t << 6) + __builtin_ctzll(v);
+            if (i >= hi) return;
+            f(i);
+        }
+    }
+}
+}  // namespace
 
 void FrameBuilder::push_op(const FrameOp &op) {
     prog.ops.push_back(op);
@@ -90,6 +132,7 @@ void FrameBuilder::open_range() {
 void FrameBuilder::gate(int32_t code, int64_t a, int64_t b) {
     if (!seg_col_) {  // a short segment: row by row on the row-major bits
         to_row();
+        colok_ = false;
         for (int64_t i = 0; i < W_; ++i) {
             const int xa = bit(x_, i, a), za = bit(z_, i, a);
             int fl = 0;
@@ -253,11 +296,28 @@ void FrameBuilder::row_xor(int64_t dst, int64_t src) {
 // reset then flips the rows with z(., q) = 1 where the outcome is 1.
 void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
     to_row();
-    int64_t p = 0;
-    while (p < n_ && !bit(x_, p + n_, q)) ++p;
     const int64_t s = 2 * n_;
+    // Column q of rows [0, 2n) from the column-major copy while it is exact
+    // (from the last transpose on, only the scratch row has changed).
+    const uint64_t *xq = colok_ ? &xc_[(size_t)(q * ww_)] : nullptr;
+    const uint64_t *zq = colok_ ? &zc_[(size_t)(q * ww_)] : nullptr;
+    int64_t p = 0;
+    if (xq)
+        p = first_set(xq, n_, 2 * n_) - n_;
+    else
+        while (p < n_ && !bit(x_, p + n_, q)) ++p;
     if (p < n_) {  // MeasureRandom (:225-265), in program order after the open window
         flush_window();
+        std::vector<int64_t> mult;  // rows i < 2n, i != p, p+n, with x(i,q) = 1: rows i themselves are not changed before their turn
+        if (xq) {
+            each_set(xq, 0, 2 * n_, [&](int64_t i) {
+                if (i != p && i != p + n_) mult.push_back(i);
+            });
+        } else {
+            for (int64_t i = 0; i < 2 * n_; ++i)
+                if (i != p && i != p + n_ && bit(x_, i, q)) mult.push_back(i);
+        }
+        colok_ = false;
         FrameOp op{};
         op.kind = F_MEAS_RAND | prog.launches.back().nrand << 8;
         op.arg = meas_index;
@@ -274,12 +334,11 @@ void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
         flip(z_, p + n_, q);
         fset(p, fget(p + n_));
         fset(p + n_, false);
-        for (int64_t i = 0; i < 2 * n_; ++i)
-            if (i != p && i != p + n_ && bit(x_, i, q)) {
-                const uint32_t c = (uint32_t)(phase_bit(i, p) ^ (int)fget(p));
-                prog.tab.push_back((uint32_t)i | c << 31);
-                row_xor(i, p);
-            }
+        for (int64_t i : mult) {
+            const uint32_t c = (uint32_t)(phase_bit(i, p) ^ (int)fget(p));
+            prog.tab.push_back((uint32_t)i | c << 31);
+            row_xor(i, p);
+        }
         op.len = (uint32_t)prog.tab.size() - op.off;
         push_op(op);
         if (reset) {
@@ -301,17 +360,28 @@ void FrameBuilder::measure(int64_t q, int32_t meas_index, bool reset) {
         z_[(size_t)(s * nw_ + t)] = 0ull;
     }
     uint32_t c = 0;
-    for (int64_t i = 0; i < n_; ++i)
-        if (bit(x_, i, q)) {
-            c ^= (uint32_t)(phase_bit(s, i + n_) ^ (int)fget(i + n_));
-            r.rd.push_back((uint32_t)(i + n_));
-            row_xor(s, i + n_);
-        }
+    auto take = [&](int64_t i) {
+        c ^= (uint32_t)(phase_bit(s, i + n_) ^ (int)fget(i + n_));
+        r.rd.push_back((uint32_t)(i + n_));
+        row_xor(s, i + n_);
+    };
+    if (xq) {
+        each_set(xq, 0, n_, take);
+    } else {
+        for (int64_t i = 0; i < n_; ++i)
+            if (bit(x_, i, q)) take(i);
+    }
     r.c = c;
     fset(s, false);
-    if (reset)
-        for (int64_t i = 0; i < W_; ++i)
-            if (bit(z_, i, q)) r.rs.push_back((uint32_t)i);
+    if (reset) {
+        if (zq) {
+            each_set(zq, 0, 2 * n_, [&](int64_t i) { r.rs.push_back((uint32_t)i); });
+            if (bit(z_, s, q)) r.rs.push_back((uint32_t)s);
+        } else {
+            for (int64_t i = 0; i < W_; ++i)
+                if (bit(z_, i, q)) r.rs.push_back((uint32_t)i);
+        }
+    }
     if (r.rd.size() > kWinRows || r.rs.size() > kWinRows) {  // too long for a window record: alone
         flush_window();
         FrameOp op{};

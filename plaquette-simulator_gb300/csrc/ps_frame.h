@@ -166,6 +166,7 @@ class FrameBuilder {
     std::vector<uint64_t> x_, z_;    // row-major [W][nw]
     std::vector<uint64_t> xc_, zc_;  // column-major [n][ww]
     bool col_ = false;
+    bool colok_ = false;    // row-major mode: the column-major copy is exact but for the scratch row
     bool seg_col_ = false;  // the current segment runs column-major
     std::vector<uint64_t> fb_;       // pending constant flips, a bit per row
     bool fget(int64_t i) const { return (fb_[(size_t)(i >> 6)] >> (i & 63)) & 1ull; }

@@ -166,6 +166,13 @@ def run_reference(args):
         times.append(secs)
     sec = sum(times) / len(times)
     value = gates * sample / sec
+    # The same circuit without its channels (the same gates: channels are not
+    # counted), once: the reference applies every channel outcome as flag
+    # gates (H S S H / S S with the shot's flag), so its noisy and noiseless
+    # rates differ.
+    from plaquette_simulator import circuits as C
+    quiet = C.surface_code_memory(meta["distance"], meta["rounds"], p=0.0)
+    qsec, _ = cpu_sample(quiet, 12345, sample)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "shot-gates/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
@@ -177,6 +184,8 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": "shot-gates/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} shots per step of the {shots}-shot workload"},
         "e2e": {"value": value, "unit": "shot-gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "noiseless": {"value": quiet.num_gates() * sample / qsec, "unit": "shot-gates/s",
+                      "what": f"the same circuit at p=0, {sample} shots, timed once"},
         "note": "the reference's own CPU build needs Kokkos (not available); its headers compiled on the "
                 "project's Kokkos-API shim validate this port in the tests, but only the port travels "
                 "to the GPU box (no reference checkout there)",

@@ -155,6 +155,59 @@ PS_HD ChannelWord channel_word(uint64_t seed, uint64_t event, uint64_t word, con
     }
 }
 
+// The survival products of a channel's table as a table: surv[j] = S_{j+1},
+// j = 0..63, by the same integer steps channel_word takes one at a time
+// (surv[63] = S_64 = thr[count]).  Unused when total = 0.
+PS_HD void channel_surv_table(uint64_t total, uint32_t *surv) {
+    const uint32_t q = (uint32_t)((1ull << 32) - total);
+    uint32_t s = q;  // S_1
+    for (int j = 0; j < 64; ++j) {
+        surv[j] = s;
+        s = mulhi32(s, q);
+    }
+}
+
+// channel_word with the survival products read from channel_surv_table's
+// table: the gap to the next hit -- the first j with u >= S_{j+1} -- is
+// found by binary search (the S_j only decrease) instead of stepping S_j.
+// The same outcomes bit for bit.
+PS_HD ChannelWord channel_word_surv(uint64_t seed, uint64_t event, uint64_t word, const uint64_t *thr, int count,
+                                    const uint32_t *surv) {
+    ChannelWord m{0ull, 0ull, 0ull, 0ull};
+    const uint64_t total = thr[count - 1];
+    if (total == 0) return m;
+    u32x4 blk = draw_block(seed, event, word, 0u, TAG_NOISE);
+    uint32_t u = blk.v[0];
+    if ((uint64_t)u < thr[count]) return m;  // no shot of the word is hit
+    uint32_t i = 1;  // the next draw
+    int pos = 0;     // the first shot not sampled yet
+    for (;;) {
+        int lo = 0, hi = 64 - pos;  // the first j in [0, 64 - pos) with u >= surv[j], else 64 - pos
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (u >= surv[mid]) hi = mid;
+            else lo = mid + 1;
+        }
+        if (lo == 64 - pos) return m;
+        pos += lo;
+        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
+        const uint64_t v = ((uint64_t)block_lane(blk, i & 3u) * total) >> 32;
+        ++i;
+        int idx = 1;
+        while (v >= thr[idx - 1]) ++idx;
+        const u64 bit = 1ull << pos;
+        const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
+        if (pa == 1 || pa == 2) m.fxa |= bit;
+        if (pa == 2 || pa == 3) m.fza |= bit;
+        if (pb == 1 || pb == 2) m.fxb |= bit;
+        if (pb == 2 || pb == 3) m.fzb |= bit;
+        if (++pos == 64) return m;
+        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
+        u = block_lane(blk, i & 3u);
+        ++i;
+    }
+}
+
 // ----------------------------------------------------------- sign math
 // Bit-sliced mod-4 accumulation of the reference's PauliProductPhase
 // (MeasurementFunctors.hpp:10-72) over 64 shots at once.  For row i (x1,z1)

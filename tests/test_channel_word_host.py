@@ -1,8 +1,9 @@
-"""channel_word (ps_common.cuh, the device's Pauli-channel sampler) compiled
-as host code with nvcc, against the oracle's restatement (ora_channel_paulis)
-on the CPU: every shot of 12,000 words, one- and two-qubit channels, totals
-from 0 to 1, bit for bit.  The GPU parity tests check the device build of the
-same function."""
+"""channel_word and channel_word_surv (ps_common.cuh, the device's
+Pauli-channel samplers: survival products stepped one by one, or binary
+searched in a table) compiled as host code with nvcc, against the oracle's
+restatement (ora_channel_paulis) on the CPU: every shot of 12,000 words, one-
+and two-qubit channels, totals from 0 to 1, bit for bit.  The GPU parity tests
+check the device builds of the same functions."""
 import os
 import shutil
 import subprocess
@@ -37,11 +38,16 @@ int main() {
         const int count = c < 5 ? 3 : 15;
         uint64_t thr[16];
         table(p, count, thr);
+        uint32_t surv[64];
+        ps::channel_surv_table(thr[count - 1], surv);
+        if (thr[count - 1] != 0 && surv[63] != thr[count]) ++bad;
         for (uint64_t ev = 0; ev < 50; ++ev) {
             static int32_t o[64 * 40 + 1];
             ora_channel_paulis(12345 + c, ev, 128, 64 * 40, p, count, o);
             for (int64_t wd = 0; wd < 40; ++wd) {
                 const ps::ChannelWord m = ps::channel_word(12345 + c, ev, 2 + wd, thr, count);
+                const ps::ChannelWord m2 = ps::channel_word_surv(12345 + c, ev, 2 + wd, thr, count, surv);
+                bad += m2.fxa != m.fxa || m2.fza != m.fza || m2.fxb != m.fxb || m2.fzb != m.fzb;
                 for (int b = 0; b < 64; ++b) {
                     const int k = o[wd * 64 + b];
                     const int pa = count == 3 ? k : k >> 2, pb = count == 3 ? 0 : k & 3;

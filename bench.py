@@ -394,22 +394,16 @@ def main():
     seg_bytes = meas_bytes = None
     if shared:
         # Algorithmic bytes of the shared-x/z plan (per run):
-        #  sign program: every launch reads and writes the signs of all rows
-        #    and shot-words (the first starts from zero), plus the records
-        #    (result + determined words per measurement);
-        #  channel sampling: the sampling launches also write the x/z
-        #    broadcast -- the x and z words of every row, qubit and shot-word
-        #    -- counted here; their outcome entries (tens of MB) are not.
-        nl = max(1, prof["sign_program"]["launches"])
+        #  sign program (one launch): the final signs of every row and
+        #    shot-word written once, plus the records (result + determined
+        #    words per measurement);
+        #  x / z broadcast: the x and z words of every row, qubit and
+        #    shot-word written once.
         kind_bytes = {
-            "sign_program": (2 * nl - 1) * W * w_words * 8 + 2 * nm * w_words * 8,
-            "channel_sample": 2 * W * n_q * w_words * 8,
+            "sign_program": W * w_words * 8 + 2 * nm * w_words * 8,
+            "xz_broadcast": 2 * W * n_q * w_words * 8,
         }
-        if prof.get("xz_broadcast", {}).get("launches"):
-            kind_bytes["xz_broadcast"] = 2 * W * n_q * w_words * 8
-            kind_bytes["channel_sample"] = 0
-        kernel_of = {"sign_program": "frame_kernel", "xz_broadcast": "broadcast_xz_kernel",
-                     "channel_sample": "noise_frame_kernel (one-pass channel sampling + its share of the x/z broadcast)"}
+        kernel_of = {"sign_program": "frame_run_kernel", "xz_broadcast": "broadcast_jobs_kernel"}
     else:
         meas_bytes = fused.measure_bytes(reset=True)
         seg_bytes = float(fused.stats["segment_bytes"])
@@ -434,12 +428,11 @@ def main():
                               "algorithmic_GBps": kind_bytes[k] / max(1e-9, prof[k]["ms"] / 1e3) / 1e9}
                           for k in kind_bytes}}
     if dom == "sign_program":
-        roofline["note"] = ("latency-bound: one CTA per shot-word runs the sign program's ops in order on "
-                            "signs held in shared memory; it moves little HBM data by design")
-    elif dom == "channel_sample":
-        roofline["note"] = ("the sampling launches draw the channel outcomes (one Philox block per channel and "
-                            "shot-word without hits) and write the x/z broadcast; achieved counts the broadcast only, "
-                            "over event times that include each launch's submit gap (a lower bound)")
+        roofline["note"] = ("latency-bound: one CTA per shot-word runs the whole sign program on signs held in "
+                            "shared memory; it moves little HBM data by design")
+    elif dom == "xz_broadcast":
+        roofline["note"] = ("the broadcast writes the final x / z bits of every row, qubit and shot; in the run "
+                            "it overlaps the sign kernel on a side stream (times here are serialised launches)")
 
     line = {
         "metric": METRIC, "value": value, "unit": "shot-gates/s", "n_gpus": world, "steps": args.steps,

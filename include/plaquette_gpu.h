@@ -217,6 +217,10 @@ typedef struct {
                              bit-identical, and the final x / z bits are
                              written to every shot; 1 = always update every
                              shot's tableau                                   */
+    int32_t frame_warps; /* shared-x/z runs: sign-kernel warps per shot-word, 4
+                             or 8 (0 = auto)                                  */
+    int32_t bcast_ctas;  /* shared-x/z runs: x / z broadcast CTAs per SM (0 =
+                             auto); the rest of each SM runs the sign kernel  */
 } ps_circuit_options;
 
 typedef struct {

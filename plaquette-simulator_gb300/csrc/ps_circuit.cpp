@@ -16,6 +16,7 @@
 
 #include "../../include/plaquette_gpu.h"
 #include "ps_frame.h"
+#include "ps_frame_dev.h"
 #include "ps_internal.h"
 #include "ps_segment.cuh"
 
@@ -103,6 +104,7 @@ struct ps_circuit {
     MeasOp *d_meas = nullptr;
     RunParams *d_params = nullptr;
     uint64_t *d_thr = nullptr;
+    std::vector<uint64_t> thr_host; // the distinct channel tables (host copy of d_thr)
     u64 **d_recs = nullptr;
     u64 *d_masks = nullptr;         // plain-mode channel masks (4w)
     u64 *d_forced = nullptr;        // [nm][w]
@@ -123,15 +125,14 @@ struct ps_circuit {
     bool force_per_shot = false;    // measurement statistics need the per-shot plan
     FrameProgram fprog;
     FrameOp *d_fops = nullptr;
-    uint32_t *d_ftab = nullptr, *d_fslot = nullptr;
+    uint32_t *d_ftab = nullptr;
     int32_t *d_frand = nullptr;
     uint64_t *d_fxz = nullptr;
-    // Outcome buffers of the shared-x/z plan (the first is d_entries /
-    // d_entry_count): sampling runs up to fent.size() - 1 segments ahead.
-    std::vector<NoiseEntry *> fent;
-    std::vector<int32_t *> fcnt;
-    cudaStream_t fstream[2] = {nullptr, nullptr};  // sampling, x/z broadcast
-    std::vector<cudaEvent_t> fev;
+    // The shared-x/z plan as a job table of one job (ps_frame_dev.h): one
+    // sign-kernel launch and one x / z broadcast beside it on a side stream.
+    FrameTable ftable;
+    cudaStream_t fstream = nullptr;  // the broadcast's side stream
+    cudaEvent_t fev[2] = {nullptr, nullptr};
     cudaGraph_t graph[2] = {nullptr, nullptr};      // [reset_state]
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
 };
@@ -788,117 +789,135 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
     return OK;
 }
 
-// The shared-x/z plan of a run from |0...0>: for each range of the sign
-// program, the channel sampling of its segment and the sign kernel; and the
-// broadcast of the final x / z bits (host-known, so it needs nothing else).
-// Unless profiled, the plan forks: the broadcast on one side stream, the
-// sampling on another running ahead of the sign kernels through NB rotating
-// outcome buffers (sampling segment j+NB waits for the sign kernel that
-// consumed segment j), both joined back at the end.
-int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
+// The device job of a compiled circuit's sign program (all but the tables
+// the caller uploads: ranges, channel records, channel tables, survival
+// products): one range per launch range of the program, and the
+// shared-memory layout.  A range's ops and measurement tab words are staged
+// in shared memory while the staging buffers stay within kFrameStageMax;
+// ranges that would need more read them from global memory.  E_ARG: the
+// program does not fit this kernel (the per-shot plan runs instead).
+int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev> &ranges,
+                     std::vector<FrameSlotDev> &slots, std::vector<FrameChanTab> &ctabs, std::vector<uint32_t> &surv) {
     ps_state *h = c->h;
+    const FrameProgram &P = c->fprog;
+    ranges.clear();
+    uint32_t max_rand = 0, max_scratch = 0, max_slots = 0;
+    // channel records (indexed like slot_off) and the distinct tables
+    slots.assign(P.slot_off.size(), FrameSlotDev{});
+    std::map<int32_t, uint32_t> table_of;
+    ctabs.clear();
+    surv.clear();
+    for (const FrameProgram::Launch &L : P.launches) {
+        max_rand = std::max(max_rand, L.nrand);
+        max_scratch = std::max(max_scratch, L.scratch);
+        FrameRangeDev r{};
+        r.op0 = L.op0;
+        r.op1 = L.op1;
+        r.rand0 = L.rand0;
+        r.nrand = L.nrand;
+        if (L.seg >= 0) {
+            if (L.op0 >= L.op1 || (P.ops[L.op0].kind & 0xFFu) != F_NOISE)
+                return fail(E_ARG, "shared-x/z plan: a sampled range must start with its noise");
+            const SegHost &sg = c->segs[(size_t)L.seg];
+            r.nslots = (int32_t)sg.slots.size();
+            r.slot_base = (uint32_t)P.ops[L.op0].arg;
+            max_slots = std::max(max_slots, (uint32_t)r.nslots);
+            if ((size_t)r.slot_base + (size_t)r.nslots >= slots.size())
+                return fail(E_ARG, "shared-x/z plan: channel table out of range");
+            for (int32_t q = 0; q < r.nslots; ++q) {
+                const NoiseSlot &sl = sg.slots[(size_t)q];
+                auto it = table_of.find(sl.thr_off);
+                if (it == table_of.end()) {
+                    if (ctabs.size() >= kFrameMaxTables) return fail(E_ARG, "shared-x/z plan: too many channel tables");
+                    it = table_of.emplace(sl.thr_off, (uint32_t)ctabs.size()).first;
+                    ctabs.push_back(FrameChanTab{sl.thr_off, sl.count, (uint32_t)surv.size(), 0u});
+                    surv.resize(surv.size() + 64);
+                    channel_surv_table(c->thr_host[(size_t)(sl.thr_off + sl.count - 1)], &surv[surv.size() - 64]);
+                }
+                const uint32_t t0 = P.slot_off[(size_t)r.slot_base + (size_t)q];
+                const uint32_t len = P.slot_off[(size_t)r.slot_base + (size_t)q + 1] - t0;
+                if (len > kFrameMaxSlotRows) return fail(E_ARG, "shared-x/z plan: a channel flips too many rows");
+                const bool never = c->thr_host[(size_t)(sl.thr_off + sl.count - 1)] == 0;
+                FrameSlotDev &d = slots[(size_t)r.slot_base + (size_t)q];
+                d.s64 = never ? 0u : (uint32_t)c->thr_host[(size_t)(sl.thr_off + sl.count)];
+                d.event = sl.event;
+                d.t0 = t0;
+                d.lt = len << 12 | (never ? kFrameNoHit : it->second);
+            }
+        }
+        r.tab0a = L.tab0 & ~3u;
+        r.ntab16 = (((L.tab1 + 3u) & ~3u) - r.tab0a) / 4;
+        ranges.push_back(r);
+    }
+    if (ranges.empty()) return fail(E_ARG, "shared-x/z plan: empty program");
+    job.R = h->R;
+    job.n = h->n;
+    job.w = h->w;
+    job.ops = c->d_fops;
+    job.tab = c->d_ftab;
+    job.nranges = (int32_t)ranges.size();
+    job.rand_meas = c->d_frand;
+    job.meas = c->d_meas;
+    job.rec = c->d_res_block;
+    job.nm = (int64_t)c->meas.size();
+    job.thr = c->d_thr;
+    job.rp = c->d_params;
+    job.max_rand = max_rand;
+    job.max_scratch = max_scratch;
+    job.max_slots = max_slots;
+    job.n_ctab = (uint32_t)ctabs.size();
+    job.n_thr = (uint32_t)c->thr_host.size();
+    job.n_surv = (uint32_t)surv.size();
+    job.stage_tabs = (size_t)job.n_ctab * 16 + (size_t)job.n_thr * 8 + (size_t)job.n_surv * 4 <= kFrameTabStage ? 1u : 0u;
+    // staging: drop the largest staged range until the buffers fit
+    std::vector<char> on(ranges.size(), 1);
+    for (;;) {
+        uint32_t tab = 0, nops = 0;
+        size_t worst = ranges.size(), worst_need = 0;
+        for (size_t i = 0; i < ranges.size(); ++i) {
+            if (!on[i]) continue;
+            tab = std::max(tab, 4 * ranges[i].ntab16);
+            nops = std::max(nops, ranges[i].op1 - ranges[i].op0);
+            const size_t need = (size_t)ranges[i].ntab16 * 16 + (size_t)(ranges[i].op1 - ranges[i].op0) * sizeof(FrameOp);
+            if (need >= worst_need) {
+                worst = i;
+                worst_need = need;
+            }
+        }
+        job.stage_u32 = tab;
+        job.max_ops = nops;
+        if (worst == ranges.size() || (size_t)tab * 4 + (size_t)nops * sizeof(FrameOp) <= kFrameStageMax) break;
+        on[worst] = 0;
+    }
+    for (size_t i = 0; i < ranges.size(); ++i) ranges[i].stage = on[i] ? 1u : 0u;
+    if (frame_job_smem(job) > kSegSmemMax) return fail(E_ARG, "sign program does not fit in shared memory");
+    return OK;
+}
+
+// The shared-x/z plan of a run from |0...0>: the whole sign program (channel
+// sampling included) as one launch, and the broadcast of the final x / z
+// bits (host-known, so it needs nothing else) beside it on a side stream,
+// joined back at the end.  Profiled, the two run one after the other.
+int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
     auto timed = [&](int kind, auto &&launch) -> int {
         if (prof && prof->begin(kind) != OK) return E_CUDA;
         int rc = launch();
         if (prof && rc == OK && prof->end() != OK) return E_CUDA;
         return rc;
     };
-    const bool fork = prof == nullptr && c->fstream[0] != nullptr;
-    cudaStream_t ss = fork ? c->fstream[0] : st, sb = fork ? c->fstream[1] : st;
-    size_t nev = 0;
-    auto record = [&](cudaStream_t s, cudaEvent_t *e) -> int {
-        if (nev >= c->fev.size()) return fail(E_ARG, "shared-x/z plan: out of events");
-        *e = c->fev[nev++];
-        PS_CUDA(cudaEventRecord(*e, s));
-        return OK;
-    };
-    const size_t nb = c->fent.size();
-    const std::vector<NoiseEntry *> &ebuf = c->fent;
-    const std::vector<int32_t *> &cbuf = c->fcnt;
-    // The x / z broadcast rides on the sampling launches: sampling launch j
-    // writes (row, qubit) pairs [j*P/S, (j+1)*P/S) of the P = W*n.  (As a
-    // kernel of its own beside the run it was slower, at every grid size and
-    // priority tried.)  Without sampling launches it is a kernel of its own
-    // on the side stream.
-    XZBroadcast bc;
-    bc.X = h->X;
-    bc.Z = h->Z;
-    bc.xz = c->d_fxz;
-    bc.n = h->n;
-    bc.w = h->w;
-    bc.nw64 = c->fprog.nw64;
-    const int64_t P = h->W * h->n;
-    int64_t nsamp = 0;
-    for (const FrameProgram::Launch &L : c->fprog.launches) nsamp += L.seg >= 0 ? 1 : 0;
-    if (fork) {
-        cudaEvent_t e0;
-        int rc = record(st, &e0);
+    if (prof || !c->fstream) {
+        int rc = timed(P_FRAME, [&] { return launch_frame_run(st, c->ftable, c->opts.frame_warps); });
         if (rc != OK) return rc;
-        PS_CUDA(cudaStreamWaitEvent(ss, e0, 0));
-        PS_CUDA(cudaStreamWaitEvent(sb, e0, 0));
-        if (nsamp == 0) {
-            XZBroadcast all = bc;
-            all.rq0 = 0;
-            all.rq1 = P;
-            rc = launch_broadcast_xz(sb, all, true);
-            if (rc != OK) return rc;
-        }
+        return timed(P_BROADCAST, [&] { return launch_broadcast_jobs(st, c->ftable, c->opts.bcast_ctas); });
     }
-    // The one-pass sampler appends to per-word lists from a zero count: the
-    // counters of this plan are zeroed at compile time, and every sign
-    // kernel zeroes the ones it consumed, so each run finds them zero.
-    std::vector<cudaEvent_t> consumed;  // sign kernel done with sampled segment j
-    bool first = true;
-    for (const FrameProgram::Launch &L : c->fprog.launches) {
-        int rc = OK;
-        size_t b = 0;
-        const bool sampled = L.seg >= 0;
-        if (sampled) {
-            const size_t j = consumed.size();
-            b = j % nb;
-            if (fork && j >= nb) PS_CUDA(cudaStreamWaitEvent(ss, consumed[j - nb], 0));
-            SegmentDev d = c->segs[(size_t)L.seg].dev;
-            d.entries = ebuf[b];
-            d.entry_count = cbuf[b];
-            XZBroadcast share = bc;
-            share.rq0 = P * (int64_t)j / nsamp;
-            share.rq1 = P * (int64_t)(j + 1) / nsamp;
-            rc = timed(P_SAMPLE, [&] {
-                return launch_noise_sample_frame(ss, d, h->w, c->d_params, c->d_fslot, (uint32_t)c->fprog.ops[L.op0].arg,
-                                                 share);
-            });
-            if (rc == OK && fork) {
-                cudaEvent_t es;
-                rc = record(ss, &es);
-                if (rc == OK) PS_CUDA(cudaStreamWaitEvent(st, es, 0));
-            }
-        }
-        if (rc == OK)
-            rc = timed(P_FRAME, [&] {
-                return launch_frame(st, h->R, h->n, h->w, c->d_fops, L.op0, L.op1, c->d_ftab, L.tab0, L.tab1,
-                                    c->d_fslot, c->d_frand + L.rand0, L.nrand, c->d_meas, c->d_res_block,
-                                    (int64_t)c->meas.size(), ebuf[b], cbuf[b], c->entry_cap, (uint64_t)h->seed,
-                                    c->d_params, first ? 1 : 0, sampled ? 1 : 0, L.scratch);
-            });
-        if (rc != OK) return rc;
-        if (sampled) {
-            cudaEvent_t ef = nullptr;
-            if (fork && record(st, &ef) != OK) return E_ARG;
-            consumed.push_back(ef);
-        }
-        first = false;
-    }
-    if (!fork) {
-        if (nsamp > 0) return OK;
-        XZBroadcast all = bc;
-        all.rq0 = 0;
-        all.rq1 = P;
-        return timed(P_BROADCAST, [&] { return launch_broadcast_xz(st, all, false); });
-    }
-    cudaEvent_t es, eb;
-    if (record(ss, &es) != OK || record(sb, &eb) != OK) return E_ARG;
-    PS_CUDA(cudaStreamWaitEvent(st, es, 0));
-    PS_CUDA(cudaStreamWaitEvent(st, eb, 0));
+    PS_CUDA(cudaEventRecord(c->fev[0], st));
+    PS_CUDA(cudaStreamWaitEvent(c->fstream, c->fev[0], 0));
+    int rc = launch_broadcast_jobs(c->fstream, c->ftable, c->opts.bcast_ctas);
+    if (rc != OK) return rc;
+    rc = launch_frame_run(st, c->ftable, c->opts.frame_warps);
+    if (rc != OK) return rc;
+    PS_CUDA(cudaEventRecord(c->fev[1], c->fstream));
+    PS_CUDA(cudaStreamWaitEvent(st, c->fev[1], 0));
     return OK;
 }
 
@@ -1131,6 +1150,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     std::vector<uint32_t> event_of(ops.size(), 0);
     std::vector<int32_t> rec_of(ops.size(), -1), thr_off(ops.size(), -1);
     std::vector<uint64_t> thr;
+    std::map<std::vector<uint64_t>, int32_t> thr_index;
     uint32_t ev = 0;
     int32_t nrec = 0;
     for (size_t i = 0; i < ops.size(); ++i) {
@@ -1151,13 +1171,21 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 return bail(fail(E_ARG, "op " + std::to_string(i) + ": channel parameters out of range"));
             uint64_t t[16];
             channel_thresholds(params + o.c, cnt, t);
-            thr_off[i] = (int32_t)thr.size();
-            thr.insert(thr.end(), t, t + cnt + 1);
+            // one copy of each distinct table (the same probabilities on
+            // every channel of a noise model is the usual case)
+            std::vector<uint64_t> key(t, t + cnt + 1);
+            auto it = thr_index.find(key);
+            if (it == thr_index.end()) {
+                it = thr_index.emplace(std::move(key), (int32_t)thr.size()).first;
+                thr.insert(thr.end(), t, t + cnt + 1);
+            }
+            thr_off[i] = it->second;
         }
         if (is_meas(o.code)) rec_of[i] = nrec++;
         if (is_meas(o.code) || is_channel(o.code)) event_of[i] = ev++;
     }
     c->num_events = ev;
+    c->thr_host = thr;
 
     // ---- records: one contiguous block, so a run's records copy out at once
     c->stats.first_record = h->recs.size();
@@ -1368,50 +1396,58 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             if (c->fprog.slot_off.empty()) c->fprog.slot_off.push_back(0);
             if (c->fprog.rand_meas.empty()) c->fprog.rand_meas.push_back(0);
             if (upload(h, c->owned, c->fprog.ops, &c->d_fops) || upload(h, c->owned, c->fprog.tab, &c->d_ftab) ||
-                upload(h, c->owned, c->fprog.slot_off, &c->d_fslot) || upload(h, c->owned, c->fprog.xz, &c->d_fxz) ||
+                upload(h, c->owned, c->fprog.xz, &c->d_fxz) ||
                 upload(h, c->owned, c->fprog.rand_meas, &c->d_frand))
                 return bail(E_CUDA);
-            // Outcome lists hold one entry per row chunk of a slot.
-            if (c->fprog.entry_cap > c->entry_cap) {
-                void *p = nullptr;
-                if (dev_alloc(h, &p, (size_t)c->fprog.entry_cap * h->w * sizeof(NoiseEntry)) != OK)
-                    return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
-                c->owned.push_back(p);
-                c->d_entries = (NoiseEntry *)p;
-                c->entry_cap = c->fprog.entry_cap;
-                for (SegHost &sg : c->segs) {
-                    sg.dev.entries = sg.slots.empty() ? nullptr : c->d_entries;
-                    sg.dev.cap = c->entry_cap;
-                }
+            FrameJobDev job{};
+            std::vector<FrameRangeDev> ranges;
+            std::vector<FrameSlotDev> fslots;
+            std::vector<FrameChanTab> ctabs;
+            std::vector<uint32_t> surv;
+            const int jrc = frame_job_ranges(c, job, ranges, fslots, ctabs, surv);
+            if (jrc == E_ARG) {
+                set_error("");  // the program does not fit the one-launch kernel: the per-shot plan runs
+                ok = false;
+            } else if (jrc != OK) {
+                return bail(jrc);
             }
-            {  // four outcome buffers where they take at most 1 GiB, else two; own zeroed counters
-                const size_t per = (size_t)c->entry_cap * h->w * sizeof(NoiseEntry);
-                const size_t nb = 4 * per <= ((size_t)1 << 30) ? 4 : 2;
-                c->fent.assign(1, c->d_entries);
-                c->fcnt.clear();
-                for (size_t b = 0; b < nb; ++b) {
-                    void *p = nullptr;
-                    if (b > 0) {
-                        if (dev_alloc(h, &p, per) != OK)
-                            return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
-                        c->owned.push_back(p);
-                        c->fent.push_back((NoiseEntry *)p);
-                    }
-                    if (dev_alloc(h, &p, (size_t)h->w * sizeof(int32_t)) != OK) return bail(E_NOMEM);
-                    c->owned.push_back(p);
-                    c->fcnt.push_back((int32_t *)p);
-                    if (cudaMemsetAsync(p, 0, (size_t)h->w * sizeof(int32_t), h->stream) != cudaSuccess)
-                        return bail(cuda_fail(cudaGetLastError(), "cudaMemsetAsync"));
-                }
-            }
-            for (int k = 0; k < 2; ++k)
-                if (cudaStreamCreateWithFlags(&c->fstream[k], cudaStreamNonBlocking) != cudaSuccess)
+            if (ok) {  // the job table of one job
+                FrameRangeDev *dr = nullptr;
+                FrameSlotDev *dsl = nullptr;
+                FrameChanTab *dct = nullptr;
+                uint32_t *dsv = nullptr;
+                if (upload(h, c->owned, ranges, &dr) || upload(h, c->owned, fslots, &dsl) ||
+                    upload(h, c->owned, ctabs, &dct) || upload(h, c->owned, surv, &dsv))
+                    return bail(E_CUDA);
+                job.ranges = dr;
+                job.slot = dsl;
+                job.ctab = dct;
+                job.surv = dsv;
+                BroadcastJobDev bj{h->X, h->Z, c->d_fxz, h->n, h->w, c->fprog.nw64};
+                const std::vector<FrameJobDev> jobs{job};
+                const std::vector<BroadcastJobDev> bjobs{bj};
+                const std::vector<int64_t> cta0{0, h->w}, chunk0{0, broadcast_chunks(h->n, h->w)};
+                FrameJobDev *dj = nullptr;
+                BroadcastJobDev *db = nullptr;
+                int64_t *dc = nullptr, *dk = nullptr;
+                if (upload(h, c->owned, jobs, &dj) || upload(h, c->owned, bjobs, &db) ||
+                    upload(h, c->owned, cta0, &dc) || upload(h, c->owned, chunk0, &dk))
+                    return bail(E_CUDA);
+                c->ftable.jobs = dj;
+                c->ftable.bjobs = db;
+                c->ftable.cta0 = dc;
+                c->ftable.chunk0 = dk;
+                c->ftable.njobs = 1;
+                c->ftable.ctas = h->w;
+                c->ftable.chunks = chunk0[1];
+                c->ftable.smem = frame_job_smem(job);
+                if (cudaStreamCreateWithFlags(&c->fstream, cudaStreamNonBlocking) != cudaSuccess)
                     return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
-            c->fev.assign(3 + 2 * c->fprog.launches.size() + 2, nullptr);
-            for (cudaEvent_t &e : c->fev)
-                if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
-                    return bail(cuda_fail(cudaGetLastError(), "cudaEventCreate"));
-            c->frame_ok = true;
+                for (cudaEvent_t &e : c->fev)
+                    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                        return bail(cuda_fail(cudaGetLastError(), "cudaEventCreate"));
+                c->frame_ok = true;
+            }
         }
     }
 
@@ -1438,15 +1474,9 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         }
     }
     st.launches_per_run += 1;  // run-parameter update
-    if (c->frame_ok) {  // runs from |0...0>: per range its sampling kernel (if any) and sign kernel, the parameters
+    if (c->frame_ok) {  // runs from |0...0>: the parameters, the sign kernel, the broadcast
         st.shared_xz = 1;
-        st.launches_per_run = 1;
-        bool sampled = false;
-        for (const FrameProgram::Launch &L : c->fprog.launches) {
-            st.launches_per_run += L.seg >= 0 ? 2 : 1;
-            sampled |= L.seg >= 0;
-        }
-        if (!sampled) st.launches_per_run += 1;  // the broadcast, on the sampling launches otherwise
+        st.launches_per_run = 3;
     }
     st.seg_rows = c->opts.seg_rows;
     st.seg_words = c->opts.seg_words;
@@ -1659,11 +1689,10 @@ ps_status ps_circuit_destroy(ps_circuit *c) {
         if (c->exec[k]) cudaGraphExecDestroy(c->exec[k]);
         if (c->graph[k]) cudaGraphDestroy(c->graph[k]);
     }
-    for (cudaStream_t fs : c->fstream)
-        if (fs) {
-            cudaStreamSynchronize(fs);
-            cudaStreamDestroy(fs);
-        }
+    if (c->fstream) {
+        cudaStreamSynchronize(c->fstream);
+        cudaStreamDestroy(c->fstream);
+    }
     for (cudaEvent_t e : c->fev)
         if (e) cudaEventDestroy(e);
     for (void *p : c->owned) dev_free(c->h, p);

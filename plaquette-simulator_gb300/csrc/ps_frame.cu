@@ -1,33 +1,21 @@
 // ps_frame.cu -- device side of shared-x/z runs (see ps_frame.h): the sign
-// program over each shot-word's signs, and the broadcast of the final x / z
-// bits to every shot.
+// program of a whole run over each shot-word's signs in ONE launch, and the
+// broadcast of the final x / z bits to every shot.  Both take a job table
+// (ps_frame_dev.h): a single circuit is a table of one job, a batch of
+// circuits is one table, so a batch run is these two launches too.
 #include <algorithm>
+#include <mutex>
+#include <set>
 
 #include "ps_draw.cuh"
-#include "ps_frame.h"
-#include "ps_internal.h"
-#include "ps_segment.cuh"
+#include "ps_frame_dev.h"
 
 namespace ps {
 
 namespace {
 
-// One CTA of FW warps per shot-word: its W signs live in shared memory while
-// it runs ops [op0, op1) in order.  Channel outcomes go one per thread over
-// all warps (XORs commute; shared atomics where two outcomes flip one row),
-// and so do the outputs of an F_LINEAR op; the other measurement ops (those
-// the builder left out of its linear maps) run on warp 0 -- a window's
-// measurements one per lane, the rows of other ops over the lanes -- with
-// block barriers around every all-warp op.  When
-// `stage` is set the launch's ops and the tab range [tab0, tab0 + ntab) of
-// its measurement ops are first copied to shared memory, so the op stream
-// runs on shared-memory latency; channel rows stay in global memory (a word
-// uses few of them).  Record k of the circuit lives at rec + k*w (results)
-// and rec + (nm + k)*w (determined flags).
-constexpr int FW = 4;  // warps per shot-word
-
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
                  : "memory");
 }
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -35,196 +23,445 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
                  : "memory");
 }
 
-__global__ void __launch_bounds__(32 * FW, 4) frame_kernel(u64 *__restrict__ R, int64_t n, int64_t w,
-                                                   const FrameOp *__restrict__ ops, uint32_t op0, uint32_t op1,
-                                                   const uint32_t *__restrict__ tab, uint32_t tab0, uint32_t ntab16,
-                                                   int stage, const uint32_t *__restrict__ slot_off,
-                                                   const int32_t *__restrict__ rand_meas, uint32_t nrand,
-                                                   const MeasOp *__restrict__ meas, u64 *__restrict__ rec,
-                                                   int64_t nm, const NoiseEntry *__restrict__ entries,
-                                                   int32_t *__restrict__ entry_count, int32_t cap, uint64_t seed,
-                                                   const RunParams *__restrict__ rp, int from_zero,
-                                                   int noise_first) {
-    extern __shared__ u64 sR[];
-    const int64_t W = 2 * n + 1;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int64_t k = blockIdx.x;
-    u64 *sout = sR + W + 1 + kWinRows;  // the launch's random outcomes, drawn up front
-    uint32_t *stab = reinterpret_cast<uint32_t *>(((uintptr_t)(sout + nrand) + 15) & ~(uintptr_t)15);
-    FrameOp *sops = reinterpret_cast<FrameOp *>(stab + 4 * ntab16);
-    u64 *snew = reinterpret_cast<u64 *>(sops + (stage ? op1 - op0 : 0u));  // F_LINEAR's new rows
-    // Signs, the tab range (16-byte chunks from the aligned tab0) and the ops
-    // are copied asynchronously, all in flight at once, while the random
-    // outcomes are drawn.
-    if (from_zero) {
-        for (int64_t i = tid; i < W; i += 32 * FW) sR[i] = 0ull;
-    } else {
-        for (int64_t i = tid; i < W; i += 32 * FW) cp_async8(&sR[i], R + i * w + k);
+// The job of a CTA (or broadcast chunk) index: the last j with first[j] <= i.
+__device__ __forceinline__ int job_of(const int64_t *__restrict__ first, int njobs, int64_t i) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(first + mid) <= i) lo = mid;
+        else hi = mid - 1;
     }
-    if (tid < 1 + (int)kWinRows) sR[W + tid] = 0ull;  // zero row (unused window reads), sinks (unused writes)
-    if (stage) {
-        for (uint32_t i = tid; i < ntab16; i += 32 * FW) cp_async16(stab + 4 * i, tab + tab0 + 4 * i);
-        for (uint32_t i = tid; i < op1 - op0; i += 32 * FW) cp_async16(sops + i, ops + op0 + i);
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-    // A launch that starts with its segment's channel outcomes: each thread's
-    // first outcome and its rows are fetched now, under the copies' latency.
-    int pcnt = 0;
-    NoiseEntry pen;
-    pen.a = 0;
-    uint32_t pv[kFrameChunk];
-    if (noise_first) {
-        pcnt = entry_count[k];
-        if (tid < pcnt) pen = entries[k * (int64_t)cap + tid];
-#pragma unroll
-        for (uint32_t u = 0; u < kFrameChunk; ++u) pv[u] = u < pen.a ? tab[(uint32_t)pen.layer + u] : 0u;
-    }
-    const uint64_t event_base = rp->event_base, word_base = rp->word_base;
-    for (uint32_t j = tid; j < nrand; j += 32 * FW)
-        sout[j] = outcome_word(meas[rand_meas[j]], seed, event_base, k, word_base);
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-    __syncthreads();
-    const uint32_t *T = stage ? stab : tab;  // measurement-op tab, indexed x - tb
-    const uint32_t tb = stage ? tab0 : 0u;
-    u64 last = 0ull;  // outcome of the latest measurement (its reset X)
-    for (uint32_t oi = op0; oi < op1; ++oi) {
-        const FrameOp o = stage ? sops[oi - op0] : ops[oi];
-        const uint32_t kind = o.kind & 0xFFu;
-        if (kind == F_NOISE) {
-            __syncthreads();  // warp 0's measurement ops before
-            auto apply = [&](const NoiseEntry &en, const uint32_t (&v)[kFrameChunk]) {
-#pragma unroll
-                for (uint32_t u = 0; u < kFrameChunk; ++u) {
-                    if (v[u] == 0u) continue;  // a row entry is never 0 (sel != 0)
-                    const uint32_t sel = v[u] >> 28;
-                    u64 m = 0ull;
-                    if (sel & 1u) m ^= en.fxa;
-                    if (sel & 2u) m ^= en.fza;
-                    if (sel & 4u) m ^= en.fxb;
-                    if (sel & 8u) m ^= en.fzb;
-                    atomicXor(&sR[v[u] & kFrameRowMask], m);
-                }
-            };
-            const bool pre = noise_first && oi == op0;
-            const int cnt = pre ? pcnt : entry_count[k];
-            const NoiseEntry *ent = entries + k * (int64_t)cap;
-            if (pre && tid < cnt) apply(pen, pv);
-            for (int e = tid + (pre ? 32 * FW : 0); e < cnt; e += 32 * FW) {
-                const NoiseEntry en = ent[e];  // layer: first row entry, a: row count (<= kFrameChunk)
-                uint32_t v[kFrameChunk];
-#pragma unroll
-                for (uint32_t u = 0; u < kFrameChunk; ++u) v[u] = u < en.a ? tab[(uint32_t)en.layer + u] : 0u;
-                apply(en, v);
-            }
-            __syncthreads();
-            if (tid == 0) entry_count[k] = 0;  // consumed: the next segment's sampling appends from 0
-        } else if (kind == F_LINEAR) {
-            // every output from the signs as they were, then the new rows
-            __syncthreads();  // warp 0's measurement ops before
-            const uint32_t *L = T + (o.off - tb);
-            const uint32_t nrec = L[0], nrow = L[1], nlast = L[2], nout = nrec + nrow + nlast;
-            const uint32_t *dst = L + 4, *beg = dst + nout, *term = beg + nout + 1;
-            for (uint32_t j = tid; j < nout; j += 32 * FW) {
-                const uint32_t d = dst[j], t1 = beg[j + 1];
-                u64 v = (d & kLinConst) ? ~0ull : 0ull;
-#pragma unroll 4
-                for (uint32_t t = beg[j]; t < t1; ++t) v ^= sR[term[t]];
-                if (j < nrec) {
-                    const int64_t m = (int64_t)(d & kLinIndex);
-                    rec[m * w + k] = v;
-                    rec[(nm + m) * w + k] = (d & kLinDet) ? ~0ull : 0ull;
-                } else {
-                    snew[j - nrec] = v;
-                }
-            }
-            __syncthreads();
-            for (uint32_t j = tid; j < nrow; j += 32 * FW) sR[dst[nrec + j] & kLinIndex] = snew[j];
-            if (nlast) last = snew[nrow];
-            __syncthreads();
-        } else if (wid != 0) {
-            continue;  // the measurement ops run on warp 0
-        } else if (kind == F_WINDOW) {
-            u64 acc = 0ull;
-            uint32_t rs[kWinRows];
-            if ((uint32_t)lane < o.len) {
-                const uint32_t *rc = T + (o.off + kWinRec * lane - tb);
-                const uint32_t m = rc[0], hdr = rc[1];
-                uint32_t rd[kWinRows];
-#pragma unroll
-                for (uint32_t t = 0; t < kWinRows; ++t) {
-                    rd[t] = rc[2 + t];
-                    rs[t] = rc[2 + kWinRows + t];
-                }
-                acc = (hdr & 1u) ? ~0ull : 0ull;
-#pragma unroll
-                for (uint32_t t = 0; t < kWinRows; ++t) acc ^= sR[rd[t]];
-                rec[(int64_t)m * w + k] = acc;
-                rec[(nm + (int64_t)m) * w + k] = ~0ull;
-                if ((uint32_t)lane == o.len - 1) sR[2 * n] = acc;
-            }
-            __syncwarp();
-            if ((uint32_t)lane < o.len) {  // a lane's reset rows are distinct, and disjoint from other lanes' (sinks aside)
-                u64 v[kWinRows];
-#pragma unroll
-                for (uint32_t t = 0; t < kWinRows; ++t) v[t] = sR[rs[t]];
-#pragma unroll
-                for (uint32_t t = 0; t < kWinRows; ++t) sR[rs[t]] = v[t] ^ acc;
-            }
-            last = __shfl_sync(0xffffffffu, acc, (int)o.len - 1);
-            __syncwarp();
-        } else if (kind == F_MEAS_DET) {
-            u64 acc = 0ull;
-            for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) acc ^= sR[T[t - tb]];
-            acc = (u64)__reduce_xor_sync(0xffffffffu, (unsigned)(acc >> 32)) << 32 |
-                  (u64)__reduce_xor_sync(0xffffffffu, (unsigned)acc);
-            if (o.kind >> 8) acc = ~acc;
-            if (lane == 0) {
-                rec[(int64_t)o.arg * w + k] = acc;
-                rec[(nm + (int64_t)o.arg) * w + k] = ~0ull;
-                sR[2 * n] = acc;
-            }
-            last = acc;
-            __syncwarp();
-        } else if (kind == F_MEAS_RAND) {
-            const u64 out = sout[o.kind >> 8];
-            const uint32_t p = T[o.off - tb];
-            const u64 rpv = sR[p + n];
-            __syncwarp();
-            if (lane == 0) {
-                sR[p] = rpv;
-                sR[p + n] = out;
-                rec[(int64_t)o.arg * w + k] = out;
-                rec[(nm + (int64_t)o.arg) * w + k] = 0ull;
-            }
-            // the multiplied rows exclude p and p+n (and are distinct): no barrier needed before them
-            for (uint32_t t = o.off + 1 + lane; t < o.off + o.len; t += 32) {
-                const uint32_t v = T[t - tb];
-                sR[v & 0x7FFFFFFFu] ^= rpv ^ ((v >> 31) ? ~0ull : 0ull);
-            }
-            last = out;
-            __syncwarp();
-        } else {  // F_RESET_X, F_FLIP
-            const u64 m = kind == F_RESET_X ? last : ~0ull;
-            for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) sR[T[t - tb]] ^= m;
-            __syncwarp();
-        }
-    }
-    __syncthreads();
-    for (int64_t i = tid; i < W; i += 32 * FW) R[i * w + k] = sR[i];
+    return lo;
 }
 
-// x / z of every shot from the shared bits: one warp per (row, qubit), lanes
-// over 16-byte word pairs.
-__global__ void __launch_bounds__(256) broadcast_xz_kernel(XZBroadcast bc) {
+// Bits 4 sub .. 4 sub + 3 of a random measurement's 64 outcomes of word k
+// (Philox block `sub`, or the forced bits) -- outcome_bits split over 16
+// lanes, so that one warp draws two measurements at once.
+__device__ __forceinline__ u64 outcome_quarter(const MeasOp &op, int sub, uint64_t seed, uint64_t event_base,
+                                               int64_t k, uint64_t word_base) {
+    u64 bits = 0ull;
+    if (op.forced) {
+        const u64 fw = op.forced[k];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int b = sub * 4 + l;
+            const float u = ((fw >> b) & 1ull) ? 0.25f : 0.75f;
+            if (u < op.bias) bits |= 1ull << b;
+        }
+    } else {
+        const u32x4 u = draw_block(seed, event_base + op.event, word_base + (uint64_t)k, (uint32_t)sub, TAG_MEASURE);
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+            if (unit_float(u.v[l]) < op.bias) bits |= 1ull << (sub * 4 + l);
+    }
+    return bits;
+}
+
+// One CTA of FW warps per shot-word k of a job runs the job's whole sign
+// program on its W signs, held in shared memory from start (all zero: the
+// run starts from |0...0>) to end.  Launch range by launch range:
+//  1. its ops and measurement tab words are copied to shared memory with
+//     cp.async (in flight during 2 and 3); the range's channel records were
+//     fetched the same way during the range before;
+//  2. the channel outcomes of its segment are drawn (the same draws as every
+//     other form) and each outcome flips the signs of its slot's rows;
+//  3. its random measurements' outcomes are drawn (they depend on no sign),
+//     two per warp;
+//  4. its ops run in order: F_LINEAR maps over all threads, other
+//     measurement ops on warp 0 (a window's measurements one per lane, the
+//     rows of other ops over the lanes).
+// So the critical path reads shared memory only, but for one batched fetch
+// of the hit channels' rows per range.  Records are written as they are
+// produced; the signs go back to R at the end.  Record m of a job lives at
+// rec + m*w (results) and rec + (nm + m)*w (determined flags).
+// At most 85 registers a thread (3 CTAs of 8 warps, or 6 of 4, per SM's
+// 64K): two sign CTAs then leave an SM room for the broadcast beside them.
+template <int FW>
+__global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const FrameJobDev *__restrict__ jobs, int njobs,
+                                                                     const int64_t *__restrict__ cta0) {
+    extern __shared__ __align__(16) u64 sm[];
+    constexpr int NT = 32 * FW;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int j = njobs > 1 ? job_of(cta0, njobs, (int64_t)blockIdx.x) : 0;
+    const FrameJobDev &J = jobs[j];
+    const int64_t n = J.n, w = J.w, W = 2 * n + 1, nm = J.nm;
+    const int64_t k = (int64_t)blockIdx.x - cta0[j];
+    const FrameSmem SL = frame_smem_layout(J);
+    char *const sb8 = reinterpret_cast<char *>(sm);
+    u64 *const sR = sm;  // signs, the zero row W, kWinRows sink rows
+    u64 *const sout = reinterpret_cast<u64 *>(sb8 + SL.out);  // a range's random outcomes
+    uint32_t *const stab = reinterpret_cast<uint32_t *>(sb8 + SL.tab);
+    FrameOp *const sops = reinterpret_cast<FrameOp *>(sb8 + SL.ops);
+    u64 *const snew = reinterpret_cast<u64 *>(sb8 + SL.nw);  // F_LINEAR's new rows
+    u64 *const shm = reinterpret_cast<u64 *>(sb8 + SL.hm);   // a chunk of hits: outcome masks (4 a hit)
+    FrameSlotDev *const sslot = reinterpret_cast<FrameSlotDev *>(sb8 + SL.slot);  // [2][max_slots]
+    uint32_t *const srow = reinterpret_cast<uint32_t *>(sb8 + SL.row);    // the chunk's hit rows
+    uint32_t *const sht0 = reinterpret_cast<uint32_t *>(sb8 + SL.t0);     // first row entry of each hit
+    uint32_t *const shpre = reinterpret_cast<uint32_t *>(sb8 + SL.pre);   // first of its rows in the chunk
+    uint32_t *const swsum = reinterpret_cast<uint32_t *>(sb8 + SL.wsum);  // per-warp row counts
+    uint16_t *const sridx = reinterpret_cast<uint16_t *>(sb8 + SL.ridx);  // hit of each staged row
+    uint32_t *const shit = reinterpret_cast<uint32_t *>(sb8 + SL.hit);    // hit channels: count, then the list
+    uint32_t *const shitl = shit + 1;
+    const FrameOp *const gops = J.ops;
+    const uint32_t *const gtab = J.tab;
+    u64 *const rec = J.rec;
+    const RunParams rp = *J.rp;
+    // channel tables: staged once when small, else read where they are
+    const FrameChanTab *ctab = J.ctab;
+    const uint64_t *thr = J.thr;
+    const uint32_t *surv = J.surv;
+    if (J.stage_tabs) {
+        FrameChanTab *c2 = reinterpret_cast<FrameChanTab *>(sb8 + SL.tabs);
+        uint64_t *t2 = reinterpret_cast<uint64_t *>(c2 + J.n_ctab);
+        uint32_t *s2 = reinterpret_cast<uint32_t *>(t2 + J.n_thr);
+        for (uint32_t i = tid; i < J.n_ctab; i += NT) c2[i] = J.ctab[i];
+        for (uint32_t i = tid; i < J.n_thr; i += NT) t2[i] = J.thr[i];
+        for (uint32_t i = tid; i < J.n_surv; i += NT) s2[i] = J.surv[i];
+        ctab = c2;
+        thr = t2;
+        surv = s2;
+    }
+    for (int64_t i = tid; i < W + 1 + (int64_t)kWinRows; i += NT) sR[i] = 0ull;
+    // cp.async groups, in commit order per range li: T(li) (its ops and tab
+    // words), R (hit rows, one group per chunk), S(li+1) (the next range's
+    // channel records, into the other buffer).  S(0) goes first.
+    auto fetch_slots = [&](const FrameRangeDev &R, int buf) {
+        const FrameSlotDev *src = J.slot + R.slot_base;
+        FrameSlotDev *dst = sslot + (size_t)buf * J.max_slots;
+        for (int i = tid; i < R.nslots; i += NT) cp_async16(dst + i, src + i);
+    };
+    FrameRangeDev L = J.ranges[0];
+    fetch_slots(L, 0);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    u64 last = 0ull;  // outcome of the latest measurement (its reset X)
+    for (int li = 0; li < J.nranges; ++li) {
+        const FrameRangeDev Ln = J.ranges[li + 1 < J.nranges ? li + 1 : li];  // in flight meanwhile
+        if (L.stage) {
+            for (uint32_t i = tid; i < L.ntab16; i += NT) cp_async16(stab + 4 * i, gtab + L.tab0a + 4 * i);
+            for (uint32_t i = tid; i < L.op1 - L.op0; i += NT) cp_async16(sops + i, gops + L.op0 + i);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // S(li): every group but T(li)
+        if (tid == 0) *shit = 0u;
+        __syncthreads();
+        const FrameSlotDev *cs = sslot + (size_t)(li & 1) * J.max_slots;
+        // 2. channel outcomes.  A first pass draws every channel's first
+        //    number (one Philox block; no shot of the word is hit unless it
+        //    is at least S_64, 94 % of channels at p = 1e-3) with all lanes
+        //    converged, two channels in flight per thread, and lists the hit
+        //    channels.  The hits are then taken in chunks: one thread per hit
+        //    samples its word (channel_word_surv: the same draws as every
+        //    other form) and fetches its slot's row entries into shared
+        //    memory, then all threads together flip the signs of those rows,
+        //    one row entry per thread (32-bit shared atomics: XORs commute,
+        //    and two slots may share a row).
+        if (L.nslots > 0) {
+            // every lane runs every iteration (the ballots below take the
+            // full warp); channels past the end just report no hit
+            for (int sb = 0; sb < L.nslots; sb += 2 * NT) {
+                bool hit[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int s = sb + tid + u * NT;
+                    hit[u] = false;
+                    if (s < L.nslots) {
+                        const FrameSlotDev d = cs[s];
+                        const uint32_t first =
+                            draw_block(rp.seed, rp.event_base + d.event, rp.word_base + (uint64_t)k, 0u, TAG_NOISE).v[0];
+                        hit[u] = (d.lt & 0xFFFu) != kFrameNoHit && first >= d.s64;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {  // warp-aggregated append
+                    const unsigned b = __ballot_sync(0xffffffffu, hit[u]);
+                    if (b == 0u) continue;
+                    uint32_t base = 0u;
+                    if (lane == 0) base = atomicAdd(shit, (uint32_t)__popc(b));
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (hit[u]) shitl[base + __popc(b & ((1u << lane) - 1u))] = (uint32_t)(sb + tid + u * NT);
+                }
+            }
+            __syncthreads();
+            const uint32_t nhit = *shit;
+            for (uint32_t c0 = 0; c0 < nhit; c0 += NT) {
+                uint32_t len = 0u, t0 = 0u;
+                if (c0 + tid < nhit) {
+                    const FrameSlotDev d = cs[shitl[c0 + tid]];
+                    const FrameChanTab ct = ctab[d.lt & 0xFFFu];
+                    const ChannelWord m = channel_word_surv(rp.seed, rp.event_base + d.event, rp.word_base + (uint64_t)k,
+                                                            thr + ct.thr_off, ct.count, surv + ct.surv_off);
+                    t0 = d.t0;
+                    len = d.lt >> 12;
+                    shm[4 * tid + 0] = m.fxa;
+                    shm[4 * tid + 1] = m.fza;
+                    shm[4 * tid + 2] = m.fxb;
+                    shm[4 * tid + 3] = m.fzb;
+                    sht0[tid] = t0;
+                }
+                // exclusive prefix of the row counts over the chunk
+                uint32_t x = len;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) swsum[wid] = x;
+                __syncthreads();
+                uint32_t woff = 0u, total = 0u;
+#pragma unroll
+                for (int q = 0; q < FW; ++q) {
+                    const uint32_t v = swsum[q];
+                    woff += q < wid ? v : 0u;
+                    total += v;
+                }
+                const uint32_t pre = woff + x - len;
+                shpre[tid] = pre;
+                // this hit's rows into the staging area (as far as it goes)
+                for (uint32_t r = 0; r < len && pre + r < kFrameRowStage; ++r) {
+                    cp_async4(srow + pre + r, gtab + t0 + r);
+                    sridx[pre + r] = (uint16_t)tid;
+                }
+                asm volatile("cp.async.commit_group;\n" ::: "memory");
+                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+                __syncthreads();
+                const uint32_t nh = min((uint32_t)NT, nhit - c0);
+                for (uint32_t e = tid; e < total; e += NT) {
+                    uint32_t h, v;
+                    if (e < kFrameRowStage) {
+                        h = sridx[e];
+                        v = srow[e];
+                    } else {  // past the staging area: the hit by binary search, the row from global memory
+                        uint32_t lo = 0u, hi = nh - 1u;  // the last hit h with shpre[h] <= e
+                        while (lo < hi) {
+                            const uint32_t mid = (lo + hi + 1u) >> 1;
+                            if (shpre[mid] <= e) lo = mid;
+                            else hi = mid - 1u;
+                        }
+                        h = lo;
+                        v = __ldg(gtab + sht0[h] + (e - shpre[h]));
+                    }
+                    const uint32_t sel = v >> 28;
+                    u64 f = 0ull;  // row | sel << 28: X on rows with z, Z on rows with x
+                    if (sel & 1u) f ^= shm[4 * h + 0];
+                    if (sel & 2u) f ^= shm[4 * h + 1];
+                    if (sel & 4u) f ^= shm[4 * h + 2];
+                    if (sel & 8u) f ^= shm[4 * h + 3];
+                    unsigned *rw = reinterpret_cast<unsigned *>(&sR[v & kFrameRowMask]);
+                    if ((uint32_t)f) atomicXor(rw, (uint32_t)f);
+                    if (f >> 32) atomicXor(rw + 1, (uint32_t)(f >> 32));
+                }
+                __syncthreads();  // the chunk applied before the next one overwrites it
+            }
+        }
+        // the next range's channel records, into the buffer range li - 1 used
+        if (li + 1 < J.nranges) fetch_slots(Ln, (li + 1) & 1);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        // 3. random outcomes: half-warps, one Philox block per lane
+        for (uint32_t r0 = 2u * (uint32_t)wid; r0 < L.nrand; r0 += 2u * FW) {
+            const uint32_t r = r0 + (uint32_t)(lane >> 4);
+            u64 bits = 0ull;
+            if (r < L.nrand)
+                bits = outcome_quarter(J.meas[J.rand_meas[L.rand0 + r]], lane & 15, rp.seed, rp.event_base, k,
+                                       rp.word_base);
+#pragma unroll
+            for (int off = 8; off > 0; off >>= 1) bits |= __shfl_xor_sync(0xffffffffu, bits, off);
+            if ((lane & 15) == 0 && r < L.nrand) sout[r] = bits;
+        }
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // T(li): every group but S(li+1)
+        __syncthreads();
+        // 4. the ops
+        const uint32_t *T = L.stage ? stab : gtab;  // measurement-op tab, indexed x - tb
+        const uint32_t tb = L.stage ? L.tab0a : 0u;
+        for (uint32_t oi = L.op0; oi < L.op1; ++oi) {
+            const FrameOp o = L.stage ? sops[oi - L.op0] : gops[oi];
+            const uint32_t kind = o.kind & 0xFFu;
+            if (kind == F_NOISE) continue;  // applied in 2 (always a range's first op)
+            if (kind == F_LINEAR) {
+                // every output from the signs as they were, then the new rows
+                __syncthreads();  // warp 0's measurement ops before
+                const uint32_t *Lm = T + (o.off - tb);
+                const uint32_t nrec = Lm[0], nrow = Lm[1], nlast = Lm[2], nout = nrec + nrow + nlast;
+                const uint32_t *dst = Lm + 4, *beg = dst + nout, *term = beg + nout + 1;
+                for (uint32_t q = tid; q < nout; q += NT) {
+                    const uint32_t d = dst[q], t1 = beg[q + 1];
+                    u64 v = (d & kLinConst) ? ~0ull : 0ull;
+#pragma unroll 4
+                    for (uint32_t t = beg[q]; t < t1; ++t) v ^= sR[term[t]];
+                    if (q < nrec) {
+                        const int64_t m = (int64_t)(d & kLinIndex);
+                        rec[m * w + k] = v;
+                        rec[(nm + m) * w + k] = (d & kLinDet) ? ~0ull : 0ull;
+                    } else {
+                        snew[q - nrec] = v;
+                    }
+                }
+                __syncthreads();
+                for (uint32_t q = tid; q < nrow; q += NT) sR[dst[nrec + q] & kLinIndex] = snew[q];
+                if (nlast) last = snew[nrow];
+                __syncthreads();
+            } else if (wid != 0) {
+                continue;  // the other measurement ops run on warp 0
+            } else if (kind == F_WINDOW) {
+                u64 acc = 0ull;
+                uint32_t rs[kWinRows];
+                if ((uint32_t)lane < o.len) {
+                    const uint32_t *rc = T + (o.off + kWinRec * lane - tb);
+                    const uint32_t m = rc[0], hdr = rc[1];
+                    uint32_t rd[kWinRows];
+#pragma unroll
+                    for (uint32_t t = 0; t < kWinRows; ++t) {
+                        rd[t] = rc[2 + t];
+                        rs[t] = rc[2 + kWinRows + t];
+                    }
+                    acc = (hdr & 1u) ? ~0ull : 0ull;
+#pragma unroll
+                    for (uint32_t t = 0; t < kWinRows; ++t) acc ^= sR[rd[t]];
+                    rec[(int64_t)m * w + k] = acc;
+                    rec[(nm + (int64_t)m) * w + k] = ~0ull;
+                    if ((uint32_t)lane == o.len - 1) sR[2 * n] = acc;
+                }
+                __syncwarp();
+                if ((uint32_t)lane < o.len) {  // a lane's reset rows are distinct, and disjoint from other lanes' (sinks aside)
+                    u64 v[kWinRows];
+#pragma unroll
+                    for (uint32_t t = 0; t < kWinRows; ++t) v[t] = sR[rs[t]];
+#pragma unroll
+                    for (uint32_t t = 0; t < kWinRows; ++t) sR[rs[t]] = v[t] ^ acc;
+                }
+                last = __shfl_sync(0xffffffffu, acc, (int)o.len - 1);
+                __syncwarp();
+            } else if (kind == F_MEAS_DET) {
+                u64 acc = 0ull;
+                for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) acc ^= sR[T[t - tb]];
+                acc = (u64)__reduce_xor_sync(0xffffffffu, (unsigned)(acc >> 32)) << 32 |
+                      (u64)__reduce_xor_sync(0xffffffffu, (unsigned)acc);
+                if (o.kind >> 8) acc = ~acc;
+                if (lane == 0) {
+                    rec[(int64_t)o.arg * w + k] = acc;
+                    rec[(nm + (int64_t)o.arg) * w + k] = ~0ull;
+                    sR[2 * n] = acc;
+                }
+                last = acc;
+                __syncwarp();
+            } else if (kind == F_MEAS_RAND) {
+                const u64 out = sout[o.kind >> 8];
+                const uint32_t p = T[o.off - tb];
+                const u64 rpv = sR[p + n];
+                __syncwarp();
+                if (lane == 0) {
+                    sR[p] = rpv;
+                    sR[p + n] = out;
+                    rec[(int64_t)o.arg * w + k] = out;
+                    rec[(nm + (int64_t)o.arg) * w + k] = 0ull;
+                }
+                // the multiplied rows exclude p and p+n (and are distinct): no barrier needed before them
+                for (uint32_t t = o.off + 1 + lane; t < o.off + o.len; t += 32) {
+                    const uint32_t v = T[t - tb];
+                    sR[v & 0x7FFFFFFFu] ^= rpv ^ ((v >> 31) ? ~0ull : 0ull);
+                }
+                last = out;
+                __syncwarp();
+            } else {  // F_RESET_X, F_FLIP
+                const u64 m = kind == F_RESET_X ? last : ~0ull;
+                for (uint32_t t = o.off + lane; t < o.off + o.len; t += 32) sR[T[t - tb]] ^= m;
+                __syncwarp();
+            }
+        }
+        __syncthreads();  // the range's ops done before the next range's staging and channel flips
+        L = Ln;
+    }
+    for (int64_t i = tid; i < W; i += NT) J.R[i * w + k] = sR[i];
+}
+
+// x / z of every shot from the shared bits.  A warp takes one chunk: one
+// (row, qubit) pair of a job whose rows are at least 32 words wide (lanes
+// over 16-byte word pairs), or 32 / (w/2) pairs of a narrower one.  Chunks
+// of a job are consecutive (chunk0).
+__global__ void __launch_bounds__(256) broadcast_jobs_kernel(const BroadcastJobDev *__restrict__ jobs, int njobs,
+                                                             const int64_t *__restrict__ chunk0, int64_t chunks) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t rq = bc.rq0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rq < bc.rq1; rq += warps)
-        broadcast_row_column(bc, rq, lane);
+    for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks; c += warps) {
+        const int j = njobs > 1 ? job_of(chunk0, njobs, c) : 0;
+        const BroadcastJobDev &B = jobs[j];
+        const int64_t hw = B.w >> 1, pairs = (2 * B.n + 1) * B.n, local = c - chunk0[j];
+        int64_t rq, kp0, step;
+        if (hw >= 16) {
+            rq = local;
+            kp0 = lane;
+            step = 32;
+        } else {
+            const int per = 32 / (int)hw;
+            rq = local * per + lane / (int)hw;
+            kp0 = lane % (int)hw;
+            step = hw;
+            if (lane >= per * (int)hw || rq >= pairs) continue;
+        }
+        const int64_t row = rq / B.n, q = rq - row * B.n;
+        const u64 xb = (B.xz[(row * 2 + 0) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+        const u64 zb = (B.xz[(row * 2 + 1) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+        const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
+        u64 *xo = B.X + rq * B.w, *zo = B.Z + rq * B.w;
+        // streaming stores (evict first): the broadcast passes 1.65 GB through
+        // L2 at d = 15 and must not evict the sign kernel's tables beside it
+        for (int64_t kp = kp0; kp < hw; kp += step) {
+            __stcs(reinterpret_cast<ulonglong2 *>(xo + 2 * kp), xv);
+            __stcs(reinterpret_cast<ulonglong2 *>(zo + 2 * kp), zv);
+        }
+    }
 }
 
 int g_frame_sms = 0;
 int g_prio_greatest = 1;  // 1: not looked up yet (priorities are <= 0)
-int g_prio_least = 1;
+
+// Both kernels of a run ask for the largest shared-memory carveout.  An SM
+// changes its L1 / shared split only when it is idle, so a broadcast left to
+// the default (no shared memory, an L1-heavy split) keeps the sign kernel's
+// CTAs off every SM it occupies until it drains.
+int same_carveout(const void *kernel) {
+    static std::mutex mu;
+    static std::set<std::pair<const void *, int>> done;
+    int dev = 0;
+    PS_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({kernel, dev})) return OK;
+    PS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared));
+    done.insert({kernel, dev});
+    return OK;
+}
+
+template <int FW>
+int launch_frame_fw(cudaStream_t st, const FrameTable &t) {
+    if (t.smem > 48 * 1024) {
+        const int rc = allow_max_smem((const void *)frame_run_kernel<FW>);
+        if (rc != OK) return rc;
+    }
+    {
+        const int rc = same_carveout((const void *)frame_run_kernel<FW>);
+        if (rc != OK) return rc;
+    }
+    // The sign kernel is the plan's critical path: launched at the highest
+    // priority, its CTAs go ahead of the broadcast's queued CTAs.
+    if (g_prio_greatest == 1) {
+        int least = 0, greatest = 0;
+        PS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        g_prio_greatest = greatest;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)t.ctas);
+    cfg.blockDim = dim3(32 * FW);
+    cfg.dynamicSmemBytes = t.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = g_prio_greatest;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PS_CUDA(cudaLaunchKernelEx(&cfg, frame_run_kernel<FW>, t.jobs, (int)t.njobs, t.cta0));
+    PS_CUDA(cudaGetLastError());
+    return OK;
+}
 
 }  // namespace
 
@@ -232,79 +469,32 @@ size_t frame_smem_bytes(int64_t n) {  // rows, the zero row, kWinRows sink rows
     return (size_t)(2 * n + 2 + kWinRows) * sizeof(u64);
 }
 
-int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
-                 const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,
-                 uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
-                 int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero,
-                 int noise_first, uint32_t scratch) {
-    // Staging keeps a CTA's shared memory small enough for two per SM.  The
-    // staged tab range starts at tab0 rounded down to 16 bytes (tab holds
-    // padding after its last word for the rounded-up end).  The F_LINEAR
-    // scratch (new rows) comes last.
-    const size_t base = ((frame_smem_bytes(n) + (size_t)nrand * sizeof(u64)) + 15) / 16 * 16;
-    const uint32_t tab0a = tab0 & ~3u, tab1a = (tab1 + 3u) & ~3u;
-    const size_t scr = (size_t)scratch * sizeof(u64);
-    const size_t staged = base + (size_t)(tab1a - tab0a) * 4 + (size_t)(op1 - op0) * sizeof(FrameOp) + scr;
-    const int stage = staged <= kFrameStageMax ? 1 : 0;
-    const size_t smem = stage ? staged : base + scr;
-    if (smem > kSegSmemMax) return E_ARG;
-    const uint32_t ntab16 = stage ? (tab1a - tab0a) / 4 : 0u;
-    if (smem > 48 * 1024) {
-        const int rc = allow_max_smem((const void *)frame_kernel);
-        if (rc != OK) return rc;
+int launch_frame_run(cudaStream_t st, const FrameTable &t, int warps) {
+    if (t.njobs <= 0 || t.ctas <= 0) return OK;
+    if (t.smem > kSegSmemMax) return fail(E_ARG, "sign program does not fit in shared memory");
+    if (t.ctas > 0x7FFFFFFFll) return fail(E_ARG, "sign program: too many shot-words in one launch");
+    switch (warps) {
+    case 4: return launch_frame_fw<4>(st, t);
+    case 0:
+    case 8: return launch_frame_fw<8>(st, t);
+    default: return fail(E_ARG, "sign kernel: 4 or 8 warps per CTA");
     }
-    // The sign kernels are the plan's critical path: launched at the highest
-    // priority, their CTAs go ahead of the side streams' queued sampling and
-    // broadcast CTAs.
-    if (g_prio_greatest == 1) {
-        int least = 0, greatest = 0;
-        PS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        g_prio_greatest = greatest;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)w);
-    cfg.blockDim = dim3(32 * FW);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributePriority;
-    attr[0].val.priority = g_prio_greatest;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    PS_CUDA(cudaLaunchKernelEx(&cfg, frame_kernel, R, n, w, ops, op0, op1, tab, tab0a, ntab16, stage, slot_off, rand_meas,
-                               nrand, meas, rec, nm, entries, entry_count, cap, seed, rp, from_zero, noise_first));
-    PS_CUDA(cudaGetLastError());
-    return OK;
 }
 
-int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc, bool yield) {
-    if (bc.rq1 <= bc.rq0) return OK;
+int launch_broadcast_jobs(cudaStream_t st, const FrameTable &t, int ctas_per_sm) {
+    if (t.njobs <= 0 || t.chunks <= 0) return OK;
     if (g_frame_sms == 0) {
         int dev = 0;
         PS_CUDA(cudaGetDevice(&dev));
         PS_CUDA(cudaDeviceGetAttribute(&g_frame_sms, cudaDevAttrMultiProcessorCount, dev));
     }
-    if (g_prio_least == 1) {
-        int least = 0, greatest = 0;
-        PS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        g_prio_least = least;
+    {
+        const int rc = same_carveout((const void *)broadcast_jobs_kernel);
+        if (rc != OK) return rc;
     }
-    // yield: one (row, qubit) pair per warp, so that CTAs retire within
-    // microseconds and the kernels beside it (the sign program, launched at
-    // the highest priority) get every SM slot that frees up; otherwise a
-    // grid of 8 CTAs per SM walking the pairs.
-    const int64_t pairs = bc.rq1 - bc.rq0;
-    const int64_t blocks = yield ? (pairs + 7) / 8 : std::min<int64_t>((pairs + 7) / 8, (int64_t)g_frame_sms * 8);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)blocks);
-    cfg.blockDim = dim3(256);
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributePriority;
-    attr[0].val.priority = g_prio_least;
-    cfg.attrs = attr;
-    cfg.numAttrs = yield ? 1 : 0;
-    PS_CUDA(cudaLaunchKernelEx(&cfg, broadcast_xz_kernel, bc));
+    const int per = ctas_per_sm > 0 ? ctas_per_sm : 2;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((t.chunks + 7) / 8, (int64_t)g_frame_sms * per));
+    broadcast_jobs_kernel<<<(unsigned)blocks, 256, 0, st>>>(t.bjobs, t.njobs, t.chunk0, t.chunks);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

@@ -33,7 +33,7 @@
 namespace ps {
 
 enum FrameKind : uint32_t {
-    F_NOISE = 0,      // entries of segment `arg` (sampled just before): tab rows per slot
+    F_NOISE = 0,      // segment noise, the range's first op: arg = slot_off index of its first slot
     F_MEAS_DET = 1,   // arg = MeasOp; tab[off..off+len) rows; kind bit 8 = constant (more rows than a window record holds)
     F_MEAS_RAND = 2,  // arg = MeasOp; tab[off] = p, then rows | c << 31; kind >> 8 = its index in the launch's random list
     F_RESET_X = 3,    // R[row] ^= outcome of the last measurement, rows tab[off..off+len)
@@ -107,31 +107,6 @@ struct FrameProgram {
     std::vector<int32_t> rand_meas;
     std::vector<Launch> launches;
 };
-
-// A range [rq0, rq1) of (row, qubit) pairs of the x / z broadcast: X and Z
-// of every shot-word := the shared bits xz ([W][2][nw64]).  The sampling
-// launches of a run share the broadcast out between them.
-struct XZBroadcast {
-    unsigned long long *X = nullptr, *Z = nullptr;
-    const uint64_t *xz = nullptr;
-    int64_t n = 0, w = 0, nw64 = 0, rq0 = 0, rq1 = 0;
-};
-
-#ifdef __CUDACC__
-// One warp writes (row, qubit) rq of X and Z for every shot-word, 16 bytes
-// per lane and store (w is even).
-__device__ __forceinline__ void broadcast_row_column(const XZBroadcast &bc, int64_t rq, int lane) {
-    const int64_t row = rq / bc.n, q = rq - row * bc.n;
-    const unsigned long long xb = (bc.xz[(row * 2 + 0) * bc.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-    const unsigned long long zb = (bc.xz[(row * 2 + 1) * bc.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-    const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
-    unsigned long long *xo = bc.X + rq * bc.w, *zo = bc.Z + rq * bc.w;
-    for (int64_t kp = lane; kp < bc.w / 2; kp += 32) {
-        *reinterpret_cast<ulonglong2 *>(xo + 2 * kp) = xv;
-        *reinterpret_cast<ulonglong2 *>(zo + 2 * kp) = zv;
-    }
-}
-#endif
 
 // Host-side simulation of the shared x / z bits and emission of the sign
 // program.  Calls follow the circuit's program order.

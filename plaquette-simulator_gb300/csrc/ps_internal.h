@@ -153,34 +153,14 @@ constexpr size_t kSegSmemMax = 227 * 1024;
 // slot_tags: entries carry their slot index instead of their layer.
 int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
                         int slot_tags = 0);
-// Shared-x/z runs: one-pass sampling into unordered per-word lists, each
-// outcome tagged with its slot's rows slot_off[base + s] .. [base + s + 1]
-// (the counters must be zero before; the sign kernel zeroes them after).
-// bc: the share of the x / z broadcast this launch writes (bc.X null: none).
-struct XZBroadcast;
-int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
-                              const uint32_t *slot_off, uint32_t base, const XZBroadcast &bc);
 int launch_segment(cudaStream_t stream, u64 *X, u64 *Z, u64 *R, int64_t n, int64_t w, const SegmentDev &seg,
                    int rows, int bw, int threads, const u64 *const *recs);
 
-// ps_frame.cu (shared-x/z runs)
-struct FrameOp;
-struct NoiseEntry;
+// ps_frame.cu (shared-x/z runs; the launches are declared in ps_frame_dev.h)
 size_t frame_smem_bytes(int64_t n);
-// Ops [op0, op1) of a sign program over every shot-word's signs R (from_zero:
-// the signs start at 0, the tableau having just been reset).
-// tab[tab0, tab1): the measurement ops' rows, staged in shared memory when
-// they fit (kFrameStageMax); rec: the circuit's record block.
+// Staging buffers of a sign program's ranges stay within this (beside the
+// signs); ranges that need more read their ops from global memory.
 constexpr size_t kFrameStageMax = 100 * 1024;
-// rand_meas[0, nrand): MeasOp indices of the launch's random measurements.
-int launch_frame(cudaStream_t st, u64 *R, int64_t n, int64_t w, const FrameOp *ops, uint32_t op0, uint32_t op1,
-                 const uint32_t *tab, uint32_t tab0, uint32_t tab1, const uint32_t *slot_off, const int32_t *rand_meas,
-                 uint32_t nrand, const MeasOp *meas, u64 *rec, int64_t nm, const NoiseEntry *entries,
-                 int32_t *entry_count, int32_t cap, uint64_t seed, const RunParams *rp, int from_zero,
-                 int noise_first, uint32_t scratch);
-// X, Z of every shot := the shared bits, (row, qubit) pairs [bc.rq0, bc.rq1);
-// yield: short CTAs at the lowest priority, for a launch beside other work.
-int launch_broadcast_xz(cudaStream_t st, const XZBroadcast &bc, bool yield);
 
 // ps_gates.cu (compiled-circuit form of the per-op kernels)
 int launch_channel_rp(cudaStream_t stream, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,

@@ -79,50 +79,6 @@ __global__ void __launch_bounds__(128) noise_compact_kernel(SegmentDev seg, int6
     if (lane == 0) seg.entry_count[k] = count;
 }
 
-// Channel sampling for shared-x/z runs, in one pass: one thread per
-// (channel slot, word) draws the word's outcomes (channel_word, the same
-// draws as the two-pass sampler) and appends a non-identity outcome to the
-// word's list with an atomic counter.  The list is unordered -- outcomes are
-// XORs -- and carries, instead of the slot, the slot's rows in the sign
-// program (slot_off[base + s] .. [base + s + 1]) cut into chunks of at most
-// kFrameChunk: one entry per chunk, layer = its first row entry, a = its row
-// count, so no consumer walks a long list alone.  The counter is zeroed by
-// the sign kernel that consumes the list.  Every warp then writes its share
-// of the x / z broadcast (one (row, qubit) pair at a time, all lanes).
-__global__ void __launch_bounds__(256) noise_frame_kernel(SegmentDev seg, int64_t w, const RunParams *__restrict__ rp,
-                                                          const uint32_t *__restrict__ slot_off, uint32_t base,
-                                                          XZBroadcast bc) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int s = (int)(t / w);
-    const int64_t k = t - (int64_t)s * w;
-    if (s < seg.nslots) {
-        const NoiseSlot sl = seg.slots[s];
-        const ChannelWord m = channel_word(rp->seed, rp->event_base + sl.event, rp->word_base + (uint64_t)k,
-                                           seg.thr + sl.thr_off, sl.count);
-        const uint32_t t0 = slot_off[base + s], t1 = slot_off[base + s + 1];
-        const int nch = (int)((t1 - t0 + kFrameChunk - 1) / kFrameChunk);
-        if ((m.fxa | m.fza | m.fxb | m.fzb) != 0ull && nch > 0) {
-            int pos = atomicAdd(&seg.entry_count[k], nch);
-            NoiseEntry e;
-            e.fxa = m.fxa;
-            e.fza = m.fza;
-            e.fxb = m.fxb;
-            e.fzb = m.fzb;
-            e.b = 0;
-            for (uint32_t c0 = t0; c0 < t1; c0 += kFrameChunk, ++pos) {
-                e.layer = (int32_t)c0;
-                e.a = (uint16_t)min((uint32_t)kFrameChunk, t1 - c0);
-                seg.entries[k * (int64_t)seg.cap + pos] = e;
-            }
-        }
-    }
-    if (!bc.X) return;
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t rq = bc.rq0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); rq < bc.rq1; rq += warps)
-        broadcast_row_column(bc, rq, lane);
-}
-
 // Tile cell: x and z of one (row, word, column) side by side, so a gate
 // reads / writes a column with one 16-byte shared-memory access.
 typedef ulonglong2 XZ;
@@ -758,15 +714,6 @@ int launch_noise_sample(cudaStream_t stream, const SegmentDev &seg, int64_t w, c
     PS_CUDA(cudaGetLastError());
     const int wpb = 4;
     noise_compact_kernel<<<(unsigned)((w + wpb - 1) / wpb), 32 * wpb, 0, stream>>>(seg, w, slot_tags);
-    PS_CUDA(cudaGetLastError());
-    return OK;
-}
-
-int launch_noise_sample_frame(cudaStream_t stream, const SegmentDev &seg, int64_t w, const RunParams *rp,
-                              const uint32_t *slot_off, uint32_t base, const XZBroadcast &bc) {
-    if (seg.nslots == 0) return OK;
-    const int64_t threads = (int64_t)seg.nslots * w;
-    noise_frame_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(seg, w, rp, slot_off, base, bc);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

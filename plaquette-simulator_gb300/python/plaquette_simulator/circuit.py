@@ -27,7 +27,8 @@ from .simulator import CliffordState, _ptr
 class CircuitOptions(C.Structure):
     _fields_ = [("mode", C.c_int32), ("use_graph", C.c_int32), ("seg_rows", C.c_int32),
                 ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32),
-                ("seg_resident", C.c_int32), ("per_shot_xz", C.c_int32)]
+                ("seg_resident", C.c_int32), ("per_shot_xz", C.c_int32), ("frame_warps", C.c_int32),
+                ("bcast_ctas", C.c_int32)]
 
 
 class CircuitStats(C.Structure):
@@ -45,7 +46,8 @@ class CircuitStats(C.Structure):
 class CompiledCircuit:
     def __init__(self, circuit: Circuit, state: CliffordState, fused: bool = True, graph: bool = True,
                  seg_rows: int = 0, seg_words: int = 0, seg_threads: int = 0, meas_words: int = 0,
-                 resident: bool = False, word_vector: bool = False, shared_xz: bool = True):
+                 resident: bool = False, word_vector: bool = False, shared_xz: bool = True,
+                 frame_warps: int = 0, bcast_ctas: int = 0):
         if circuit.num_qubits != state.get_num_qubits():
             raise ValueError("circuit and state have different qubit counts")
         self._L = _lib.load()
@@ -54,7 +56,8 @@ class CompiledCircuit:
         self._ops = np.ascontiguousarray(circuit.op_array(), dtype=np.int32)
         self._params = np.ascontiguousarray(circuit.param_array(), dtype=np.float32)
         opts = CircuitOptions(1 if fused else 0, 1 if graph else 0, seg_rows, seg_words, seg_threads, meas_words,
-                              2 if word_vector else (1 if resident else 0), 0 if shared_xz else 1)
+                              2 if word_vector else (1 if resident else 0), 0 if shared_xz else 1, frame_warps,
+                              bcast_ctas)
         h = C.c_void_p()
         check(self._L.ps_circuit_compile(state.handle, _ptr(self._ops), len(self._ops), _ptr(self._params),
                                          len(self._params), C.byref(opts), C.byref(h)))

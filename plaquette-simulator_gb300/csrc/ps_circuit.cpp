@@ -830,7 +830,12 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
                 if (it == table_of.end()) {
                     if (ctabs.size() >= kFrameMaxTables) return fail(E_ARG, "shared-x/z plan: too many channel tables");
                     it = table_of.emplace(sl.thr_off, (uint32_t)ctabs.size()).first;
-                    ctabs.push_back(FrameChanTab{sl.thr_off, sl.count, (uint32_t)surv.size(), 0u});
+                    FrameChanTab ct{};
+                    ct.thr_off = sl.thr_off;
+                    ct.count = sl.count;
+                    ct.surv_off = (uint32_t)surv.size();
+                    ct.est = channel_est_factors(c->thr_host[(size_t)(sl.thr_off + sl.count - 1)], sl.count);
+                    ctabs.push_back(ct);
                     surv.resize(surv.size() + 64);
                     channel_surv_table(c->thr_host[(size_t)(sl.thr_off + sl.count - 1)], &surv[surv.size() - 64]);
                 }
@@ -868,7 +873,7 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
     job.n_ctab = (uint32_t)ctabs.size();
     job.n_thr = (uint32_t)c->thr_host.size();
     job.n_surv = (uint32_t)surv.size();
-    job.stage_tabs = (size_t)job.n_ctab * 16 + (size_t)job.n_thr * 8 + (size_t)job.n_surv * 4 <= kFrameTabStage ? 1u : 0u;
+    job.stage_tabs = (size_t)job.n_ctab * sizeof(FrameChanTab) + (size_t)job.n_thr * 8 + (size_t)job.n_surv * 4 <= kFrameTabStage ? 1u : 0u;
     // staging: drop the largest staged range until the buffers fit
     std::vector<char> on(ranges.size(), 1);
     for (;;) {

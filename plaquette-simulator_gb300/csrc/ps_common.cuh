@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
 #include <string>
 
 typedef unsigned long long u64;
@@ -195,6 +196,81 @@ PS_HD ChannelWord channel_word_surv(uint64_t seed, uint64_t event, uint64_t word
         ++i;
         int idx = 1;
         while (v >= thr[idx - 1]) ++idx;
+        const u64 bit = 1ull << pos;
+        const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
+        if (pa == 1 || pa == 2) m.fxa |= bit;
+        if (pa == 2 || pa == 3) m.fza |= bit;
+        if (pb == 1 || pb == 2) m.fxb |= bit;
+        if (pb == 2 || pb == 3) m.fzb |= bit;
+        if (++pos == 64) return m;
+        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
+        u = block_lane(blk, i & 3u);
+        ++i;
+    }
+}
+
+// Float estimates for channel_word_est: the gap to the next hit is near
+// log2(u / 2^32) / log2(q / 2^32) - 1 (S_{j+1} is about 2^32 (q / 2^32)^(j+1)),
+// and the Pauli index near v count / total.  channel_est_factors gives the
+// two factors of a table.
+struct ChannelEst {
+    float inv_lq;  // 1 / (log2(q) - 32), q = 2^32 - total
+    float kmul;    // count / total
+};
+inline ChannelEst channel_est_factors(uint64_t total, int count) {
+    ChannelEst e;
+    const double q = 4294967296.0 - (double)total;
+    e.inv_lq = q > 0.0 ? (float)(1.0 / (std::log2(q) - 32.0)) : 0.0f;
+    e.kmul = total > 0 ? (float)((double)count / (double)total) : 0.0f;
+    return e;
+}
+
+// channel_word with both searches started from the float estimates and
+// settled on the integer tables: the first j in [0, lim) with u >= surv[j]
+// (surv = channel_surv_table), and the first k with v < thr[k].  Whatever
+// the estimate, the two correcting walks end on the same index as the
+// stepped search, so the outcomes are channel_word's bit for bit; a close
+// estimate only makes the walks short.
+PS_HD int channel_first_at_least(uint32_t u, const uint32_t *surv, int lim, int g) {
+    g = g < 0 ? 0 : (g > lim ? lim : g);
+    while (g > 0 && u >= surv[g - 1]) --g;
+    while (g < lim && u < surv[g]) ++g;
+    return g;
+}
+PS_HD int channel_first_above(uint64_t v, const uint64_t *thr, int count, int k) {
+    k = k < 0 ? 0 : (k > count - 1 ? count - 1 : k);
+    while (k > 0 && v < thr[k - 1]) --k;
+    while (v >= thr[k]) ++k;  // stops at count - 1 at the latest: v < total = thr[count - 1]
+    return k;
+}
+PS_HD float channel_log2(float x) {
+#ifdef __CUDA_ARCH__
+    return __log2f(x);
+#else
+    return std::log2(x);
+#endif
+}
+PS_HD ChannelWord channel_word_est(uint64_t seed, uint64_t event, uint64_t word, const uint64_t *thr, int count,
+                                   const uint32_t *surv, ChannelEst est) {
+    ChannelWord m{0ull, 0ull, 0ull, 0ull};
+    const uint64_t total = thr[count - 1];
+    if (total == 0) return m;
+    u32x4 blk = draw_block(seed, event, word, 0u, TAG_NOISE);
+    uint32_t u = blk.v[0];
+    if ((uint64_t)u < thr[count]) return m;  // no shot of the word is hit
+    uint32_t i = 1;  // the next draw
+    int pos = 0;     // the first shot not sampled yet
+    for (;;) {
+        const float L = (channel_log2((float)u) - 32.0f) * est.inv_lq;  // u = 0: +inf, clamped
+        const int ge = L >= 0.0f ? (L < 80.0f ? (int)ceilf(L) - 1 : 80) : 0;
+        const int lim = 64 - pos;
+        const int g = channel_first_at_least(u, surv, lim, ge);
+        if (g == lim) return m;
+        pos += g;
+        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
+        const uint64_t v = ((uint64_t)block_lane(blk, i & 3u) * total) >> 32;
+        ++i;
+        const int idx = 1 + channel_first_above(v, thr, count, (int)((float)v * est.kmul));
         const u64 bit = 1ull << pos;
         const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
         if (pa == 1 || pa == 2) m.fxa |= bit;

@@ -96,10 +96,8 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
     u64 *const shm = reinterpret_cast<u64 *>(sb8 + SL.hm);   // a chunk of hits: outcome masks (4 a hit)
     FrameSlotDev *const sslot = reinterpret_cast<FrameSlotDev *>(sb8 + SL.slot);  // [2][max_slots]
     uint32_t *const srow = reinterpret_cast<uint32_t *>(sb8 + SL.row);    // the chunk's hit rows
-    uint32_t *const sht0 = reinterpret_cast<uint32_t *>(sb8 + SL.t0);     // first row entry of each hit
-    uint32_t *const shpre = reinterpret_cast<uint32_t *>(sb8 + SL.pre);   // first of its rows in the chunk
-    uint32_t *const swsum = reinterpret_cast<uint32_t *>(sb8 + SL.wsum);  // per-warp row counts
     uint16_t *const sridx = reinterpret_cast<uint16_t *>(sb8 + SL.ridx);  // hit of each staged row
+    uint32_t *const srcnt = reinterpret_cast<uint32_t *>(sb8 + SL.cnt);   // staged rows taken
     uint32_t *const shit = reinterpret_cast<uint32_t *>(sb8 + SL.hit);    // hit channels: count, then the list
     uint32_t *const shitl = shit + 1;
     const FrameOp *const gops = J.ops;
@@ -149,10 +147,10 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
         //    number (one Philox block; no shot of the word is hit unless it
         //    is at least S_64, 94 % of channels at p = 1e-3) with all lanes
         //    converged, two channels in flight per thread, and lists the hit
-        //    channels.  The hits are then taken in chunks: one thread per hit
-        //    samples its word (channel_word_surv: the same draws as every
-        //    other form) and fetches its slot's row entries into shared
-        //    memory, then all threads together flip the signs of those rows,
+        //    channels.  The hits are then taken in chunks: a thread per hit
+        //    fetches its slot's row entries into shared memory and samples
+        //    its word (channel_word_est: the same draws as every other
+        //    form), then all threads together flip the signs of those rows,
         //    one row entry per thread (32-bit shared atomics: XORs commute,
         //    and two slots may share a row).
         if (L.nslots > 0) {
@@ -184,63 +182,51 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
             __syncthreads();
             const uint32_t nhit = *shit;
             for (uint32_t c0 = 0; c0 < nhit; c0 += NT) {
-                uint32_t len = 0u, t0 = 0u;
-                if (c0 + tid < nhit) {
-                    const FrameSlotDev d = cs[shitl[c0 + tid]];
-                    const FrameChanTab ct = ctab[d.lt & 0xFFFu];
-                    const ChannelWord m = channel_word_surv(rp.seed, rp.event_base + d.event, rp.word_base + (uint64_t)k,
-                                                            thr + ct.thr_off, ct.count, surv + ct.surv_off);
-                    t0 = d.t0;
-                    len = d.lt >> 12;
-                    shm[4 * tid + 0] = m.fxa;
-                    shm[4 * tid + 1] = m.fza;
-                    shm[4 * tid + 2] = m.fxb;
-                    shm[4 * tid + 3] = m.fzb;
-                    sht0[tid] = t0;
-                }
-                // exclusive prefix of the row counts over the chunk
-                uint32_t x = len;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                    if (lane >= o) x += y;
-                }
-                if (lane == 31) swsum[wid] = x;
+                const uint32_t cend = min(nhit, c0 + (uint32_t)NT);
+                if (tid == 0) *srcnt = 0u;
                 __syncthreads();
-                uint32_t woff = 0u, total = 0u;
-#pragma unroll
-                for (int q = 0; q < FW; ++q) {
-                    const uint32_t v = swsum[q];
-                    woff += q < wid ? v : 0u;
-                    total += v;
-                }
-                const uint32_t pre = woff + x - len;
-                shpre[tid] = pre;
-                // this hit's rows into the staging area (as far as it goes)
-                for (uint32_t r = 0; r < len && pre + r < kFrameRowStage; ++r) {
-                    cp_async4(srow + pre + r, gtab + t0 + r);
-                    sridx[pre + r] = (uint16_t)tid;
+                // one thread per hit, spread over the warps (chunk hit l on
+                // lane l / FW of warp l % FW): it fetches the hit slot's rows
+                // into the staging area first, then samples the word
+                const uint32_t l = (uint32_t)lane * FW + (uint32_t)wid, h = c0 + l;
+                if (h < cend) {
+                    const FrameSlotDev d = cs[shitl[h]];
+                    const uint32_t len = d.lt >> 12, t0 = d.t0;
+                    const uint32_t pos = atomicAdd(srcnt, len);
+                    const bool staged = pos + len <= kFrameRowStage;
+                    for (uint32_t r = 0; r < len && pos + r < kFrameRowStage; ++r) {
+                        if (staged) cp_async4(srow + pos + r, gtab + t0 + r);
+                        sridx[pos + r] = staged ? (uint16_t)l : (uint16_t)0xFFFFu;  // 0xFFFF: skip
+                    }
+                    const FrameChanTab ct = ctab[d.lt & 0xFFFu];
+                    const ChannelWord m = channel_word_est(rp.seed, rp.event_base + d.event, rp.word_base + (uint64_t)k,
+                                                           thr + ct.thr_off, ct.count, surv + ct.surv_off, ct.est);
+                    shm[4 * l + 0] = m.fxa;
+                    shm[4 * l + 1] = m.fza;
+                    shm[4 * l + 2] = m.fxb;
+                    shm[4 * l + 3] = m.fzb;
+                    if (!staged) {  // rows that do not fit: applied now, from global memory
+                        for (uint32_t r = 0; r < len; ++r) {
+                            const uint32_t v = __ldg(gtab + t0 + r), sel = v >> 28;
+                            u64 f = 0ull;
+                            if (sel & 1u) f ^= m.fxa;
+                            if (sel & 2u) f ^= m.fza;
+                            if (sel & 4u) f ^= m.fxb;
+                            if (sel & 8u) f ^= m.fzb;
+                            unsigned *rw = reinterpret_cast<unsigned *>(&sR[v & kFrameRowMask]);
+                            if ((uint32_t)f) atomicXor(rw, (uint32_t)f);
+                            if (f >> 32) atomicXor(rw + 1, (uint32_t)(f >> 32));
+                        }
+                    }
                 }
                 asm volatile("cp.async.commit_group;\n" ::: "memory");
                 asm volatile("cp.async.wait_group 0;\n" ::: "memory");
                 __syncthreads();
-                const uint32_t nh = min((uint32_t)NT, nhit - c0);
-                for (uint32_t e = tid; e < total; e += NT) {
-                    uint32_t h, v;
-                    if (e < kFrameRowStage) {
-                        h = sridx[e];
-                        v = srow[e];
-                    } else {  // past the staging area: the hit by binary search, the row from global memory
-                        uint32_t lo = 0u, hi = nh - 1u;  // the last hit h with shpre[h] <= e
-                        while (lo < hi) {
-                            const uint32_t mid = (lo + hi + 1u) >> 1;
-                            if (shpre[mid] <= e) lo = mid;
-                            else hi = mid - 1u;
-                        }
-                        h = lo;
-                        v = __ldg(gtab + sht0[h] + (e - shpre[h]));
-                    }
-                    const uint32_t sel = v >> 28;
+                const uint32_t nst = min(*srcnt, kFrameRowStage);
+                for (uint32_t e = tid; e < nst; e += NT) {
+                    const uint32_t h = sridx[e];
+                    if (h == 0xFFFFu) continue;
+                    const uint32_t v = srow[e], sel = v >> 28;
                     u64 f = 0ull;  // row | sel << 28: X on rows with z, Z on rows with x
                     if (sel & 1u) f ^= shm[4 * h + 0];
                     if (sel & 2u) f ^= shm[4 * h + 1];

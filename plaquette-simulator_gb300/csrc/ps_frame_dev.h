@@ -24,20 +24,23 @@ constexpr uint32_t kFrameNoHit = 4095;
 constexpr uint32_t kFrameMaxTables = 4095;
 constexpr uint32_t kFrameMaxSlotRows = (1u << 20) - 1;
 
-// A distinct channel table: thresholds at thr + thr_off (count + 1 entries)
-// and survival products at surv + surv_off (channel_surv_table).
+// A distinct channel table: thresholds at thr + thr_off (count + 1 entries),
+// survival products at surv + surv_off (channel_surv_table) and the factors
+// of the sampler's estimates (channel_est_factors).
 struct FrameChanTab {
     int32_t thr_off;
     int32_t count;
     uint32_t surv_off;
     uint32_t pad;
+    ChannelEst est;
+    uint32_t pad2[2];
 };
 
 // Hits of a range's channels are sampled and applied in chunks of at most
-// this many (one per thread of an 8-warp CTA); the rows of a chunk's hits
-// are fetched into shared memory up to kFrameRowStage entries (the rest are
-// read from global memory); the channel tables are staged in shared memory
-// when they take at most kFrameTabStage bytes.
+// this many; the rows of a chunk's hits are fetched into shared memory up to
+// kFrameRowStage entries (a hit whose rows do not fit applies them from
+// global memory); the channel tables are staged in shared memory when they
+// take at most kFrameTabStage bytes.
 constexpr uint32_t kFrameHitChunk = 256;
 constexpr uint32_t kFrameRowStage = 2048;
 constexpr uint32_t kFrameTabStage = 4096;
@@ -86,10 +89,10 @@ struct FrameJobDev {
 // signs (W rows, the zero row, kWinRows sink rows), random outcomes, staged
 // tab words, staged ops, F_LINEAR's new rows, a chunk of hits' outcome
 // masks, two buffers of channel records (the range's, the next one's being
-// fetched), the channel tables, the hit rows, the chunk's first row entries
-// and prefix, per-warp sums, the hit index of each staged row, the hit list.
+// fetched), the channel tables, the hit rows and the hit of each (u16), the
+// staged-row count, the hit list.
 struct FrameSmem {
-    size_t out, tab, ops, nw, hm, slot, tabs, row, t0, pre, wsum, ridx, hit, total;
+    size_t out, tab, ops, nw, hm, slot, tabs, row, ridx, cnt, hit, total;
 };
 __host__ __device__ inline size_t frame_align16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline FrameSmem frame_smem_layout(const FrameJobDev &j) {
@@ -101,12 +104,10 @@ __host__ __device__ inline FrameSmem frame_smem_layout(const FrameJobDev &j) {
     L.hm = frame_align16(L.nw + (size_t)j.max_scratch * 8);
     L.slot = L.hm + (size_t)kFrameHitChunk * 32;
     L.tabs = L.slot + (size_t)2 * j.max_slots * 16;
-    L.row = frame_align16(L.tabs + (j.stage_tabs ? (size_t)j.n_ctab * 16 + (size_t)j.n_thr * 8 + (size_t)j.n_surv * 4 : 0));
-    L.t0 = L.row + (size_t)kFrameRowStage * 4;
-    L.pre = L.t0 + (size_t)kFrameHitChunk * 4;
-    L.wsum = L.pre + (size_t)kFrameHitChunk * 4;
-    L.ridx = L.wsum + 16 * 4;
-    L.hit = L.ridx + (size_t)kFrameRowStage * 2;
+    L.row = frame_align16(L.tabs + (j.stage_tabs ? (size_t)j.n_ctab * sizeof(FrameChanTab) + (size_t)j.n_thr * 8 + (size_t)j.n_surv * 4 : 0));
+    L.ridx = L.row + (size_t)kFrameRowStage * 4;
+    L.cnt = L.ridx + (size_t)kFrameRowStage * 2;
+    L.hit = L.cnt + 4;
     L.total = L.hit + (size_t)(j.max_slots + 1) * 4;
     return L;
 }

@@ -1,6 +1,6 @@
-"""channel_word and channel_word_surv (ps_common.cuh, the device's
-Pauli-channel samplers: survival products stepped one by one, or binary
-searched in a table) compiled as host code with nvcc, against the oracle's
+"""channel_word, channel_word_surv and channel_word_est (ps_common.cuh, the
+device's Pauli-channel samplers: survival products stepped one by one, binary
+searched in a table, or walked to from a float estimate) compiled as host code with nvcc, against the oracle's
 restatement (ora_channel_paulis) on the CPU: every shot of 12,000 words, one-
 and two-qubit channels, totals from 0 to 1, bit for bit.  The GPU parity tests
 check the device builds of the same functions."""
@@ -41,6 +41,7 @@ int main() {
         uint32_t surv[64];
         ps::channel_surv_table(thr[count - 1], surv);
         if (thr[count - 1] != 0 && surv[63] != thr[count]) ++bad;
+        const ps::ChannelEst est = ps::channel_est_factors(thr[count - 1], count);
         for (uint64_t ev = 0; ev < 50; ++ev) {
             static int32_t o[64 * 40 + 1];
             ora_channel_paulis(12345 + c, ev, 128, 64 * 40, p, count, o);
@@ -48,6 +49,11 @@ int main() {
                 const ps::ChannelWord m = ps::channel_word(12345 + c, ev, 2 + wd, thr, count);
                 const ps::ChannelWord m2 = ps::channel_word_surv(12345 + c, ev, 2 + wd, thr, count, surv);
                 bad += m2.fxa != m.fxa || m2.fza != m.fza || m2.fxb != m.fxb || m2.fzb != m.fzb;
+                const ps::ChannelWord m3 = ps::channel_word_est(12345 + c, ev, 2 + wd, thr, count, surv, est);
+                bad += m3.fxa != m.fxa || m3.fza != m.fza || m3.fxb != m.fxb || m3.fzb != m.fzb;
+                // a poor estimate (one that knows nothing) settles on the same outcomes
+                const ps::ChannelWord m4 = ps::channel_word_est(12345 + c, ev, 2 + wd, thr, count, surv, ps::ChannelEst{0.0f, 0.0f});
+                bad += m4.fxa != m.fxa || m4.fza != m.fza || m4.fxb != m.fxb || m4.fzb != m.fzb;
                 for (int b = 0; b < 64; ++b) {
                     const int k = o[wd * 64 + b];
                     const int pa = count == 3 ? k : k >> 2, pb = count == 3 ? 0 : k & 3;

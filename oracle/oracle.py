@@ -19,7 +19,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libps_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libplaquette_ref.so")
-REF_SRC = "/root/reference/plaquette_simulator/src"
 
 OP_H, OP_S, OP_X, OP_Y, OP_Z, OP_CX, OP_CZ, OP_M, OP_R, OP_PAULI1, OP_PAULI2, OP_H_IF, OP_S_IF = range(13)
 
@@ -29,8 +28,8 @@ _i64, _u64, _i32, _f32, _vp = C.c_int64, C.c_uint64, C.c_int32, C.c_float, C.c_v
 def build(ref: bool = True) -> None:
     """Compile the oracle (and, if the reference headers exist, oracle/_ref)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref and os.path.isfile(os.path.join(REF_SRC, "CliffordState.hpp")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if ref:  # only where the reference is checked out (REF_SRC, see oracle/Makefile)
+        subprocess.run(["make", "-s", "-C", HERE, "ref-if-present"], check=True)
 
 
 _lib = None

@@ -42,6 +42,14 @@ def ref_runs():
 
 
 @pytest.fixture(scope="session")
+def ref_circuits():
+    """The reference's benchmark circuits with the reference's own outputs
+    (make_golden.py: benchmarks/circuits.tar.gz run on oracle/_ref)."""
+    with open(os.path.join(GOLDEN, "reference_circuits.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
 def gpu_lib():
     """Builds (if needed) and loads the CUDA library; skips without a GPU."""
     import build as psbuild

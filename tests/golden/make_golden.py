@@ -10,8 +10,14 @@ has the reference checked out; the outputs are committed).
    headers compiled on the project's Kokkos-API shim, oracle/_ref) for seeded
    circuits under forced random outcomes: per-record results / determined
    flags and a digest of the final tableau.
+3. reference_circuits.json -- the same outputs of the reference for its own
+   benchmark circuits (benchmarks/circuits.tar.gz, the line format of
+   CliffordCircuit.hpp:32-66), each stored as the op table it parses to.
+   The archive holds 59 text circuits; its member width_depth_4_10.circuit
+   is itself a copy of the archive, not a circuit, and is left out.
 
 Usage: python tests/golden/make_golden.py [--ref-src PATH]
+(default: the checkout root of $REF_SRC, else the one oracle/Makefile names)
 """
 from __future__ import annotations
 
@@ -143,15 +149,78 @@ def runs() -> dict:
             "cases": cases}
 
 
+def bench_circuits(ref_root: str) -> dict:
+    """The reference's benchmark circuits, run by the reference (oracle/_ref)
+    and by the oracle on 70 shots (one full 64-shot word and a partial one)
+    under seeded forced outcomes; the two must agree before anything is
+    written."""
+    import tarfile
+
+    import oracle as O
+    from plaquette_simulator import circuits as C
+
+    O.build(ref=True)
+    rng = np.random.default_rng(4242)
+    cases = []
+    with tarfile.open(os.path.join(ref_root, "benchmarks", "circuits.tar.gz")) as tf:
+        for m in sorted(tf.getmembers(), key=lambda m: m.name):
+            f = tf.extractfile(m)
+            if f is None:
+                continue
+            raw = f.read()
+            if raw[:2] == b"\x1f\x8b":  # the archive copy, not a circuit
+                continue
+            width = int(m.name.split("_")[2])
+            circ = C.parse_text(raw.decode(), width)
+            B = 70
+            nm = circ.num_measurements()
+            forced = rng.integers(0, 256, size=(max(nm, 1), (B + 7) // 8), dtype=np.uint8)
+            seed = 7000 + len(cases)
+            ref = O.Reference(width, B, seed=seed)
+            ref.run(circ.op_array(), circ.param_array(), forced)
+            ora = O.Oracle(width, B, seed=seed)
+            ora.run(circ.op_array(), circ.param_array(), forced)
+            assert all(np.array_equal(a, b) for a, b in zip(ref.tableau(), ora.tableau())), m.name
+            recs = []
+            for rid in range(nm):
+                res, det = ref.record(rid)
+                o_res, o_det = ora.record(rid)
+                assert np.array_equal(res, o_res) and np.array_equal(det, o_det), (m.name, rid)
+                recs.append([np.packbits(res.astype(np.uint8), bitorder="little").tolist(),
+                             np.packbits(det.astype(np.uint8), bitorder="little").tolist()])
+            cases.append({
+                "name": m.name, "num_qubits": width, "batch": B, "seed": seed,
+                "ops": circ.op_array().reshape(-1).tolist(), "params": [float(v) for v in circ.param_array()],
+                "forced": forced.tolist(), "records": recs,
+                "tableau_sha256": tableau_digest(ref.tableau()), "checksum": int(ref.checksum()),
+            })
+    return {"generator": "reference headers on oracle/kokkos_shim (oracle/_ref/libplaquette_ref.so), "
+                         "benchmarks/circuits.tar.gz", "cases": cases}
+
+
+def default_ref_root() -> str:
+    src = os.environ.get("REF_SRC")
+    if src:
+        return os.path.abspath(os.path.join(src, "..", ".."))
+    import subprocess
+    out = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "print-ref-root"], check=True,
+                         capture_output=True, text=True)
+    return out.stdout.strip()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default="/root/reference")
+    ap.add_argument("--ref-src", default=None, help="the reference checkout's root")
     args = ap.parse_args()
+    if args.ref_src is None:
+        args.ref_src = default_ref_root()
     with open(os.path.join(HERE, "reference_kat.json"), "w") as f:
         json.dump(kat(args.ref_src), f, indent=1)
     with open(os.path.join(HERE, "reference_runs.json"), "w") as f:
         json.dump(runs(), f)
-    print("wrote", os.path.join(HERE, "reference_kat.json"), os.path.join(HERE, "reference_runs.json"))
+    with open(os.path.join(HERE, "reference_circuits.json"), "w") as f:
+        json.dump(bench_circuits(args.ref_src), f, separators=(",", ":"))
+    print("wrote reference_kat.json, reference_runs.json, reference_circuits.json in", HERE)
 
 
 if __name__ == "__main__":

@@ -96,34 +96,24 @@ def test_noiseless_surface_code_detectors_on_oracle(O):
         assert np.array_equal(par, rec[(rounds - 1) * 2 * na + len(lay.x_anc) + a])
 
 
-def test_reference_benchmark_circuits_parse_and_match(O):
-    """The reference's own benchmark circuits (benchmarks/circuits.tar.gz),
-    read at test time where the reference is checked out: each parses, and
-    oracle and reference agree on it under forced outcomes."""
-    import tarfile
-    path = "/root/reference/benchmarks/circuits.tar.gz"
-    if not os.path.exists(path) or not O.ref_available():
-        pytest.skip("reference checkout not present")
-    rng = np.random.default_rng(5)
-    checked = 0
-    with tarfile.open(path) as tf:
-        for m in tf.getmembers():
-            f = tf.extractfile(m)
-            if f is None:
-                continue
-            raw = f.read()
-            try:
-                text = raw.decode()
-                width = int(m.name.split("_")[2])
-                circ = C.parse_text(text, width)
-            except (UnicodeDecodeError, ValueError, IndexError):
-                continue  # width_depth_4_10.circuit is itself an archive
-            B = 3
-            nm = circ.num_measurements()
-            forced = rng.integers(0, 256, size=(max(nm, 1), 1), dtype=np.uint8)
-            a, b = O.Oracle(width, B, seed=1), O.Reference(width, B, seed=1)
-            a.run(circ.op_array(), circ.param_array(), forced)
-            b.run(circ.op_array(), circ.param_array(), forced)
-            assert all(np.array_equal(x, y) for x, y in zip(a.tableau(), b.tableau())), m.name
-            checked += 1
-    assert checked >= 50
+def test_reference_benchmark_circuits_oracle_pinned(O, ref_circuits):
+    """The oracle against the reference's own outputs on the reference's 59
+    benchmark circuits (benchmarks/circuits.tar.gz, committed as op tables
+    with the outputs by make_golden.py): every record bit for bit, and the
+    final tableau's digest and checksum."""
+    import hashlib
+    assert len(ref_circuits["cases"]) == 59
+    for case in ref_circuits["cases"]:
+        B = case["batch"]
+        o = O.Oracle(case["num_qubits"], B, seed=case["seed"])
+        o.run(np.array(case["ops"], np.int32).reshape(-1, 4), np.array(case["params"], np.float32),
+              np.array(case["forced"], np.uint8))
+        for rid, (rb, db) in enumerate(case["records"]):
+            res, det = o.record(rid)
+            assert np.packbits(res.astype(np.uint8), bitorder="little").tolist() == rb, (case["name"], rid)
+            assert np.packbits(det.astype(np.uint8), bitorder="little").tolist() == db, (case["name"], rid)
+        h = hashlib.sha256()
+        for arr in o.tableau():
+            h.update(np.ascontiguousarray(arr, dtype=np.int32).tobytes())
+        assert h.hexdigest() == case["tableau_sha256"], case["name"]
+        assert o.checksum() == case["checksum"], case["name"]

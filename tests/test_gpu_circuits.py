@@ -194,3 +194,77 @@ def test_words_per_cta_match_oracle(ps, O, name, meas_words):
     o = O.Oracle(circ.num_qubits, B, seed=31)
     o.run(circ.op_array(), circ.param_array())
     _check(st, o, cc.first_record, circ.num_measurements())
+
+
+@pytest.mark.parametrize("form", ["per_op", "plain", "fused", "fused_graph"])
+def test_reference_benchmark_circuits_on_gpu(ps, ref_circuits, form):
+    """The reference's 59 benchmark circuits (benchmarks/circuits.tar.gz, in
+    the line format of CliffordCircuit.hpp:32-66) against the reference's own
+    outputs (tests/golden/reference_circuits.json): op by op through the C
+    ABI, and compiled in the plain and fused forms; every record and the
+    final tableau, bit for bit."""
+    import hashlib
+    from drivers import run_ops_gpu
+    from plaquette_simulator import circuits as C
+    from plaquette_simulator.circuit import CompiledCircuit
+    for case in ref_circuits["cases"]:
+        B = case["batch"]
+        ops = np.array(case["ops"], np.int32).reshape(-1, 4)
+        params = np.array(case["params"], np.float32)
+        forced = np.array(case["forced"], np.uint8)
+        st = ps.CliffordState(case["num_qubits"], B, case["seed"], True)
+        first = 0
+        if form == "per_op":
+            run_ops_gpu(st, ops, params, forced)
+        else:
+            circ = C.Circuit(case["num_qubits"])
+            circ.ops = [tuple(int(v) for v in row) for row in ops]
+            circ.params = [float(v) for v in params]
+            cc = CompiledCircuit(circ, st, fused=form != "plain", graph=form == "fused_graph")
+            if case["records"]:
+                cc.set_forced(forced)
+            cc.run(reset=False)
+            first = cc.first_record
+        for rid, (rb, db) in enumerate(case["records"]):
+            res, det = st.record_bits(first + rid)
+            assert res.tolist() == rb, (form, case["name"], rid)
+            assert det.tolist() == db, (form, case["name"], rid)
+        h = hashlib.sha256()
+        for arr in st.device_to_host_numpy():
+            h.update(np.ascontiguousarray(arr, dtype=np.int32).tobytes())
+        assert h.hexdigest() == case["tableau_sha256"], (form, case["name"])
+        assert st.check_sum() == case["checksum"], (form, case["name"])
+
+
+_CONFIG_ORACLE = {}
+
+
+def _config(name):
+    """The two CPU-sized workloads of the benchmark definition at their full
+    sizes: n = 64 random {H, S, CX} circuit of 1000 gates then M on every
+    qubit, 1024 shots; the d = 5 rotated surface-code memory, 5 rounds,
+    p = 1e-3, 4096 shots.  Seed 12345, native (Philox) draws."""
+    from plaquette_simulator import circuits as C
+    if name == "clifford_n64_1000g_s1024":
+        return C.random_clifford(64, 1000, seed=12345), 1024
+    return C.surface_code_memory(5, 5, p=1e-3), 4096
+
+
+@pytest.mark.parametrize("name", ["clifford_n64_1000g_s1024", "surface_d5_r5_p1e-3_s4096"])
+@pytest.mark.parametrize("form", ["plain", "fused_per_shot", "fused_shared_xz"])
+def test_baseline_configs_full_size(ps, O, name, form):
+    """Whole tableau and every record of each shot against the oracle (run
+    once per workload), bit for bit."""
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ, B = _config(name)
+    if name not in _CONFIG_ORACLE:
+        o = O.Oracle(circ.num_qubits, B, seed=12345)
+        o.run(circ.op_array(), circ.param_array())
+        _CONFIG_ORACLE[name] = o
+    o = _CONFIG_ORACLE[name]
+    st = ps.CliffordState(circ.num_qubits, B, 12345, True)
+    cc = CompiledCircuit(circ, st, fused=form != "plain", graph=True, shared_xz=form == "fused_shared_xz")
+    assert bool(cc.stats["shared_xz"]) == (form == "fused_shared_xz")
+    cc.run(reset=True)
+    st.synchronize()
+    _check(st, o, cc.first_record, circ.num_measurements())

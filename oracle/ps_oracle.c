@@ -37,7 +37,7 @@ void ora_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-enum { TAG_MEASURE = 1, TAG_NOISE = 2 };
+enum { TAG_MEASURE = 1, TAG_NOISE = 2, TAG_NOISE_FIRST = 3 };
 
 /* One 32-bit draw for (seed, event, global shot, tag), the draw of a
  * random measurement's shot.  Shot g lives in 64-shot word g>>6; the word's
@@ -461,8 +461,10 @@ static void apply_flag_paulis(ora_state *s, int64_t q, const int32_t *fx, const 
  * gaps: with S_0 = 2^32 and S_{j+1} = floor(S_j (2^32 - total) / 2^32), a
  * draw u puts the next hit g shots on, g the first with u >= S_{g+1}; one
  * more draw v picks the hit's Pauli, the first k with
- * floor(v total / 2^32) < thr[k].  Draw i of the word is lane i%4 of Philox
- * block (i/4, word, event, TAG_NOISE). */
+ * floor(v total / 2^32) < thr[k].  The first draw of a word is lane
+ * event%4 of Philox block (0, word, event/4, TAG_NOISE_FIRST) -- one block
+ * serves four consecutive channel events -- and draw i >= 1 is lane
+ * (i-1)%4 of block (1 + (i-1)/4, word, event, TAG_NOISE). */
 static uint64_t surv64(uint64_t total) {
     if (total == 0) return (uint64_t)1 << 32;
     const uint64_t q = ((uint64_t)1 << 32) - total;
@@ -477,12 +479,14 @@ static void channel_word(int64_t seed, uint64_t event, uint64_t word, const uint
     const uint64_t total = thr[count - 1];
     if (total == 0) return;
     const uint32_t key[2] = {(uint32_t)((uint64_t)seed & 0xffffffffu), (uint32_t)((uint64_t)seed >> 32)};
-    uint32_t ctr[4] = {0u, (uint32_t)word, (uint32_t)event, TAG_NOISE}, blk[4];
+    uint32_t ctr[4] = {0u, (uint32_t)word, (uint32_t)(event >> 2), TAG_NOISE_FIRST}, blk[4];
     ora_philox4x32_10(ctr, key, blk);
-    uint32_t u = blk[0];
+    uint32_t u = blk[event & 3u];
     if ((uint64_t)u < s64) return;
     const uint64_t q = ((uint64_t)1 << 32) - total;
-    uint32_t i = 1;
+    ctr[2] = (uint32_t)event;
+    ctr[3] = TAG_NOISE;
+    uint32_t i = 0; /* later draws: lane i%4 of block 1 + i/4 */
     int pos = 0;
     for (;;) {
         uint64_t s = (uint64_t)1 << 32;
@@ -492,7 +496,7 @@ static void channel_word(int64_t seed, uint64_t event, uint64_t word, const uint
             if (++pos == 64) return;
         }
         if ((i & 3u) == 0u) {
-            ctr[0] = i >> 2;
+            ctr[0] = 1u + (i >> 2);
             ora_philox4x32_10(ctr, key, blk);
         }
         const uint64_t v = ((uint64_t)blk[i & 3u] * total) >> 32;
@@ -502,7 +506,7 @@ static void channel_word(int64_t seed, uint64_t event, uint64_t word, const uint
         idx[pos] = k;
         if (++pos == 64) return;
         if ((i & 3u) == 0u) {
-            ctr[0] = i >> 2;
+            ctr[0] = 1u + (i >> 2);
             ora_philox4x32_10(ctr, key, blk);
         }
         u = blk[i & 3u];

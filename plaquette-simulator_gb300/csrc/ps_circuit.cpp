@@ -131,6 +131,7 @@ struct ps_circuit {
     // The shared-x/z plan as a job table of one job (ps_frame_dev.h): one
     // sign-kernel launch and one x / z broadcast beside it on a side stream.
     FrameTable ftable;
+    int32_t *d_ferr = nullptr;       // the sign kernel's error word (a bounded wait gave up)
     cudaStream_t fstream = nullptr;  // the broadcast's side stream
     cudaEvent_t fev[2] = {nullptr, nullptr};
     cudaGraph_t graph[2] = {nullptr, nullptr};      // [reset_state]
@@ -797,13 +798,17 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
 // ranges that would need more read them from global memory.  E_ARG: the
 // program does not fit this kernel (the per-shot plan runs instead).
 int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev> &ranges,
-                     std::vector<FrameSlotDev> &slots, std::vector<FrameChanTab> &ctabs, std::vector<uint32_t> &surv) {
+                     std::vector<FrameSlotDev> &slots, std::vector<uint32_t> &s64, std::vector<uint32_t> &events,
+                     std::vector<FrameChanTab> &ctabs,
+                     std::vector<uint32_t> &surv) {
     ps_state *h = c->h;
     const FrameProgram &P = c->fprog;
     ranges.clear();
     uint32_t max_rand = 0, max_scratch = 0, max_slots = 0;
     // channel records (indexed like slot_off) and the distinct tables
-    slots.assign(P.slot_off.size(), FrameSlotDev{});
+    slots.clear();
+    events.assign(P.slot_off.size(), 0u);
+    s64.clear();
     std::map<int32_t, uint32_t> table_of;
     ctabs.clear();
     surv.clear();
@@ -822,8 +827,14 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
             r.nslots = (int32_t)sg.slots.size();
             r.slot_base = (uint32_t)P.ops[L.op0].arg;
             max_slots = std::max(max_slots, (uint32_t)r.nslots);
-            if ((size_t)r.slot_base + (size_t)r.nslots >= slots.size())
+            if ((size_t)r.slot_base + (size_t)r.nslots >= events.size())
                 return fail(E_ARG, "shared-x/z plan: channel table out of range");
+            // this segment's channel records from a 16-byte boundary, padded to one
+            r.rec_base = (uint32_t)slots.size();
+            slots.resize(slots.size() + (((size_t)r.nslots + 1) & ~(size_t)1), FrameSlotDev{0u, kFrameNoHit});
+            // this segment's S_64 words from a 16-byte boundary, padded to one
+            r.s64_base = (uint32_t)s64.size();
+            s64.resize(s64.size() + (((size_t)r.nslots + 3) & ~(size_t)3), 0xFFFFFFFFu);
             for (int32_t q = 0; q < r.nslots; ++q) {
                 const NoiseSlot &sl = sg.slots[(size_t)q];
                 auto it = table_of.find(sl.thr_off);
@@ -843,18 +854,28 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
                 const uint32_t len = P.slot_off[(size_t)r.slot_base + (size_t)q + 1] - t0;
                 if (len > kFrameMaxSlotRows) return fail(E_ARG, "shared-x/z plan: a channel flips too many rows");
                 const bool never = c->thr_host[(size_t)(sl.thr_off + sl.count - 1)] == 0;
-                FrameSlotDev &d = slots[(size_t)r.slot_base + (size_t)q];
-                d.s64 = never ? 0u : (uint32_t)c->thr_host[(size_t)(sl.thr_off + sl.count)];
-                d.event = sl.event;
+                FrameSlotDev &d = slots[(size_t)r.rec_base + (size_t)q];
                 d.t0 = t0;
                 d.lt = len << 12 | (never ? kFrameNoHit : it->second);
+                events[(size_t)r.slot_base + (size_t)q] = sl.event;
+                s64[(size_t)r.s64_base + (size_t)q] =
+                    never ? 0xFFFFFFFFu : (uint32_t)c->thr_host[(size_t)(sl.thr_off + sl.count)];
             }
+        }
+        r.ev0 = -1;
+        if (r.nslots > 0) {  // consecutive events: the kernel draws first draws four channels a block
+            bool run = true;
+            for (int32_t q = 1; q < r.nslots && run; ++q)
+                run = events[(size_t)r.slot_base + q] == events[(size_t)r.slot_base] + (uint32_t)q;
+            if (run && events[(size_t)r.slot_base] <= 0x7FFFFFFFu) r.ev0 = (int32_t)events[(size_t)r.slot_base];
         }
         r.tab0a = L.tab0 & ~3u;
         r.ntab16 = (((L.tab1 + 3u) & ~3u) - r.tab0a) / 4;
         ranges.push_back(r);
     }
     if (ranges.empty()) return fail(E_ARG, "shared-x/z plan: empty program");
+    if (slots.empty()) slots.resize(2, FrameSlotDev{0u, kFrameNoHit});
+    if (s64.empty()) s64.resize(4, 0xFFFFFFFFu);
     job.R = h->R;
     job.n = h->n;
     job.w = h->w;
@@ -1407,9 +1428,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             FrameJobDev job{};
             std::vector<FrameRangeDev> ranges;
             std::vector<FrameSlotDev> fslots;
+            std::vector<uint32_t> fs64, fev;
             std::vector<FrameChanTab> ctabs;
             std::vector<uint32_t> surv;
-            const int jrc = frame_job_ranges(c, job, ranges, fslots, ctabs, surv);
+            const int jrc = frame_job_ranges(c, job, ranges, fslots, fs64, fev, ctabs, surv);
             if (jrc == E_ARG) {
                 set_error("");  // the program does not fit the one-launch kernel: the per-shot plan runs
                 ok = false;
@@ -1420,12 +1442,24 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 FrameRangeDev *dr = nullptr;
                 FrameSlotDev *dsl = nullptr;
                 FrameChanTab *dct = nullptr;
-                uint32_t *dsv = nullptr;
+                uint32_t *dsv = nullptr, *ds64 = nullptr, *dev = nullptr;
                 if (upload(h, c->owned, ranges, &dr) || upload(h, c->owned, fslots, &dsl) ||
-                    upload(h, c->owned, ctabs, &dct) || upload(h, c->owned, surv, &dsv))
+                    upload(h, c->owned, fs64, &ds64) || upload(h, c->owned, fev, &dev) || upload(h, c->owned, ctabs, &dct) ||
+                    upload(h, c->owned, surv, &dsv))
                     return bail(E_CUDA);
                 job.ranges = dr;
                 job.slot = dsl;
+                job.slot_s64 = ds64;
+                job.slot_event = dev;
+                {
+                    void *pe = nullptr;
+                    if (dev_alloc(h, &pe, sizeof(int32_t)) != OK) return bail(E_NOMEM);
+                    c->owned.push_back(pe);
+                    c->d_ferr = static_cast<int32_t *>(pe);
+                    if (cudaMemsetAsync(pe, 0, sizeof(int32_t), h->stream) != cudaSuccess)
+                        return bail(cuda_fail(cudaGetLastError(), "cudaMemsetAsync"));
+                    job.err = c->d_ferr;
+                }
                 job.ctab = dct;
                 job.surv = dsv;
                 BroadcastJobDev bj{h->X, h->Z, c->d_fxz, h->n, h->w, c->fprog.nw64};
@@ -1608,7 +1642,10 @@ ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *de
         PS_CUDA(cudaMemcpyAsync(results, c->d_res_block, bytes, cudaMemcpyDeviceToHost, h->stream));
     if (determined && bytes)
         PS_CUDA(cudaMemcpyAsync(determined, c->d_det_block, bytes, cudaMemcpyDeviceToHost, h->stream));
+    int32_t err = 0;  // the sign kernel's error word (shared-x/z runs)
+    if (c->d_ferr) PS_CUDA(cudaMemcpyAsync(&err, c->d_ferr, sizeof err, cudaMemcpyDeviceToHost, h->stream));
     PS_CUDA(cudaStreamSynchronize(h->stream));
+    if (err) return fail(E_TIMEOUT, "a copy of the sign program did not arrive in time; the run's records are void");
     return OK;
 }
 

@@ -63,7 +63,7 @@ PS_HD u32x4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, ui
     return r;
 }
 
-enum : uint32_t { TAG_MEASURE = 1, TAG_NOISE = 2 };
+enum : uint32_t { TAG_MEASURE = 1, TAG_NOISE = 2, TAG_NOISE_FIRST = 3 };
 
 // Philox block `sub` of global word `word` for event `event`.  A random
 // measurement's draws: block sub (0..15) covers shots 4*sub .. 4*sub+3 of
@@ -90,9 +90,12 @@ PS_HD float unit_float(uint32_t u) { return (float)(u >> 8) * (1.0f / 16777216.0
 // shots in a row are missed, in 32-bit fixed point: integer arithmetic, so
 // every platform computes the same bits); a draw u puts the next hit g
 // shots on, g the first with u >= S_{g+1}, and one more draw v picks the
-// hit's Pauli as the first k with floor(v total / 2^32) < thr[k].  Draw i of
-// a word is lane i%4 of Philox block i/4 keyed by (seed, event, word,
-// TAG_NOISE).  A word with no hit -- u < S_64 -- costs one block.
+// hit's Pauli as the first k with floor(v total / 2^32) < thr[k].  The first
+// draw of a word is lane event%4 of the Philox block keyed by (seed,
+// event/4, word, TAG_NOISE_FIRST), so one block serves the first draws of
+// four consecutive channel events; draw i >= 1 is lane (i-1)%4 of block
+// 1 + (i-1)/4 keyed by (seed, event, word, TAG_NOISE).  A word with no hit
+// -- u < S_64 -- costs a quarter of a block.
 // floor(a b / 2^32) for a, b < 2^32: the survival step S_{j+1} from S_j,
 // exact for j >= 1 (S_1 = 2^32 - total < 2^32).
 PS_HD uint32_t mulhi32(uint32_t a, uint32_t b) {
@@ -121,16 +124,41 @@ struct ChannelWord {
     u64 fxa, fza, fxb, fzb;  // shots with X or Y / Y or Z on qubit a, and on qubit b
 };
 
+// The first draw of channel `event` for a word (lane event%4 of the block
+// its group of four events shares).
+PS_HD uint32_t channel_first_draw(uint64_t seed, uint64_t event, uint64_t word) {
+    return block_lane(draw_block(seed, event >> 2, word, 0u, TAG_NOISE_FIRST), (uint32_t)(event & 3u));
+}
+
+// Later draws of a word: draw i >= 1 is lane (i-1)%4 of block 1 + (i-1)/4.
+struct ChannelDraws {
+    uint64_t seed, event, word;
+    u32x4 blk;
+    uint32_t i = 0;  // later draws taken so far
+    PS_HD uint32_t next() {
+        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, 1u + (i >> 2), TAG_NOISE);
+        return block_lane(blk, i++ & 3u);
+    }
+};
+
+PS_HD void channel_set(ChannelWord &m, int pos, int idx, int count) {
+    const u64 bit = 1ull << pos;
+    const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
+    if (pa == 1 || pa == 2) m.fxa |= bit;
+    if (pa == 2 || pa == 3) m.fza |= bit;
+    if (pb == 1 || pb == 2) m.fxb |= bit;
+    if (pb == 2 || pb == 3) m.fzb |= bit;
+}
+
 PS_HD ChannelWord channel_word(uint64_t seed, uint64_t event, uint64_t word, const uint64_t *thr, int count) {
     ChannelWord m{0ull, 0ull, 0ull, 0ull};
     const uint64_t total = thr[count - 1];
     if (total == 0) return m;
-    u32x4 blk = draw_block(seed, event, word, 0u, TAG_NOISE);
-    uint32_t u = blk.v[0];
+    uint32_t u = channel_first_draw(seed, event, word);
     if ((uint64_t)u < thr[count]) return m;  // no shot of the word is hit
     const uint32_t q = (uint32_t)((1ull << 32) - total);
-    uint32_t i = 1;  // the next draw
-    int pos = 0;     // the first shot not sampled yet
+    ChannelDraws dr{seed, event, word};
+    int pos = 0;  // the first shot not sampled yet
     for (;;) {
         uint32_t s = q;  // S_1
         for (;;) {       // the gap to the next hit
@@ -138,21 +166,12 @@ PS_HD ChannelWord channel_word(uint64_t seed, uint64_t event, uint64_t word, con
             if (++pos == 64) return m;
             s = mulhi32(s, q);
         }
-        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
-        const uint64_t v = ((uint64_t)block_lane(blk, i & 3u) * total) >> 32;
-        ++i;
+        const uint64_t v = ((uint64_t)dr.next() * total) >> 32;
         int idx = 1;
         while (v >= thr[idx - 1]) ++idx;
-        const u64 bit = 1ull << pos;
-        const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
-        if (pa == 1 || pa == 2) m.fxa |= bit;
-        if (pa == 2 || pa == 3) m.fza |= bit;
-        if (pb == 1 || pb == 2) m.fxb |= bit;
-        if (pb == 2 || pb == 3) m.fzb |= bit;
+        channel_set(m, pos, idx, count);
         if (++pos == 64) return m;
-        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
-        u = block_lane(blk, i & 3u);
-        ++i;
+        u = dr.next();
     }
 }
 
@@ -177,11 +196,10 @@ PS_HD ChannelWord channel_word_surv(uint64_t seed, uint64_t event, uint64_t word
     ChannelWord m{0ull, 0ull, 0ull, 0ull};
     const uint64_t total = thr[count - 1];
     if (total == 0) return m;
-    u32x4 blk = draw_block(seed, event, word, 0u, TAG_NOISE);
-    uint32_t u = blk.v[0];
+    uint32_t u = channel_first_draw(seed, event, word);
     if ((uint64_t)u < thr[count]) return m;  // no shot of the word is hit
-    uint32_t i = 1;  // the next draw
-    int pos = 0;     // the first shot not sampled yet
+    ChannelDraws dr{seed, event, word};
+    int pos = 0;  // the first shot not sampled yet
     for (;;) {
         int lo = 0, hi = 64 - pos;  // the first j in [0, 64 - pos) with u >= surv[j], else 64 - pos
         while (lo < hi) {
@@ -191,21 +209,12 @@ PS_HD ChannelWord channel_word_surv(uint64_t seed, uint64_t event, uint64_t word
         }
         if (lo == 64 - pos) return m;
         pos += lo;
-        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
-        const uint64_t v = ((uint64_t)block_lane(blk, i & 3u) * total) >> 32;
-        ++i;
+        const uint64_t v = ((uint64_t)dr.next() * total) >> 32;
         int idx = 1;
         while (v >= thr[idx - 1]) ++idx;
-        const u64 bit = 1ull << pos;
-        const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
-        if (pa == 1 || pa == 2) m.fxa |= bit;
-        if (pa == 2 || pa == 3) m.fza |= bit;
-        if (pb == 1 || pb == 2) m.fxb |= bit;
-        if (pb == 2 || pb == 3) m.fzb |= bit;
+        channel_set(m, pos, idx, count);
         if (++pos == 64) return m;
-        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
-        u = block_lane(blk, i & 3u);
-        ++i;
+        u = dr.next();
     }
 }
 
@@ -225,7 +234,7 @@ inline ChannelEst channel_est_factors(uint64_t total, int count) {
     return e;
 }
 
-// channel_word with both searches started from the float estimates and
+// Both searches of channel_word_est, started from the float estimates and
 // settled on the integer tables: the first j in [0, lim) with u >= surv[j]
 // (surv = channel_surv_table), and the first k with v < thr[k].  Whatever
 // the estimate, the two correcting walks end on the same index as the
@@ -250,38 +259,35 @@ PS_HD float channel_log2(float x) {
     return std::log2(x);
 #endif
 }
-PS_HD ChannelWord channel_word_est(uint64_t seed, uint64_t event, uint64_t word, const uint64_t *thr, int count,
-                                   const uint32_t *surv, ChannelEst est) {
+
+// The outcomes of a word whose first draw u hit (u >= S_64), from there on.
+PS_HD ChannelWord channel_word_est_hit(uint64_t seed, uint64_t event, uint64_t word, uint32_t u, const uint64_t *thr,
+                                       int count, const uint32_t *surv, ChannelEst est) {
     ChannelWord m{0ull, 0ull, 0ull, 0ull};
     const uint64_t total = thr[count - 1];
-    if (total == 0) return m;
-    u32x4 blk = draw_block(seed, event, word, 0u, TAG_NOISE);
-    uint32_t u = blk.v[0];
-    if ((uint64_t)u < thr[count]) return m;  // no shot of the word is hit
-    uint32_t i = 1;  // the next draw
-    int pos = 0;     // the first shot not sampled yet
+    ChannelDraws dr{seed, event, word};
+    int pos = 0;  // the first shot not sampled yet
     for (;;) {
-        const float L = (channel_log2((float)u) - 32.0f) * est.inv_lq;  // u = 0: +inf, clamped
+        const float L = (channel_log2((float)u) - 32.0f) * est.inv_lq;  // u = 0: +inf or NaN, clamped
         const int ge = L >= 0.0f ? (L < 80.0f ? (int)ceilf(L) - 1 : 80) : 0;
         const int lim = 64 - pos;
         const int g = channel_first_at_least(u, surv, lim, ge);
         if (g == lim) return m;
         pos += g;
-        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
-        const uint64_t v = ((uint64_t)block_lane(blk, i & 3u) * total) >> 32;
-        ++i;
+        const uint64_t v = ((uint64_t)dr.next() * total) >> 32;
         const int idx = 1 + channel_first_above(v, thr, count, (int)((float)v * est.kmul));
-        const u64 bit = 1ull << pos;
-        const int pa = count == 3 ? idx : (idx >> 2), pb = count == 3 ? 0 : (idx & 3);
-        if (pa == 1 || pa == 2) m.fxa |= bit;
-        if (pa == 2 || pa == 3) m.fza |= bit;
-        if (pb == 1 || pb == 2) m.fxb |= bit;
-        if (pb == 2 || pb == 3) m.fzb |= bit;
+        channel_set(m, pos, idx, count);
         if (++pos == 64) return m;
-        if ((i & 3u) == 0u) blk = draw_block(seed, event, word, i >> 2, TAG_NOISE);
-        u = block_lane(blk, i & 3u);
-        ++i;
+        u = dr.next();
     }
+}
+
+PS_HD ChannelWord channel_word_est(uint64_t seed, uint64_t event, uint64_t word, const uint64_t *thr, int count,
+                                   const uint32_t *surv, ChannelEst est) {
+    if (thr[count - 1] == 0) return ChannelWord{0ull, 0ull, 0ull, 0ull};
+    const uint32_t u = channel_first_draw(seed, event, word);
+    if ((uint64_t)u < thr[count]) return ChannelWord{0ull, 0ull, 0ull, 0ull};  // no shot of the word is hit
+    return channel_word_est_hit(seed, event, word, u, thr, count, surv, est);
 }
 
 // ----------------------------------------------------------- sign math

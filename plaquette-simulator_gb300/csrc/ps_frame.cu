@@ -23,6 +23,34 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
                  : "memory");
 }
 
+// Bulk copies (TMA, no tensor map) into shared memory, completed on an
+// mbarrier: one thread issues a copy of a whole contiguous block, every
+// consumer polls the barrier's phase, at most kFrameWaitLimit times.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint64_t *bar, uint32_t bytes) {  // the one arrival, and its bytes
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kFrameWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(ok)
+                     : "r"(smem_u32(bar)), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
 // The job of a CTA (or broadcast chunk) index: the last j with first[j] <= i.
 __device__ __forceinline__ int job_of(const int64_t *__restrict__ first, int njobs, int64_t i) {
     int lo = 0, hi = njobs - 1;
@@ -93,13 +121,18 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
     uint32_t *const stab = reinterpret_cast<uint32_t *>(sb8 + SL.tab);
     FrameOp *const sops = reinterpret_cast<FrameOp *>(sb8 + SL.ops);
     u64 *const snew = reinterpret_cast<u64 *>(sb8 + SL.nw);  // F_LINEAR's new rows
-    u64 *const shm = reinterpret_cast<u64 *>(sb8 + SL.hm);   // a chunk of hits: outcome masks (4 a hit)
-    FrameSlotDev *const sslot = reinterpret_cast<FrameSlotDev *>(sb8 + SL.slot);  // [2][max_slots]
-    uint32_t *const srow = reinterpret_cast<uint32_t *>(sb8 + SL.row);    // the chunk's hit rows
-    uint16_t *const sridx = reinterpret_cast<uint16_t *>(sb8 + SL.ridx);  // hit of each staged row
-    uint32_t *const srcnt = reinterpret_cast<uint32_t *>(sb8 + SL.cnt);   // staged rows taken
-    uint32_t *const shit = reinterpret_cast<uint32_t *>(sb8 + SL.hit);    // hit channels: count, then the list
-    uint32_t *const shitl = shit + 1;
+    FrameSlotDev *const sslot = reinterpret_cast<FrameSlotDev *>(sb8 + SL.slot);  // [2][max_slots rounded to 2]
+    uint32_t *const ss64 = reinterpret_cast<uint32_t *>(sb8 + SL.s64);             // [2][max_slots rounded to 4]
+    uint32_t *const srow = reinterpret_cast<uint32_t *>(sb8 + SL.row);             // the chunk's hit rows
+    u64 *const shm = reinterpret_cast<u64 *>(sb8 + SL.hm);                         // the chunk's outcome masks (4 a hit)
+    uint32_t *const shrow = reinterpret_cast<uint32_t *>(sb8 + SL.hrow);           // its first staged row (or ~0u)
+    uint32_t *const shlen = reinterpret_cast<uint32_t *>(sb8 + SL.hlen);           // its staged row count
+    uint32_t *const shpre = reinterpret_cast<uint32_t *>(sb8 + SL.hpre);           // prefix of the counts
+    uint32_t *const swsum = reinterpret_cast<uint32_t *>(sb8 + SL.wsum);           // per-warp sums
+    uint32_t *const shit = reinterpret_cast<uint32_t *>(sb8 + SL.hit);    // hit channels: count, then (channel, first draw)
+    uint32_t *const srcnt = shit + 1;  // staged row words taken
+    uint32_t *const shitl = shit + 2;
+    uint64_t *const sbar = reinterpret_cast<uint64_t *>(sb8 + SL.bar);  // [0..1] channel records, [2] ops + tab
     const FrameOp *const gops = J.ops;
     const uint32_t *const gtab = J.tab;
     u64 *const rec = J.rec;
@@ -120,91 +153,169 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
         surv = s2;
     }
     for (int64_t i = tid; i < W + 1 + (int64_t)kWinRows; i += NT) sR[i] = 0ull;
-    // cp.async groups, in commit order per range li: T(li) (its ops and tab
-    // words), R (hit rows, one group per chunk), S(li+1) (the next range's
-    // channel records, into the other buffer).  S(0) goes first.
-    auto fetch_slots = [&](const FrameRangeDev &R, int buf) {
-        const FrameSlotDev *src = J.slot + R.slot_base;
-        FrameSlotDev *dst = sslot + (size_t)buf * J.max_slots;
-        for (int i = tid; i < R.nslots; i += NT) cp_async16(dst + i, src + i);
+    // Bulk copies: the channel records and S_64 words of range li + 1 into
+    // buffer (li + 1) & 1 (barrier sbar[(li + 1) & 1]) while range li runs,
+    // and a range's ops and tab words at its start (sbar[2]); thread 0
+    // issues them.  Barrier phases flip with every completed copy.
+    if (tid == 0) {
+        for (int b = 0; b < 3; ++b) mbar_init(sbar + b);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    uint32_t pend = 0u;  // thread 0: the barriers with a copy in flight (bits 0..2)
+    auto fetch_slots = [&](const FrameRangeDev &R, int buf) {  // thread 0; a range with channels
+        const uint32_t rb = (((uint32_t)R.nslots + 1u) & ~1u) * (uint32_t)sizeof(FrameSlotDev),
+                       sb = (((uint32_t)R.nslots + 3u) & ~3u) * 4u;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        pend |= 1u << buf;
+        mbar_expect(sbar + buf, rb + sb);
+        bulk_copy(sslot + (size_t)buf * ((J.max_slots + 1) & ~1u), J.slot + R.rec_base, rb, sbar + buf);
+        bulk_copy(ss64 + (size_t)buf * ((J.max_slots + 3) & ~3u), J.slot_s64 + R.s64_base, sb, sbar + buf);
+    };
+    uint32_t sph[2] = {0u, 0u}, tph = 0u;  // the phases the next waits look for
+    // Waits (every thread) for barrier b's copy.  False when a wait gave up
+    // in any thread: the error word is set, the copies still in flight are
+    // waited for (bounded), and the caller leaves the kernel.
+    auto wait_bar = [&](int b) -> bool {
+        uint32_t &ph = b < 2 ? sph[b] : tph;
+        const bool ok = mbar_wait(sbar + b, ph);
+        ph ^= 1u;
+        if (__syncthreads_or(!ok) == 0) {
+            pend &= ~(1u << b);
+            return true;
+        }
+        if (tid == 0) {
+            atomicOr(J.err, kFrameErrWait);
+            for (int c = 0; c < 3; ++c)
+                if ((pend >> c) & 1u) (void)mbar_wait(sbar + c, c == b ? (ph ^ 1u) : (c < 2 ? sph[c] : tph));
+        }
+        return false;
     };
     FrameRangeDev L = J.ranges[0];
-    fetch_slots(L, 0);
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    if (tid == 0 && L.nslots > 0) fetch_slots(L, 0);
     u64 last = 0ull;  // outcome of the latest measurement (its reset X)
     for (int li = 0; li < J.nranges; ++li) {
         const FrameRangeDev Ln = J.ranges[li + 1 < J.nranges ? li + 1 : li];  // in flight meanwhile
-        if (L.stage) {
-            for (uint32_t i = tid; i < L.ntab16; i += NT) cp_async16(stab + 4 * i, gtab + L.tab0a + 4 * i);
-            for (uint32_t i = tid; i < L.op1 - L.op0; i += NT) cp_async16(sops + i, gops + L.op0 + i);
+        if (tid == 0) {
+            *shit = 0u;
+            *srcnt = 0u;
+            if (L.stage) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                pend |= 4u;
+                mbar_expect(sbar + 2, L.ntab16 * 16u + (L.op1 - L.op0) * 16u);
+                if (L.ntab16) bulk_copy(stab, gtab + L.tab0a, L.ntab16 * 16u, sbar + 2);
+                if (L.op1 > L.op0) bulk_copy(sops, gops + L.op0, (L.op1 - L.op0) * 16u, sbar + 2);
+            }
         }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // S(li): every group but T(li)
-        if (tid == 0) *shit = 0u;
-        __syncthreads();
-        const FrameSlotDev *cs = sslot + (size_t)(li & 1) * J.max_slots;
+        if (L.nslots > 0) {
+            if (!wait_bar(li & 1)) return;
+        } else {
+            __syncthreads();
+        }
+        const FrameSlotDev *cs = sslot + (size_t)(li & 1) * ((J.max_slots + 1) & ~1u);
+        const uint32_t *cs64 = ss64 + (size_t)(li & 1) * ((J.max_slots + 3) & ~3u);
         // 2. channel outcomes.  A first pass draws every channel's first
-        //    number (one Philox block; no shot of the word is hit unless it
-        //    is at least S_64, 94 % of channels at p = 1e-3) with all lanes
-        //    converged, two channels in flight per thread, and lists the hit
-        //    channels.  The hits are then taken in chunks: a thread per hit
-        //    fetches its slot's row entries into shared memory and samples
-        //    its word (channel_word_est: the same draws as every other
-        //    form), then all threads together flip the signs of those rows,
-        //    one row entry per thread (32-bit shared atomics: XORs commute,
-        //    and two slots may share a row).
+        //    number (a Philox block gives the first numbers of four channels;
+        //    no shot of the word is hit unless it is at least S_64, 94 % of
+        //    channels at p = 1e-3) with all lanes converged, and lists the
+        //    hit channels with their first numbers.  Then a thread per hit
+        //    samples its word (channel_word_est_hit: the same draws as every
+        //    other form) and flips the signs of its slot's rows, prefetched
+        //    meanwhile (32-bit shared atomics: XORs commute, and two slots
+        //    may share a row).
         if (L.nslots > 0) {
             // every lane runs every iteration (the ballots below take the
-            // full warp); channels past the end just report no hit
-            for (int sb = 0; sb < L.nslots; sb += 2 * NT) {
-                bool hit[2];
+            // full warp); channels past the end just report no hit.  With
+            // consecutive events a warp takes 128 events at a time: lane t
+            // draws the block of group t (events 4t .. 4t + 3), and in slice
+            // q lane t takes event 32q + t, whose number it gets by shuffle,
+            // so that the S_64 words are read contiguously.  Else one block
+            // a channel.
+            const uint64_t e0 = rp.event_base + (uint64_t)(L.ev0 >= 0 ? L.ev0 : 0);
+            const uint64_t g0 = e0 >> 2;  // the first group
+            const int64_t nunits = L.ev0 >= 0 ? (int64_t)(((e0 + (uint64_t)L.nslots - 1) >> 2) - g0 + 1)
+                                              : (int64_t)L.nslots;
+            auto append = [&](bool hit, uint32_t slot, uint32_t u) {  // warp-aggregated
+                const unsigned b = __ballot_sync(0xffffffffu, hit);
+                if (b == 0u) return;
+                uint32_t base = 0u;
+                if (lane == 0) base = atomicAdd(shit, (uint32_t)__popc(b));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (hit) {
+                    const uint32_t at = base + __popc(b & ((1u << lane) - 1u));
+                    shitl[2 * at] = slot;
+                    shitl[2 * at + 1] = u;
+                }
+            };
+            if (L.ev0 >= 0) {
+                for (int64_t wb = 32 * (int64_t)wid; wb < nunits; wb += 32 * FW) {  // the warp's 32 groups
+                    u32x4 blk{};
+                    if (wb + lane < nunits)
+                        blk = draw_block(rp.seed, g0 + (uint64_t)(wb + lane), rp.word_base + (uint64_t)k, 0u, TAG_NOISE_FIRST);
 #pragma unroll
-                for (int u = 0; u < 2; ++u) {
-                    const int s = sb + tid + u * NT;
-                    hit[u] = false;
-                    if (s < L.nslots) {
-                        const FrameSlotDev d = cs[s];
-                        const uint32_t first =
-                            draw_block(rp.seed, rp.event_base + d.event, rp.word_base + (uint64_t)k, 0u, TAG_NOISE).v[0];
-                        hit[u] = (d.lt & 0xFFFu) != kFrameNoHit && first >= d.s64;
+                    for (int q = 0; q < 4; ++q) {
+                        const int src = 8 * q + (lane >> 2);
+                        uint32_t x[4];
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) x[c] = __shfl_sync(0xffffffffu, blk.v[c], src);
+                        const uint32_t u = (lane & 3) == 0 ? x[0] : (lane & 3) == 1 ? x[1] : (lane & 3) == 2 ? x[2] : x[3];
+                        const int64_t sl = (int64_t)(4 * (g0 + (uint64_t)wb)) + 32 * q + lane - (int64_t)e0;
+                        const bool hit = sl >= 0 && sl < L.nslots && u >= cs64[sl];
+                        append(hit, (uint32_t)sl, u);
                     }
                 }
-#pragma unroll
-                for (int u = 0; u < 2; ++u) {  // warp-aggregated append
-                    const unsigned b = __ballot_sync(0xffffffffu, hit[u]);
-                    if (b == 0u) continue;
-                    uint32_t base = 0u;
-                    if (lane == 0) base = atomicAdd(shit, (uint32_t)__popc(b));
-                    base = __shfl_sync(0xffffffffu, base, 0);
-                    if (hit[u]) shitl[base + __popc(b & ((1u << lane) - 1u))] = (uint32_t)(sb + tid + u * NT);
+            } else {
+                for (int64_t ub = 0; ub < nunits; ub += NT) {
+                    const int64_t unit = ub + tid;
+                    bool hit = false;
+                    uint32_t u = 0u;
+                    if (unit < nunits) {
+                        u = channel_first_draw(rp.seed, rp.event_base + J.slot_event[L.slot_base + unit],
+                                               rp.word_base + (uint64_t)k);
+                        hit = u >= cs64[unit];
+                    }
+                    append(hit, (uint32_t)unit, u);
                 }
             }
             __syncthreads();
             const uint32_t nhit = *shit;
-            for (uint32_t c0 = 0; c0 < nhit; c0 += NT) {
-                const uint32_t cend = min(nhit, c0 + (uint32_t)NT);
+            // The hits, kFrameHitChunk at a time.  A thread per hit (spread
+            // over the warps: hit c0 + l on lane l / FW of warp l % FW)
+            // stages the 16-byte-aligned cover of its slot's rows (16-byte
+            // copies; tab holds padding after its end) and samples its word
+            // meanwhile; then all threads apply the chunk's rows together,
+            // row entry e on thread e % NT (the hit by binary search in the
+            // prefix of the row counts), so that a long row list does not
+            // hold the CTA back.
+            for (uint32_t c0 = 0; c0 < nhit; c0 += kFrameHitChunk) {
+                const uint32_t cend = min(nhit, c0 + kFrameHitChunk);
                 if (tid == 0) *srcnt = 0u;
                 __syncthreads();
-                // one thread per hit, spread over the warps (chunk hit l on
-                // lane l / FW of warp l % FW): it fetches the hit slot's rows
-                // into the staging area first, then samples the word
-                const uint32_t l = (uint32_t)lane * FW + (uint32_t)wid, h = c0 + l;
-                if (h < cend) {
-                    const FrameSlotDev d = cs[shitl[h]];
+                for (uint32_t l0 = 0; l0 < kFrameHitChunk; l0 += NT) {
+                    const uint32_t l = l0 + (uint32_t)lane * FW + (uint32_t)wid, h = c0 + l;
+                    if (h >= cend) continue;
+                    const uint32_t s0 = shitl[2 * h];
+                    const FrameSlotDev d = cs[s0];
                     const uint32_t len = d.lt >> 12, t0 = d.t0;
-                    const uint32_t pos = atomicAdd(srcnt, len);
-                    const bool staged = pos + len <= kFrameRowStage;
-                    for (uint32_t r = 0; r < len && pos + r < kFrameRowStage; ++r) {
-                        if (staged) cp_async4(srow + pos + r, gtab + t0 + r);
-                        sridx[pos + r] = staged ? (uint16_t)l : (uint16_t)0xFFFFu;  // 0xFFFF: skip
+                    const uint32_t a0 = t0 & ~3u, span = ((t0 + len + 3u) & ~3u) - a0;
+                    const uint32_t pos = atomicAdd(srcnt, span);
+                    const bool staged = pos + span <= kFrameRowStage;
+                    if (staged)
+                        for (uint32_t c = 0; c < span; c += 4) cp_async16(srow + pos + c, gtab + a0 + c);
+                    ChannelWord m{0ull, 0ull, 0ull, 0ull};
+                    const uint32_t tb = d.lt & 0xFFFu;
+                    if (tb != kFrameNoHit) {  // (a channel that never hits has S_64 = 2^32 - 1)
+                        const FrameChanTab ct = ctab[tb];
+                        const uint32_t ev = L.ev0 >= 0 ? (uint32_t)L.ev0 + s0 : J.slot_event[L.slot_base + s0];
+                        m = channel_word_est_hit(rp.seed, rp.event_base + ev, rp.word_base + (uint64_t)k, shitl[2 * h + 1],
+                                                 thr + ct.thr_off, ct.count, surv + ct.surv_off, ct.est);
                     }
-                    const FrameChanTab ct = ctab[d.lt & 0xFFFu];
-                    const ChannelWord m = channel_word_est(rp.seed, rp.event_base + d.event, rp.word_base + (uint64_t)k,
-                                                           thr + ct.thr_off, ct.count, surv + ct.surv_off, ct.est);
-                    shm[4 * l + 0] = m.fxa;
-                    shm[4 * l + 1] = m.fza;
-                    shm[4 * l + 2] = m.fxb;
-                    shm[4 * l + 3] = m.fzb;
+                    shm[4 * (h - c0) + 0] = m.fxa;
+                    shm[4 * (h - c0) + 1] = m.fza;
+                    shm[4 * (h - c0) + 2] = m.fxb;
+                    shm[4 * (h - c0) + 3] = m.fzb;
+                    shrow[h - c0] = staged ? pos + (t0 - a0) : ~0u;
+                    shlen[h - c0] = staged ? len : 0u;
                     if (!staged) {  // rows that do not fit: applied now, from global memory
                         for (uint32_t r = 0; r < len; ++r) {
                             const uint32_t v = __ldg(gtab + t0 + r), sel = v >> 28;
@@ -222,26 +333,58 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
                 asm volatile("cp.async.commit_group;\n" ::: "memory");
                 asm volatile("cp.async.wait_group 0;\n" ::: "memory");
                 __syncthreads();
-                const uint32_t nst = min(*srcnt, kFrameRowStage);
-                for (uint32_t e = tid; e < nst; e += NT) {
-                    const uint32_t h = sridx[e];
-                    if (h == 0xFFFFu) continue;
-                    const uint32_t v = srow[e], sel = v >> 28;
+                // exclusive prefix of the chunk's staged row counts: each
+                // warp scans hits 32 w .. 32 w + 31 (every lane runs it)
+                const uint32_t nh = cend - c0;
+                uint32_t total = 0u;
+                for (uint32_t b0 = 0; b0 < nh; b0 += NT) {
+                    const uint32_t i = b0 + tid;
+                    const uint32_t len = i < nh ? shlen[i] : 0u;
+                    uint32_t x = len;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                        if (lane >= o) x += y;
+                    }
+                    if (lane == 31) swsum[wid] = x;
+                    __syncthreads();
+                    uint32_t woff = total, add = 0u;
+#pragma unroll
+                    for (int q = 0; q < FW; ++q) {
+                        const uint32_t v = swsum[q];
+                        woff += q < wid ? v : 0u;
+                        add += v;
+                    }
+                    if (i < nh) shpre[i] = woff + x - len;
+                    total += add;
+                    __syncthreads();
+                }
+                for (uint32_t e = tid; e < total; e += NT) {
+                    // the last hit with shpre <= e: it has staged rows (a hit
+                    // without any shares its prefix with the next one, and
+                    // the last one's prefix is the total)
+                    uint32_t lo = 0u, hi = nh - 1u;
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi + 1u) >> 1;
+                        if (shpre[mid] <= e) lo = mid;
+                        else hi = mid - 1u;
+                    }
+                    const uint32_t v = srow[shrow[lo] + (e - shpre[lo])], sel = v >> 28;
                     u64 f = 0ull;  // row | sel << 28: X on rows with z, Z on rows with x
-                    if (sel & 1u) f ^= shm[4 * h + 0];
-                    if (sel & 2u) f ^= shm[4 * h + 1];
-                    if (sel & 4u) f ^= shm[4 * h + 2];
-                    if (sel & 8u) f ^= shm[4 * h + 3];
+                    if (sel & 1u) f ^= shm[4 * lo + 0];
+                    if (sel & 2u) f ^= shm[4 * lo + 1];
+                    if (sel & 4u) f ^= shm[4 * lo + 2];
+                    if (sel & 8u) f ^= shm[4 * lo + 3];
                     unsigned *rw = reinterpret_cast<unsigned *>(&sR[v & kFrameRowMask]);
                     if ((uint32_t)f) atomicXor(rw, (uint32_t)f);
                     if (f >> 32) atomicXor(rw + 1, (uint32_t)(f >> 32));
                 }
-                __syncthreads();  // the chunk applied before the next one overwrites it
+                __syncthreads();  // the chunk applied before the next one reuses the staging
             }
+            __syncthreads();  // every hit applied before the ops
         }
         // the next range's channel records, into the buffer range li - 1 used
-        if (li + 1 < J.nranges) fetch_slots(Ln, (li + 1) & 1);
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        if (tid == 0 && li + 1 < J.nranges && Ln.nslots > 0) fetch_slots(Ln, (li + 1) & 1);
         // 3. random outcomes: half-warps, one Philox block per lane
         for (uint32_t r0 = 2u * (uint32_t)wid; r0 < L.nrand; r0 += 2u * FW) {
             const uint32_t r = r0 + (uint32_t)(lane >> 4);
@@ -253,8 +396,11 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
             for (int off = 8; off > 0; off >>= 1) bits |= __shfl_xor_sync(0xffffffffu, bits, off);
             if ((lane & 15) == 0 && r < L.nrand) sout[r] = bits;
         }
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // T(li): every group but S(li+1)
-        __syncthreads();
+        if (L.stage) {
+            if (!wait_bar(2)) return;
+        } else {
+            __syncthreads();
+        }
         // 4. the ops
         const uint32_t *T = L.stage ? stab : gtab;  // measurement-op tab, indexed x - tb
         const uint32_t tb = L.stage ? L.tab0a : 0u;

@@ -10,13 +10,11 @@
 namespace ps {
 
 // A channel of a sign program, indexed like slot_off (slot_base + slot):
-// s64 = thr[count] = S_64 (a first draw below it hits no shot of the word),
-// its event offset, its rows tab[t0, t0 + len) and its table, packed as
-// lt = len << 12 | table; table kFrameNoHit marks a channel that never hits
-// (total probability 0).
+// its rows tab[t0, t0 + len) and its table, packed as lt = len << 12 |
+// table; table kFrameNoHit marks a channel that never hits (total
+// probability 0).  Its S_64 word (a first draw below it hits no shot of the
+// word) and its event offset are kept in arrays of their own.
 struct FrameSlotDev {
-    uint32_t s64;
-    uint32_t event;
     uint32_t t0;
     uint32_t lt;
 };
@@ -36,14 +34,13 @@ struct FrameChanTab {
     uint32_t pad2[2];
 };
 
-// Hits of a range's channels are sampled and applied in chunks of at most
-// this many; the rows of a chunk's hits are fetched into shared memory up to
-// kFrameRowStage entries (a hit whose rows do not fit applies them from
-// global memory); the channel tables are staged in shared memory when they
-// take at most kFrameTabStage bytes.
+// The channel tables are staged in shared memory when they take at most
+// kFrameTabStage bytes.  A range's hits are taken kFrameHitChunk at a time;
+// their rows are staged in shared memory, up to kFrameRowStage words a chunk
+// (a hit whose rows do not fit applies them alone, from global memory).
+constexpr uint32_t kFrameTabStage = 4096;
 constexpr uint32_t kFrameHitChunk = 256;
 constexpr uint32_t kFrameRowStage = 2048;
-constexpr uint32_t kFrameTabStage = 4096;
 
 // One launch range of a sign program (FrameProgram::Launch): its segment's
 // channel outcomes, drawn and applied first, then ops [op0, op1).
@@ -54,7 +51,10 @@ struct FrameRangeDev {
     uint32_t tab0a, ntab16;  // staged tab words: 16-byte chunks from tab0a (stage = 1)
     uint32_t rand0, nrand;   // rand_meas[rand0, rand0 + nrand): the range's random measurements
     uint32_t stage;          // 1: ops and tab range staged in shared memory
-    uint32_t pad;
+    int32_t ev0;             // >= 0: the channels' events are ev0, ev0 + 1, ... (first draws by groups of four)
+    uint32_t s64_base;       // slot_s64 index of the segment's first S_64 word (a multiple of 4)
+    uint32_t rec_base;       // slot index of the segment's first channel record (even: 16-byte aligned)
+    uint32_t pad[2];
 };
 
 // One job: a sign program over the signs R of every shot-word of one state.
@@ -73,7 +73,9 @@ struct FrameJobDev {
     u64 *rec;  // record block: results [nm][w], then determined [nm][w]
     int64_t nm;
     const uint64_t *thr;  // channel threshold tables
-    const FrameSlotDev *slot;
+    const FrameSlotDev *slot;    // channel records, per range from rec_base
+    const uint32_t *slot_s64;    // S_64 of every channel (0xFFFFFFFF for one that never hits), per range from s64_base
+    const uint32_t *slot_event;  // event offset of every channel, like slot (ranges with ev0 < 0 read it)
     const FrameChanTab *ctab;
     const uint32_t *surv;
     const RunParams *rp;
@@ -83,16 +85,26 @@ struct FrameJobDev {
     // words, surv words; staged when stage_tabs = 1)
     uint32_t max_rand, stage_u32, max_ops, max_scratch, max_slots;
     uint32_t n_ctab, n_thr, n_surv, stage_tabs, pad2;
+    int32_t *err;  // set to kFrameErrWait when a bounded wait gave up (the run's results are void)
 };
+
+// A sign CTA gives up on an asynchronous copy after this many polls of its
+// barrier (each poll may suspend the thread for a while), sets the job's
+// error word and leaves.
+constexpr uint32_t kFrameWaitLimit = 1u << 22;
+constexpr int32_t kFrameErrWait = 1;
 
 // Shared-memory layout of the sign kernel for one job (byte offsets):
 // signs (W rows, the zero row, kWinRows sink rows), random outcomes, staged
-// tab words, staged ops, F_LINEAR's new rows, a chunk of hits' outcome
-// masks, two buffers of channel records (the range's, the next one's being
-// fetched), the channel tables, the hit rows and the hit of each (u16), the
-// staged-row count, the hit list.
+// tab words, staged ops, F_LINEAR's new rows, two buffers of channel
+// records and two of their S_64 words (the range's, the next one's being
+// fetched), the channel tables, the hit rows, a chunk of hits (outcome
+// masks, first staged row, row count, prefix of the counts), per-warp sums,
+// the hit list (count, staged row words, then channel and first draw of
+// each hit), the barriers of the bulk copies (channel records: two, staged
+// ops and tab words: one).
 struct FrameSmem {
-    size_t out, tab, ops, nw, hm, slot, tabs, row, ridx, cnt, hit, total;
+    size_t out, tab, ops, nw, slot, s64, tabs, row, hm, hrow, hlen, hpre, wsum, hit, bar, total;
 };
 __host__ __device__ inline size_t frame_align16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline FrameSmem frame_smem_layout(const FrameJobDev &j) {
@@ -101,14 +113,20 @@ __host__ __device__ inline FrameSmem frame_smem_layout(const FrameJobDev &j) {
     L.tab = frame_align16(L.out + (size_t)j.max_rand * 8);
     L.ops = L.tab + (size_t)j.stage_u32 * 4;
     L.nw = L.ops + (size_t)j.max_ops * 16;
-    L.hm = frame_align16(L.nw + (size_t)j.max_scratch * 8);
-    L.slot = L.hm + (size_t)kFrameHitChunk * 32;
-    L.tabs = L.slot + (size_t)2 * j.max_slots * 16;
-    L.row = frame_align16(L.tabs + (j.stage_tabs ? (size_t)j.n_ctab * sizeof(FrameChanTab) + (size_t)j.n_thr * 8 + (size_t)j.n_surv * 4 : 0));
-    L.ridx = L.row + (size_t)kFrameRowStage * 4;
-    L.cnt = L.ridx + (size_t)kFrameRowStage * 2;
-    L.hit = L.cnt + 4;
-    L.total = L.hit + (size_t)(j.max_slots + 1) * 4;
+    L.slot = frame_align16(L.nw + (size_t)j.max_scratch * 8);
+    L.s64 = frame_align16(L.slot + (size_t)2 * ((j.max_slots + 1) & ~1u) * sizeof(FrameSlotDev));
+    L.tabs = frame_align16(L.s64 + (size_t)2 * ((j.max_slots + 3) & ~3u) * 4);
+    L.row = frame_align16(L.tabs + (j.stage_tabs ? (size_t)j.n_ctab * sizeof(FrameChanTab) + (size_t)j.n_thr * 8 +
+                                                       (size_t)j.n_surv * 4
+                                                 : 0));
+    L.hm = L.row + (size_t)kFrameRowStage * 4;
+    L.hrow = L.hm + (size_t)kFrameHitChunk * 32;
+    L.hlen = L.hrow + (size_t)kFrameHitChunk * 4;
+    L.hpre = L.hlen + (size_t)kFrameHitChunk * 4;
+    L.wsum = L.hpre + (size_t)kFrameHitChunk * 4;
+    L.hit = L.wsum + 16 * 4;
+    L.bar = frame_align16(L.hit + (size_t)(2 * j.max_slots + 2) * 4);
+    L.total = L.bar + 32;
     return L;
 }
 

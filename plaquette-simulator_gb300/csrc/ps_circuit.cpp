@@ -799,7 +799,7 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
 // program does not fit this kernel (the per-shot plan runs instead).
 int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev> &ranges,
                      std::vector<FrameSlotDev> &slots, std::vector<uint32_t> &s64, std::vector<uint32_t> &events,
-                     std::vector<FrameChanTab> &ctabs,
+                     std::vector<int32_t> &nv_range, std::vector<FrameChanTab> &ctabs,
                      std::vector<uint32_t> &surv) {
     ps_state *h = c->h;
     const FrameProgram &P = c->fprog;
@@ -807,6 +807,7 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
     uint32_t max_rand = 0, max_scratch = 0, max_slots = 0;
     // channel records (indexed like slot_off) and the distinct tables
     slots.clear();
+    nv_range.clear();
     events.assign(P.slot_off.size(), 0u);
     s64.clear();
     std::map<int32_t, uint32_t> table_of;
@@ -863,11 +864,16 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
             }
         }
         r.ev0 = -1;
+        r.nv = -1;
         if (r.nslots > 0) {  // consecutive events: the kernel draws first draws four channels a block
             bool run = true;
             for (int32_t q = 1; q < r.nslots && run; ++q)
                 run = events[(size_t)r.slot_base + q] == events[(size_t)r.slot_base] + (uint32_t)q;
             if (run && events[(size_t)r.slot_base] <= 0x7FFFFFFFu) r.ev0 = (int32_t)events[(size_t)r.slot_base];
+        }
+        if (r.nslots > 0) {  // its noise vectors: block nv of nvec
+            r.nv = (int32_t)nv_range.size();
+            nv_range.push_back((int32_t)ranges.size());
         }
         r.tab0a = L.tab0 & ~3u;
         r.ntab16 = (((L.tab1 + 3u) & ~3u) - r.tab0a) / 4;
@@ -894,6 +900,7 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
     job.n_ctab = (uint32_t)ctabs.size();
     job.n_thr = (uint32_t)c->thr_host.size();
     job.n_surv = (uint32_t)surv.size();
+    job.nnv = (int32_t)nv_range.size();
     job.stage_tabs = (size_t)job.n_ctab * sizeof(FrameChanTab) + (size_t)job.n_thr * 8 + (size_t)job.n_surv * 4 <= kFrameTabStage ? 1u : 0u;
     // staging: drop the largest staged range until the buffers fit
     std::vector<char> on(ranges.size(), 1);
@@ -917,13 +924,15 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
     }
     for (size_t i = 0; i < ranges.size(); ++i) ranges[i].stage = on[i] ? 1u : 0u;
     if (frame_job_smem(job) > kSegSmemMax) return fail(E_ARG, "sign program does not fit in shared memory");
+    if (job.nnv > 0 && noise_job_smem(job) > kSegSmemMax) return fail(E_ARG, "channel noise does not fit in shared memory");
     return OK;
 }
 
-// The shared-x/z plan of a run from |0...0>: the whole sign program (channel
-// sampling included) as one launch, and the broadcast of the final x / z
-// bits (host-known, so it needs nothing else) beside it on a side stream,
-// joined back at the end.  Profiled, the two run one after the other.
+// The shared-x/z plan of a run from |0...0>: the noise vectors of every range
+// and shot-word, then the whole sign program as one launch, with the
+// broadcast of the final x / z bits (host-known, so it needs nothing else)
+// beside them on a side stream, joined back at the end.  Profiled, the three
+// run one after the other.
 int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
     auto timed = [&](int kind, auto &&launch) -> int {
         if (prof && prof->begin(kind) != OK) return E_CUDA;
@@ -932,13 +941,18 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
         return rc;
     };
     if (prof || !c->fstream) {
-        int rc = timed(P_FRAME, [&] { return launch_frame_run(st, c->ftable, c->opts.frame_warps); });
+        int rc = timed(P_SAMPLE, [&] { return launch_noise_vectors(st, c->ftable); });
+        if (rc == OK) rc = timed(P_FRAME, [&] { return launch_frame_run(st, c->ftable, c->opts.frame_warps); });
         if (rc != OK) return rc;
         return timed(P_BROADCAST, [&] { return launch_broadcast_jobs(st, c->ftable, c->opts.bcast_ctas); });
     }
+    // The broadcast runs beside the noise vectors and the sign program.
+    // (Whatever runs beside its stream of stores slows down two- to
+    // three-fold; of the orders measured this one ends first.)
     PS_CUDA(cudaEventRecord(c->fev[0], st));
     PS_CUDA(cudaStreamWaitEvent(c->fstream, c->fev[0], 0));
     int rc = launch_broadcast_jobs(c->fstream, c->ftable, c->opts.bcast_ctas);
+    if (rc == OK) rc = launch_noise_vectors(st, c->ftable);
     if (rc != OK) return rc;
     rc = launch_frame_run(st, c->ftable, c->opts.frame_warps);
     if (rc != OK) return rc;
@@ -1429,9 +1443,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             std::vector<FrameRangeDev> ranges;
             std::vector<FrameSlotDev> fslots;
             std::vector<uint32_t> fs64, fev;
+            std::vector<int32_t> nvr;
             std::vector<FrameChanTab> ctabs;
             std::vector<uint32_t> surv;
-            const int jrc = frame_job_ranges(c, job, ranges, fslots, fs64, fev, ctabs, surv);
+            const int jrc = frame_job_ranges(c, job, ranges, fslots, fs64, fev, nvr, ctabs, surv);
             if (jrc == E_ARG) {
                 set_error("");  // the program does not fit the one-launch kernel: the per-shot plan runs
                 ok = false;
@@ -1443,10 +1458,19 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 FrameSlotDev *dsl = nullptr;
                 FrameChanTab *dct = nullptr;
                 uint32_t *dsv = nullptr, *ds64 = nullptr, *dev = nullptr;
+                int32_t *dnvr = nullptr;
                 if (upload(h, c->owned, ranges, &dr) || upload(h, c->owned, fslots, &dsl) ||
                     upload(h, c->owned, fs64, &ds64) || upload(h, c->owned, fev, &dev) || upload(h, c->owned, ctabs, &dct) ||
-                    upload(h, c->owned, surv, &dsv))
+                    upload(h, c->owned, surv, &dsv) || upload(h, c->owned, nvr, &dnvr))
                     return bail(E_CUDA);
+                job.nv_range = dnvr;
+                if (job.nnv > 0) {  // the noise vectors: [nnv][w][Wp] words
+                    void *pn = nullptr;
+                    const size_t nb = (size_t)job.nnv * (size_t)h->w * (size_t)frame_wp(h->n) * sizeof(u64);
+                    if (dev_alloc(h, &pn, nb) != OK) return bail(fail(E_NOMEM, "device allocation of noise vectors failed"));
+                    c->owned.push_back(pn);
+                    job.nvec = static_cast<u64 *>(pn);
+                }
                 job.ranges = dr;
                 job.slot = dsl;
                 job.slot_s64 = ds64;
@@ -1465,21 +1489,25 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 BroadcastJobDev bj{h->X, h->Z, c->d_fxz, h->n, h->w, c->fprog.nw64};
                 const std::vector<FrameJobDev> jobs{job};
                 const std::vector<BroadcastJobDev> bjobs{bj};
-                const std::vector<int64_t> cta0{0, h->w}, chunk0{0, broadcast_chunks(h->n, h->w)};
+                const std::vector<int64_t> cta0{0, h->w}, chunk0{0, broadcast_chunks(h->n, h->w)},
+                    ncta0{0, (int64_t)job.nnv * h->w};
                 FrameJobDev *dj = nullptr;
                 BroadcastJobDev *db = nullptr;
-                int64_t *dc = nullptr, *dk = nullptr;
+                int64_t *dc = nullptr, *dk = nullptr, *dn = nullptr;
                 if (upload(h, c->owned, jobs, &dj) || upload(h, c->owned, bjobs, &db) ||
-                    upload(h, c->owned, cta0, &dc) || upload(h, c->owned, chunk0, &dk))
+                    upload(h, c->owned, cta0, &dc) || upload(h, c->owned, chunk0, &dk) || upload(h, c->owned, ncta0, &dn))
                     return bail(E_CUDA);
                 c->ftable.jobs = dj;
                 c->ftable.bjobs = db;
                 c->ftable.cta0 = dc;
+                c->ftable.ncta0 = dn;
                 c->ftable.chunk0 = dk;
                 c->ftable.njobs = 1;
                 c->ftable.ctas = h->w;
+                c->ftable.nctas = ncta0[1];
                 c->ftable.chunks = chunk0[1];
                 c->ftable.smem = frame_job_smem(job);
+                c->ftable.nsmem = job.nnv > 0 ? noise_job_smem(job) : 0;
                 if (cudaStreamCreateWithFlags(&c->fstream, cudaStreamNonBlocking) != cudaSuccess)
                     return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
                 for (cudaEvent_t &e : c->fev)
@@ -1515,7 +1543,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     st.launches_per_run += 1;  // run-parameter update
     if (c->frame_ok) {  // runs from |0...0>: the parameters, the sign kernel, the broadcast
         st.shared_xz = 1;
-        st.launches_per_run = 3;
+        st.launches_per_run = c->ftable.nctas > 0 ? 4 : 3;
     }
     st.seg_rows = c->opts.seg_rows;
     st.seg_words = c->opts.seg_words;

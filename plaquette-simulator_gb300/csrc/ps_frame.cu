@@ -1,8 +1,12 @@
-// ps_frame.cu -- device side of shared-x/z runs (see ps_frame.h): the sign
-// program of a whole run over each shot-word's signs in ONE launch, and the
-// broadcast of the final x / z bits to every shot.  Both take a job table
-// (ps_frame_dev.h): a single circuit is a table of one job, a batch of
-// circuits is one table, so a batch run is these two launches too.
+// ps_frame.cu -- device side of shared-x/z runs (see ps_frame.h): three
+// kernels a run, each one launch for a whole job table (ps_frame_dev.h):
+//  - noise_vec_kernel: for every range with channels and every shot-word,
+//    the XOR that the range's channel outcomes make on the signs (one CTA
+//    each, independent of the signs, so all of them at once);
+//  - frame_run_kernel: the sign program of a whole run over each shot-word's
+//    signs, held in shared memory from start to end;
+//  - broadcast_jobs_kernel: the final x / z bits written to every shot,
+//    beside the other two.
 #include <algorithm>
 #include <mutex>
 #include <set>
@@ -13,15 +17,6 @@
 namespace ps {
 
 namespace {
-
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
-                 : "memory");
-}
 
 // Bulk copies (TMA, no tensor map) into shared memory, completed on an
 // mbarrier: one thread issues a copy of a whole contiguous block, every
@@ -85,59 +80,41 @@ __device__ __forceinline__ u64 outcome_quarter(const MeasOp &op, int sub, uint64
     return bits;
 }
 
-// One CTA of FW warps per shot-word k of a job runs the job's whole sign
-// program on its W signs, held in shared memory from start (all zero: the
-// run starts from |0...0>) to end.  Launch range by launch range:
-//  1. its ops and measurement tab words are copied to shared memory with
-//     cp.async (in flight during 2 and 3); the range's channel records were
-//     fetched the same way during the range before;
-//  2. the channel outcomes of its segment are drawn (the same draws as every
-//     other form) and each outcome flips the signs of its slot's rows;
-//  3. its random measurements' outcomes are drawn (they depend on no sign),
-//     two per warp;
-//  4. its ops run in order: F_LINEAR maps over all threads, other
-//     measurement ops on warp 0 (a window's measurements one per lane, the
-//     rows of other ops over the lanes).
-// So the critical path reads shared memory only, but for one batched fetch
-// of the hit channels' rows per range.  Records are written as they are
-// produced; the signs go back to R at the end.  Record m of a job lives at
-// rec + m*w (results) and rec + (nm + m)*w (determined flags).
-// At most 85 registers a thread (3 CTAs of 8 warps, or 6 of 4, per SM's
-// 64K): two sign CTAs then leave an SM room for the broadcast beside them.
-template <int FW>
-__global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const FrameJobDev *__restrict__ jobs, int njobs,
-                                                                     const int64_t *__restrict__ cta0) {
+// One CTA of NW warps per (range with channels, shot-word) of a job: the
+// XOR its channel outcomes make on the signs of the word's 64 shots.  A
+// first pass draws every channel's first number (a Philox block gives the
+// first numbers of four consecutive channel events: lane t draws the block
+// of group t, and in slice q lane t takes event 32q + t, whose number it
+// gets by shuffle, so that the S_64 words are read contiguously; no shot of
+// the word is hit unless the number is at least S_64, 94 % of channels at
+// p = 1e-3) and lists the hit channels with their first numbers.  Then a
+// thread per hit samples its word (channel_word_est_hit: the same draws as
+// every other form) and flips its slot's rows in the sum (32-bit shared
+// atomics: XORs commute, and two slots may share a row).
+template <int NW>
+__global__ void __launch_bounds__(32 * NW) noise_vec_kernel(const FrameJobDev *__restrict__ jobs, int njobs,
+                                                            const int64_t *__restrict__ ncta0) {
     extern __shared__ __align__(16) u64 sm[];
-    constexpr int NT = 32 * FW;
+    constexpr int NT = 32 * NW;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int j = njobs > 1 ? job_of(cta0, njobs, (int64_t)blockIdx.x) : 0;
+    const int j = njobs > 1 ? job_of(ncta0, njobs, (int64_t)blockIdx.x) : 0;
     const FrameJobDev &J = jobs[j];
-    const int64_t n = J.n, w = J.w, W = 2 * n + 1, nm = J.nm;
-    const int64_t k = (int64_t)blockIdx.x - cta0[j];
-    const FrameSmem SL = frame_smem_layout(J);
+    const int64_t w = J.w, Wp = frame_wp(J.n);
+    const int64_t local = (int64_t)blockIdx.x - ncta0[j];
+    const int64_t v = local / w, k = local - v * w;
+    const FrameRangeDev L = J.ranges[J.nv_range[v]];
+    const NoiseSmem SL = noise_smem_layout(J);
     char *const sb8 = reinterpret_cast<char *>(sm);
-    u64 *const sR = sm;  // signs, the zero row W, kWinRows sink rows
-    u64 *const sout = reinterpret_cast<u64 *>(sb8 + SL.out);  // a range's random outcomes
-    uint32_t *const stab = reinterpret_cast<uint32_t *>(sb8 + SL.tab);
-    FrameOp *const sops = reinterpret_cast<FrameOp *>(sb8 + SL.ops);
-    u64 *const snew = reinterpret_cast<u64 *>(sb8 + SL.nw);  // F_LINEAR's new rows
-    FrameSlotDev *const sslot = reinterpret_cast<FrameSlotDev *>(sb8 + SL.slot);  // [2][max_slots rounded to 2]
-    uint32_t *const ss64 = reinterpret_cast<uint32_t *>(sb8 + SL.s64);             // [2][max_slots rounded to 4]
-    uint32_t *const srow = reinterpret_cast<uint32_t *>(sb8 + SL.row);             // the chunk's hit rows
-    u64 *const shm = reinterpret_cast<u64 *>(sb8 + SL.hm);                         // the chunk's outcome masks (4 a hit)
-    uint32_t *const shrow = reinterpret_cast<uint32_t *>(sb8 + SL.hrow);           // its first staged row (or ~0u)
-    uint32_t *const shlen = reinterpret_cast<uint32_t *>(sb8 + SL.hlen);           // its staged row count
-    uint32_t *const shpre = reinterpret_cast<uint32_t *>(sb8 + SL.hpre);           // prefix of the counts
-    uint32_t *const swsum = reinterpret_cast<uint32_t *>(sb8 + SL.wsum);           // per-warp sums
-    uint32_t *const shit = reinterpret_cast<uint32_t *>(sb8 + SL.hit);    // hit channels: count, then (channel, first draw)
-    uint32_t *const srcnt = shit + 1;  // staged row words taken
+    u64 *const acc = sm;
+    uint32_t *const shit = reinterpret_cast<uint32_t *>(sb8 + SL.hit);  // hit channels: count, then (channel, first draw)
     uint32_t *const shitl = shit + 2;
-    uint64_t *const sbar = reinterpret_cast<uint64_t *>(sb8 + SL.bar);  // [0..1] channel records, [2] ops + tab
-    const FrameOp *const gops = J.ops;
+    u64 *const shm = reinterpret_cast<u64 *>(sb8 + SL.hm);               // the chunk's outcome masks (4 a hit)
+    uint32_t *const sht0 = reinterpret_cast<uint32_t *>(sb8 + SL.ht0);   // first row entry of each
+    uint32_t *const shlen = reinterpret_cast<uint32_t *>(sb8 + SL.hlen); // its row count
+    uint32_t *const shpre = reinterpret_cast<uint32_t *>(sb8 + SL.hpre); // prefix of the counts
+    uint32_t *const swsum = reinterpret_cast<uint32_t *>(sb8 + SL.wsum); // per-warp sums
     const uint32_t *const gtab = J.tab;
-    u64 *const rec = J.rec;
     const RunParams rp = *J.rp;
-    // channel tables: staged once when small, else read where they are
     const FrameChanTab *ctab = J.ctab;
     const uint64_t *thr = J.thr;
     const uint32_t *surv = J.surv;
@@ -152,239 +129,234 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
         thr = t2;
         surv = s2;
     }
+    for (int64_t i = tid; i < Wp; i += NT) acc[i] = 0ull;
+    if (tid == 0) *shit = 0u;
+    __syncthreads();
+    const uint32_t *const s64 = J.slot_s64 + L.s64_base;
+    const FrameSlotDev *const rec = J.slot + L.rec_base;
+    auto append = [&](bool hit, uint32_t slot, uint32_t u) {  // warp-aggregated; every lane calls it
+        const unsigned b = __ballot_sync(0xffffffffu, hit);
+        if (b == 0u) return;
+        uint32_t base = 0u;
+        if (lane == 0) base = atomicAdd(shit, (uint32_t)__popc(b));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (hit) {
+            const uint32_t at = base + __popc(b & ((1u << lane) - 1u));
+            shitl[2 * at] = slot;
+            shitl[2 * at + 1] = u;
+        }
+    };
+    if (L.ev0 >= 0) {
+        const uint64_t e0 = rp.event_base + (uint64_t)L.ev0, g0 = e0 >> 2;
+        const int64_t ngroups = (int64_t)(((e0 + (uint64_t)L.nslots - 1) >> 2) - g0 + 1);
+        for (int64_t wb = 32 * (int64_t)wid; wb < ngroups; wb += 32 * NW) {  // the warp's 32 groups
+            u32x4 blk{};
+            if (wb + lane < ngroups)
+                blk = draw_block(rp.seed, g0 + (uint64_t)(wb + lane), rp.word_base + (uint64_t)k, 0u, TAG_NOISE_FIRST);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int src = 8 * q + (lane >> 2);
+                uint32_t x[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) x[c] = __shfl_sync(0xffffffffu, blk.v[c], src);
+                const uint32_t u = (lane & 3) == 0 ? x[0] : (lane & 3) == 1 ? x[1] : (lane & 3) == 2 ? x[2] : x[3];
+                const int64_t sl = (int64_t)(4 * (g0 + (uint64_t)wb)) + 32 * q + lane - (int64_t)e0;
+                const bool hit = sl >= 0 && sl < L.nslots && u >= __ldg(s64 + sl);
+                append(hit, (uint32_t)sl, u);
+            }
+        }
+    } else {
+        for (int64_t ub = 0; ub < L.nslots; ub += NT) {
+            const int64_t unit = ub + tid;
+            bool hit = false;
+            uint32_t u = 0u;
+            if (unit < L.nslots) {
+                u = channel_first_draw(rp.seed, rp.event_base + J.slot_event[L.slot_base + unit], rp.word_base + (uint64_t)k);
+                hit = u >= __ldg(s64 + unit);
+            }
+            append(hit, (uint32_t)unit, u);
+        }
+    }
+    __syncthreads();
+    // The hits, NT at a time: a thread per hit (spread over the warps: hit
+    // c0 + l on lane l / NW of warp l % NW) samples its word, then all
+    // threads apply the chunk's rows together, row entry e on thread e % NT
+    // (its hit by binary search in the prefix of the row counts), so that a
+    // long row list does not hold its warp back.
+    const uint32_t nhit = *shit;
+    for (uint32_t c0 = 0; c0 < nhit; c0 += NT) {
+        const uint32_t l = (uint32_t)lane * NW + (uint32_t)wid, h = c0 + l;
+        uint32_t len = 0u;
+        if (h < nhit) {
+            const uint32_t s0 = shitl[2 * h];
+            const FrameSlotDev d = rec[s0];
+            const uint32_t tb = d.lt & 0xFFFu;
+            ChannelWord m{0ull, 0ull, 0ull, 0ull};
+            if (tb != kFrameNoHit) {  // (a channel that never hits has S_64 = 2^32 - 1)
+                const FrameChanTab ct = ctab[tb];
+                const uint32_t ev = L.ev0 >= 0 ? (uint32_t)L.ev0 + s0 : J.slot_event[L.slot_base + s0];
+                m = channel_word_est_hit(rp.seed, rp.event_base + ev, rp.word_base + (uint64_t)k, shitl[2 * h + 1],
+                                         thr + ct.thr_off, ct.count, surv + ct.surv_off, ct.est);
+                len = d.lt >> 12;
+            }
+            shm[4 * l + 0] = m.fxa;
+            shm[4 * l + 1] = m.fza;
+            shm[4 * l + 2] = m.fxb;
+            shm[4 * l + 3] = m.fzb;
+            sht0[l] = d.t0;
+        }
+        shlen[l] = len;
+        __syncthreads();
+        // exclusive prefix of the row counts, in chunk order (thread tid
+        // takes entry tid here)
+        const uint32_t mine = shlen[tid];
+        uint32_t x = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) swsum[wid] = x;
+        __syncthreads();
+        uint32_t woff = 0u, total = 0u;
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            const uint32_t vq = swsum[q];
+            woff += q < wid ? vq : 0u;
+            total += vq;
+        }
+        shpre[tid] = woff + x - mine;
+        __syncthreads();
+        for (uint32_t e = tid; e < total; e += NT) {
+            // the last hit with shpre <= e: it has rows (one without any
+            // shares its prefix with the next, and the last one's prefix is
+            // the total)
+            uint32_t lo = 0u, hi = NT - 1u;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1u) >> 1;
+                if (shpre[mid] <= e) lo = mid;
+                else hi = mid - 1u;
+            }
+            const uint32_t vr = __ldg(gtab + sht0[lo] + (e - shpre[lo])), sel = vr >> 28;
+            u64 f = 0ull;  // row | sel << 28: X on rows with z, Z on rows with x
+            if (sel & 1u) f ^= shm[4 * lo + 0];
+            if (sel & 2u) f ^= shm[4 * lo + 1];
+            if (sel & 4u) f ^= shm[4 * lo + 2];
+            if (sel & 8u) f ^= shm[4 * lo + 3];
+            unsigned *rw = reinterpret_cast<unsigned *>(&acc[vr & kFrameRowMask]);
+            if ((uint32_t)f) atomicXor(rw, (uint32_t)f);
+            if (f >> 32) atomicXor(rw + 1, (uint32_t)(f >> 32));
+        }
+        __syncthreads();  // the chunk applied before the next one reuses its arrays
+    }
+    __syncthreads();
+    u64 *const out = J.nvec + ((int64_t)v * w + k) * Wp;
+    for (int64_t i = tid; i < Wp; i += NT) out[i] = acc[i];
+}
+
+// One CTA of FW warps per shot-word k of a job runs the job's whole sign
+// program on its W signs, held in shared memory from start (all zero: the
+// run starts from |0...0>) to end.  Launch range by launch range:
+//  1. its ops and measurement tab words come to shared memory by a bulk
+//     copy (in flight during 2 and 3), and so does the noise vector of the
+//     next range with channels;
+//  2. its own noise vector (fetched during the range before) is XORed into
+//     the signs;
+//  3. its random measurements' outcomes are drawn (they depend on no sign),
+//     two per warp;
+//  4. its ops run in order: F_LINEAR maps over all threads, other
+//     measurement ops on warp 0 (a window's measurements one per lane, the
+//     rows of other ops over the lanes).
+// Records are written as they are produced; the signs go back to R at the
+// end.  Record m of a job lives at rec + m*w (results) and rec + (nm + m)*w
+// (determined flags).  At most 85 registers a thread (3 CTAs of 8 warps,
+// or 6 of 4, per SM's 64K): two sign CTAs then leave an SM room for the
+// broadcast beside them.
+template <int FW>
+__global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const FrameJobDev *__restrict__ jobs, int njobs,
+                                                                     const int64_t *__restrict__ cta0) {
+    extern __shared__ __align__(16) u64 sm[];
+    constexpr int NT = 32 * FW;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int j = njobs > 1 ? job_of(cta0, njobs, (int64_t)blockIdx.x) : 0;
+    const FrameJobDev &J = jobs[j];
+    const int64_t n = J.n, w = J.w, W = 2 * n + 1, nm = J.nm, wp = frame_wp(n);
+    const int64_t k = (int64_t)blockIdx.x - cta0[j];
+    const FrameSmem SL = frame_smem_layout(J);
+    char *const sb8 = reinterpret_cast<char *>(sm);
+    u64 *const sR = sm;  // signs, the zero row W, kWinRows sink rows
+    u64 *const sout = reinterpret_cast<u64 *>(sb8 + SL.out);  // a range's random outcomes
+    u64 *const snew = reinterpret_cast<u64 *>(sb8 + SL.nw);  // F_LINEAR's new rows
+    u64 *const snv = reinterpret_cast<u64 *>(sb8 + SL.nv);   // [2][wp] noise vectors
+    uint64_t *const sbar = reinterpret_cast<uint64_t *>(sb8 + SL.bar);  // [0..1] noise vectors, [2..3] tab + ops
+    // staging buffer b: tab words, then ops
+    auto stab_of = [&](int b) { return reinterpret_cast<uint32_t *>(sb8 + SL.tab + (size_t)b * SL.tabsz); };
+    auto sops_of = [&](int b) {
+        return reinterpret_cast<FrameOp *>(sb8 + SL.tab + (size_t)b * SL.tabsz + (size_t)J.stage_u32 * 4);
+    };
+    const FrameOp *const gops = J.ops;
+    const uint32_t *const gtab = J.tab;
+    u64 *const rec = J.rec;
+    const RunParams rp = *J.rp;
     for (int64_t i = tid; i < W + 1 + (int64_t)kWinRows; i += NT) sR[i] = 0ull;
-    // Bulk copies: the channel records and S_64 words of range li + 1 into
-    // buffer (li + 1) & 1 (barrier sbar[(li + 1) & 1]) while range li runs,
-    // and a range's ops and tab words at its start (sbar[2]); thread 0
-    // issues them.  Barrier phases flip with every completed copy.
+    // Bulk copies, issued by thread 0 while range li runs: the noise vector
+    // of range li + 1 (when it has channels) into buffer (li + 1) & 1
+    // (barrier sbar[(li + 1) & 1]), and its staged tab words and ops into
+    // buffer (li + 1) & 1 (barrier sbar[2 + ((li + 1) & 1)]).  Barrier
+    // phases flip with every completed copy.
     if (tid == 0) {
-        for (int b = 0; b < 3; ++b) mbar_init(sbar + b);
+        for (int b = 0; b < 4; ++b) mbar_init(sbar + b);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
-    uint32_t pend = 0u;  // thread 0: the barriers with a copy in flight (bits 0..2)
-    auto fetch_slots = [&](const FrameRangeDev &R, int buf) {  // thread 0; a range with channels
-        const uint32_t rb = (((uint32_t)R.nslots + 1u) & ~1u) * (uint32_t)sizeof(FrameSlotDev),
-                       sb = (((uint32_t)R.nslots + 3u) & ~3u) * 4u;
+    uint32_t pend = 0u;  // thread 0: the barriers with a copy in flight (bits 0..3)
+    auto fetch_nv = [&](const FrameRangeDev &R, int buf) {  // thread 0; a range with channels
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         pend |= 1u << buf;
-        mbar_expect(sbar + buf, rb + sb);
-        bulk_copy(sslot + (size_t)buf * ((J.max_slots + 1) & ~1u), J.slot + R.rec_base, rb, sbar + buf);
-        bulk_copy(ss64 + (size_t)buf * ((J.max_slots + 3) & ~3u), J.slot_s64 + R.s64_base, sb, sbar + buf);
+        mbar_expect(sbar + buf, (uint32_t)(wp * 8));
+        bulk_copy(snv + (int64_t)buf * wp, J.nvec + ((int64_t)R.nv * w + k) * wp, (uint32_t)(wp * 8), sbar + buf);
     };
-    uint32_t sph[2] = {0u, 0u}, tph = 0u;  // the phases the next waits look for
+    auto fetch_tab = [&](const FrameRangeDev &R, int buf) {  // thread 0; a staged range
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        pend |= 4u << buf;
+        mbar_expect(sbar + 2 + buf, R.ntab16 * 16u + (R.op1 - R.op0) * 16u);
+        if (R.ntab16) bulk_copy(stab_of(buf), gtab + R.tab0a, R.ntab16 * 16u, sbar + 2 + buf);
+        if (R.op1 > R.op0) bulk_copy(sops_of(buf), gops + R.op0, (R.op1 - R.op0) * 16u, sbar + 2 + buf);
+    };
+    uint32_t ph[4] = {0u, 0u, 0u, 0u};  // the phases the next waits look for
     // Waits (every thread) for barrier b's copy.  False when a wait gave up
     // in any thread: the error word is set, the copies still in flight are
     // waited for (bounded), and the caller leaves the kernel.
     auto wait_bar = [&](int b) -> bool {
-        uint32_t &ph = b < 2 ? sph[b] : tph;
-        const bool ok = mbar_wait(sbar + b, ph);
-        ph ^= 1u;
+        const bool ok = mbar_wait(sbar + b, ph[b]);
+        ph[b] ^= 1u;
         if (__syncthreads_or(!ok) == 0) {
             pend &= ~(1u << b);
             return true;
         }
         if (tid == 0) {
             atomicOr(J.err, kFrameErrWait);
-            for (int c = 0; c < 3; ++c)
-                if ((pend >> c) & 1u) (void)mbar_wait(sbar + c, c == b ? (ph ^ 1u) : (c < 2 ? sph[c] : tph));
+            for (int c = 0; c < 4; ++c)
+                if ((pend >> c) & 1u) (void)mbar_wait(sbar + c, c == b ? (ph[c] ^ 1u) : ph[c]);
         }
         return false;
     };
     FrameRangeDev L = J.ranges[0];
-    if (tid == 0 && L.nslots > 0) fetch_slots(L, 0);
+    if (tid == 0 && L.nv >= 0) fetch_nv(L, 0);
+    if (tid == 0 && L.stage) fetch_tab(L, 0);
     u64 last = 0ull;  // outcome of the latest measurement (its reset X)
     for (int li = 0; li < J.nranges; ++li) {
         const FrameRangeDev Ln = J.ranges[li + 1 < J.nranges ? li + 1 : li];  // in flight meanwhile
-        if (tid == 0) {
-            *shit = 0u;
-            *srcnt = 0u;
-            if (L.stage) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                pend |= 4u;
-                mbar_expect(sbar + 2, L.ntab16 * 16u + (L.op1 - L.op0) * 16u);
-                if (L.ntab16) bulk_copy(stab, gtab + L.tab0a, L.ntab16 * 16u, sbar + 2);
-                if (L.op1 > L.op0) bulk_copy(sops, gops + L.op0, (L.op1 - L.op0) * 16u, sbar + 2);
-            }
-        }
-        if (L.nslots > 0) {
+        // the next range's tab words and ops, into the buffer the range before used
+        if (tid == 0 && li + 1 < J.nranges && Ln.stage) fetch_tab(Ln, (li + 1) & 1);
+        // 2. the range's channel outcomes (its first op, F_NOISE)
+        if (L.nv >= 0) {
             if (!wait_bar(li & 1)) return;
-        } else {
-            __syncthreads();
+            const u64 *nv = snv + (int64_t)(li & 1) * wp;
+            for (int64_t i = tid; i < W; i += NT) sR[i] ^= nv[i];
         }
-        const FrameSlotDev *cs = sslot + (size_t)(li & 1) * ((J.max_slots + 1) & ~1u);
-        const uint32_t *cs64 = ss64 + (size_t)(li & 1) * ((J.max_slots + 3) & ~3u);
-        // 2. channel outcomes.  A first pass draws every channel's first
-        //    number (a Philox block gives the first numbers of four channels;
-        //    no shot of the word is hit unless it is at least S_64, 94 % of
-        //    channels at p = 1e-3) with all lanes converged, and lists the
-        //    hit channels with their first numbers.  Then a thread per hit
-        //    samples its word (channel_word_est_hit: the same draws as every
-        //    other form) and flips the signs of its slot's rows, prefetched
-        //    meanwhile (32-bit shared atomics: XORs commute, and two slots
-        //    may share a row).
-        if (L.nslots > 0) {
-            // every lane runs every iteration (the ballots below take the
-            // full warp); channels past the end just report no hit.  With
-            // consecutive events a warp takes 128 events at a time: lane t
-            // draws the block of group t (events 4t .. 4t + 3), and in slice
-            // q lane t takes event 32q + t, whose number it gets by shuffle,
-            // so that the S_64 words are read contiguously.  Else one block
-            // a channel.
-            const uint64_t e0 = rp.event_base + (uint64_t)(L.ev0 >= 0 ? L.ev0 : 0);
-            const uint64_t g0 = e0 >> 2;  // the first group
-            const int64_t nunits = L.ev0 >= 0 ? (int64_t)(((e0 + (uint64_t)L.nslots - 1) >> 2) - g0 + 1)
-                                              : (int64_t)L.nslots;
-            auto append = [&](bool hit, uint32_t slot, uint32_t u) {  // warp-aggregated
-                const unsigned b = __ballot_sync(0xffffffffu, hit);
-                if (b == 0u) return;
-                uint32_t base = 0u;
-                if (lane == 0) base = atomicAdd(shit, (uint32_t)__popc(b));
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (hit) {
-                    const uint32_t at = base + __popc(b & ((1u << lane) - 1u));
-                    shitl[2 * at] = slot;
-                    shitl[2 * at + 1] = u;
-                }
-            };
-            if (L.ev0 >= 0) {
-                for (int64_t wb = 32 * (int64_t)wid; wb < nunits; wb += 32 * FW) {  // the warp's 32 groups
-                    u32x4 blk{};
-                    if (wb + lane < nunits)
-                        blk = draw_block(rp.seed, g0 + (uint64_t)(wb + lane), rp.word_base + (uint64_t)k, 0u, TAG_NOISE_FIRST);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int src = 8 * q + (lane >> 2);
-                        uint32_t x[4];
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) x[c] = __shfl_sync(0xffffffffu, blk.v[c], src);
-                        const uint32_t u = (lane & 3) == 0 ? x[0] : (lane & 3) == 1 ? x[1] : (lane & 3) == 2 ? x[2] : x[3];
-                        const int64_t sl = (int64_t)(4 * (g0 + (uint64_t)wb)) + 32 * q + lane - (int64_t)e0;
-                        const bool hit = sl >= 0 && sl < L.nslots && u >= cs64[sl];
-                        append(hit, (uint32_t)sl, u);
-                    }
-                }
-            } else {
-                for (int64_t ub = 0; ub < nunits; ub += NT) {
-                    const int64_t unit = ub + tid;
-                    bool hit = false;
-                    uint32_t u = 0u;
-                    if (unit < nunits) {
-                        u = channel_first_draw(rp.seed, rp.event_base + J.slot_event[L.slot_base + unit],
-                                               rp.word_base + (uint64_t)k);
-                        hit = u >= cs64[unit];
-                    }
-                    append(hit, (uint32_t)unit, u);
-                }
-            }
-            __syncthreads();
-            const uint32_t nhit = *shit;
-            // The hits, kFrameHitChunk at a time.  A thread per hit (spread
-            // over the warps: hit c0 + l on lane l / FW of warp l % FW)
-            // stages the 16-byte-aligned cover of its slot's rows (16-byte
-            // copies; tab holds padding after its end) and samples its word
-            // meanwhile; then all threads apply the chunk's rows together,
-            // row entry e on thread e % NT (the hit by binary search in the
-            // prefix of the row counts), so that a long row list does not
-            // hold the CTA back.
-            for (uint32_t c0 = 0; c0 < nhit; c0 += kFrameHitChunk) {
-                const uint32_t cend = min(nhit, c0 + kFrameHitChunk);
-                if (tid == 0) *srcnt = 0u;
-                __syncthreads();
-                for (uint32_t l0 = 0; l0 < kFrameHitChunk; l0 += NT) {
-                    const uint32_t l = l0 + (uint32_t)lane * FW + (uint32_t)wid, h = c0 + l;
-                    if (h >= cend) continue;
-                    const uint32_t s0 = shitl[2 * h];
-                    const FrameSlotDev d = cs[s0];
-                    const uint32_t len = d.lt >> 12, t0 = d.t0;
-                    const uint32_t a0 = t0 & ~3u, span = ((t0 + len + 3u) & ~3u) - a0;
-                    const uint32_t pos = atomicAdd(srcnt, span);
-                    const bool staged = pos + span <= kFrameRowStage;
-                    if (staged)
-                        for (uint32_t c = 0; c < span; c += 4) cp_async16(srow + pos + c, gtab + a0 + c);
-                    ChannelWord m{0ull, 0ull, 0ull, 0ull};
-                    const uint32_t tb = d.lt & 0xFFFu;
-                    if (tb != kFrameNoHit) {  // (a channel that never hits has S_64 = 2^32 - 1)
-                        const FrameChanTab ct = ctab[tb];
-                        const uint32_t ev = L.ev0 >= 0 ? (uint32_t)L.ev0 + s0 : J.slot_event[L.slot_base + s0];
-                        m = channel_word_est_hit(rp.seed, rp.event_base + ev, rp.word_base + (uint64_t)k, shitl[2 * h + 1],
-                                                 thr + ct.thr_off, ct.count, surv + ct.surv_off, ct.est);
-                    }
-                    shm[4 * (h - c0) + 0] = m.fxa;
-                    shm[4 * (h - c0) + 1] = m.fza;
-                    shm[4 * (h - c0) + 2] = m.fxb;
-                    shm[4 * (h - c0) + 3] = m.fzb;
-                    shrow[h - c0] = staged ? pos + (t0 - a0) : ~0u;
-                    shlen[h - c0] = staged ? len : 0u;
-                    if (!staged) {  // rows that do not fit: applied now, from global memory
-                        for (uint32_t r = 0; r < len; ++r) {
-                            const uint32_t v = __ldg(gtab + t0 + r), sel = v >> 28;
-                            u64 f = 0ull;
-                            if (sel & 1u) f ^= m.fxa;
-                            if (sel & 2u) f ^= m.fza;
-                            if (sel & 4u) f ^= m.fxb;
-                            if (sel & 8u) f ^= m.fzb;
-                            unsigned *rw = reinterpret_cast<unsigned *>(&sR[v & kFrameRowMask]);
-                            if ((uint32_t)f) atomicXor(rw, (uint32_t)f);
-                            if (f >> 32) atomicXor(rw + 1, (uint32_t)(f >> 32));
-                        }
-                    }
-                }
-                asm volatile("cp.async.commit_group;\n" ::: "memory");
-                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-                __syncthreads();
-                // exclusive prefix of the chunk's staged row counts: each
-                // warp scans hits 32 w .. 32 w + 31 (every lane runs it)
-                const uint32_t nh = cend - c0;
-                uint32_t total = 0u;
-                for (uint32_t b0 = 0; b0 < nh; b0 += NT) {
-                    const uint32_t i = b0 + tid;
-                    const uint32_t len = i < nh ? shlen[i] : 0u;
-                    uint32_t x = len;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                        if (lane >= o) x += y;
-                    }
-                    if (lane == 31) swsum[wid] = x;
-                    __syncthreads();
-                    uint32_t woff = total, add = 0u;
-#pragma unroll
-                    for (int q = 0; q < FW; ++q) {
-                        const uint32_t v = swsum[q];
-                        woff += q < wid ? v : 0u;
-                        add += v;
-                    }
-                    if (i < nh) shpre[i] = woff + x - len;
-                    total += add;
-                    __syncthreads();
-                }
-                for (uint32_t e = tid; e < total; e += NT) {
-                    // the last hit with shpre <= e: it has staged rows (a hit
-                    // without any shares its prefix with the next one, and
-                    // the last one's prefix is the total)
-                    uint32_t lo = 0u, hi = nh - 1u;
-                    while (lo < hi) {
-                        const uint32_t mid = (lo + hi + 1u) >> 1;
-                        if (shpre[mid] <= e) lo = mid;
-                        else hi = mid - 1u;
-                    }
-                    const uint32_t v = srow[shrow[lo] + (e - shpre[lo])], sel = v >> 28;
-                    u64 f = 0ull;  // row | sel << 28: X on rows with z, Z on rows with x
-                    if (sel & 1u) f ^= shm[4 * lo + 0];
-                    if (sel & 2u) f ^= shm[4 * lo + 1];
-                    if (sel & 4u) f ^= shm[4 * lo + 2];
-                    if (sel & 8u) f ^= shm[4 * lo + 3];
-                    unsigned *rw = reinterpret_cast<unsigned *>(&sR[v & kFrameRowMask]);
-                    if ((uint32_t)f) atomicXor(rw, (uint32_t)f);
-                    if (f >> 32) atomicXor(rw + 1, (uint32_t)(f >> 32));
-                }
-                __syncthreads();  // the chunk applied before the next one reuses the staging
-            }
-            __syncthreads();  // every hit applied before the ops
-        }
-        // the next range's channel records, into the buffer range li - 1 used
-        if (tid == 0 && li + 1 < J.nranges && Ln.nslots > 0) fetch_slots(Ln, (li + 1) & 1);
+        // the next range's noise vector, into the buffer the range before used
+        if (tid == 0 && li + 1 < J.nranges && Ln.nv >= 0) fetch_nv(Ln, (li + 1) & 1);
         // 3. random outcomes: half-warps, one Philox block per lane
         for (uint32_t r0 = 2u * (uint32_t)wid; r0 < L.nrand; r0 += 2u * FW) {
             const uint32_t r = r0 + (uint32_t)(lane >> 4);
@@ -397,17 +369,19 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
             if ((lane & 15) == 0 && r < L.nrand) sout[r] = bits;
         }
         if (L.stage) {
-            if (!wait_bar(2)) return;
+            if (!wait_bar(2 + (li & 1))) return;
         } else {
             __syncthreads();
         }
+        const uint32_t *const stab = stab_of(li & 1);
+        const FrameOp *const sops = sops_of(li & 1);
         // 4. the ops
         const uint32_t *T = L.stage ? stab : gtab;  // measurement-op tab, indexed x - tb
         const uint32_t tb = L.stage ? L.tab0a : 0u;
         for (uint32_t oi = L.op0; oi < L.op1; ++oi) {
             const FrameOp o = L.stage ? sops[oi - L.op0] : gops[oi];
             const uint32_t kind = o.kind & 0xFFu;
-            if (kind == F_NOISE) continue;  // applied in 2 (always a range's first op)
+            if (kind == F_NOISE) continue;  // applied in 2
             if (kind == F_LINEAR) {
                 // every output from the signs as they were, then the new rows
                 __syncthreads();  // warp 0's measurement ops before
@@ -499,7 +473,7 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
                 __syncwarp();
             }
         }
-        __syncthreads();  // the range's ops done before the next range's staging and channel flips
+        __syncthreads();  // the range's ops done before the next range's staging and noise
         L = Ln;
     }
     for (int64_t i = tid; i < W; i += NT) J.R[i * w + k] = sR[i];
@@ -508,12 +482,40 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
 // x / z of every shot from the shared bits.  A warp takes one chunk: one
 // (row, qubit) pair of a job whose rows are at least 32 words wide (lanes
 // over 16-byte word pairs), or 32 / (w/2) pairs of a narrower one.  Chunks
-// of a job are consecutive (chunk0).
+// of a job are consecutive (chunk0).  A warp steps through its chunks c,
+// c + warps, ...; in a one-job table the wide form's (row, qubit) advances by
+// a constant step, so only the first pair takes a division.  The stores are
+// streaming (evict first): the broadcast passes 1.65 GB through L2 at
+// d = 15 and must not evict the tables of the kernels beside it.
 __global__ void __launch_bounds__(256) broadcast_jobs_kernel(const BroadcastJobDev *__restrict__ jobs, int njobs,
                                                              const int64_t *__restrict__ chunk0, int64_t chunks) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks; c += warps) {
+    const int64_t c0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (njobs == 1 && (jobs[0].w >> 1) >= 16) {
+        const BroadcastJobDev &B = jobs[0];
+        const int64_t hw = B.w >> 1, n = B.n;
+        const int64_t drow = warps / n, dq = warps - drow * n;
+        int64_t row = c0 / n, q = c0 - row * n;
+        for (int64_t c = c0; c < chunks; c += warps) {
+            const u64 xb = (B.xz[(row * 2 + 0) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+            const u64 zb = (B.xz[(row * 2 + 1) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+            const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
+            u64 *xo = B.X + c * B.w, *zo = B.Z + c * B.w;
+            for (int64_t kp = lane; kp < hw; kp += 32) {
+                __stcs(reinterpret_cast<ulonglong2 *>(xo + 2 * kp), xv);
+                __stcs(reinterpret_cast<ulonglong2 *>(zo + 2 * kp), zv);
+            }
+            q += dq;
+            row += drow;
+            if (q >= n) {
+                q -= n;
+                ++row;
+            }
+        }
+        return;
+    }
+    for (int64_t c = c0; c < chunks; c += warps) {
         const int j = njobs > 1 ? job_of(chunk0, njobs, c) : 0;
         const BroadcastJobDev &B = jobs[j];
         const int64_t hw = B.w >> 1, pairs = (2 * B.n + 1) * B.n, local = c - chunk0[j];
@@ -534,8 +536,6 @@ __global__ void __launch_bounds__(256) broadcast_jobs_kernel(const BroadcastJobD
         const u64 zb = (B.xz[(row * 2 + 1) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
         const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
         u64 *xo = B.X + rq * B.w, *zo = B.Z + rq * B.w;
-        // streaming stores (evict first): the broadcast passes 1.65 GB through
-        // L2 at d = 15 and must not evict the sign kernel's tables beside it
         for (int64_t kp = kp0; kp < hw; kp += step) {
             __stcs(reinterpret_cast<ulonglong2 *>(xo + 2 * kp), xv);
             __stcs(reinterpret_cast<ulonglong2 *>(zo + 2 * kp), zv);
@@ -563,23 +563,26 @@ int same_carveout(const void *kernel) {
     return OK;
 }
 
+int prio_greatest() {
+    if (g_prio_greatest == 1) {
+        int least = 0, greatest = 0;
+        PS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        g_prio_greatest = greatest;
+    }
+    return OK;
+}
+
 template <int FW>
 int launch_frame_fw(cudaStream_t st, const FrameTable &t) {
     if (t.smem > 48 * 1024) {
         const int rc = allow_max_smem((const void *)frame_run_kernel<FW>);
         if (rc != OK) return rc;
     }
-    {
-        const int rc = same_carveout((const void *)frame_run_kernel<FW>);
-        if (rc != OK) return rc;
-    }
+    int rc = same_carveout((const void *)frame_run_kernel<FW>);
+    if (rc == OK) rc = prio_greatest();
+    if (rc != OK) return rc;
     // The sign kernel is the plan's critical path: launched at the highest
     // priority, its CTAs go ahead of the broadcast's queued CTAs.
-    if (g_prio_greatest == 1) {
-        int least = 0, greatest = 0;
-        PS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        g_prio_greatest = greatest;
-    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)t.ctas);
     cfg.blockDim = dim3(32 * FW);
@@ -599,6 +602,38 @@ int launch_frame_fw(cudaStream_t st, const FrameTable &t) {
 
 size_t frame_smem_bytes(int64_t n) {  // rows, the zero row, kWinRows sink rows
     return (size_t)(2 * n + 2 + kWinRows) * sizeof(u64);
+}
+
+int launch_noise_vectors(cudaStream_t st, const FrameTable &t) {
+    if (t.njobs <= 0 || t.nctas <= 0) return OK;
+    if (t.nsmem > kSegSmemMax) return fail(E_ARG, "channel noise does not fit in shared memory");
+    // At most six noise CTAs an SM (8K registers each): the broadcast's two
+    // CTAs (16K registers) always find room beside them, whichever of the
+    // two kernels reaches the SMs first.
+    const size_t smem = std::max<size_t>(t.nsmem, kNoiseSmemFloor);
+    if (t.nctas > 0x7FFFFFFFll) return fail(E_ARG, "channel noise: too many (range, shot-word) pairs in one launch");
+    const void *kern = (const void *)noise_vec_kernel<kNoiseWarps>;
+    cudaLaunchConfig_t cfg;
+    if (smem > 48 * 1024) {
+        const int rc = allow_max_smem(kern);
+        if (rc != OK) return rc;
+    }
+    int rc = same_carveout(kern);
+    if (rc == OK) rc = prio_greatest();
+    if (rc != OK) return rc;
+    cfg = {};
+    cfg.gridDim = dim3((unsigned)t.nctas);
+    cfg.blockDim = dim3(32 * kNoiseWarps);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;  // on the critical path too, ahead of the sign kernel
+    attr[0].val.priority = g_prio_greatest;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PS_CUDA(cudaLaunchKernelEx(&cfg, noise_vec_kernel<kNoiseWarps>, t.jobs, (int)t.njobs, t.ncta0));
+    PS_CUDA(cudaGetLastError());
+    return OK;
 }
 
 int launch_frame_run(cudaStream_t st, const FrameTable &t, int warps) {

@@ -1,7 +1,8 @@
 // ps_frame_dev.h -- device descriptors of shared-x/z runs (ps_frame.h): the
-// job table of the one-launch sign-program kernel and of the x / z broadcast.
-// A single circuit is a table of one job; a batch puts all of its jobs in one
-// table, so each of the two kernels is one launch for the whole batch.
+// job table of the three kernels of a run -- the channel noise of every
+// range and shot-word, the one-launch sign program, the x / z broadcast.  A
+// single circuit is a table of one job; a batch puts all of its jobs in one
+// table, so each kernel is one launch for the whole batch.
 #pragma once
 #include "ps_frame.h"
 #include "ps_internal.h"
@@ -35,12 +36,8 @@ struct FrameChanTab {
 };
 
 // The channel tables are staged in shared memory when they take at most
-// kFrameTabStage bytes.  A range's hits are taken kFrameHitChunk at a time;
-// their rows are staged in shared memory, up to kFrameRowStage words a chunk
-// (a hit whose rows do not fit applies them alone, from global memory).
+// kFrameTabStage bytes.
 constexpr uint32_t kFrameTabStage = 4096;
-constexpr uint32_t kFrameHitChunk = 256;
-constexpr uint32_t kFrameRowStage = 2048;
 
 // One launch range of a sign program (FrameProgram::Launch): its segment's
 // channel outcomes, drawn and applied first, then ops [op0, op1).
@@ -54,7 +51,8 @@ struct FrameRangeDev {
     int32_t ev0;             // >= 0: the channels' events are ev0, ev0 + 1, ... (first draws by groups of four)
     uint32_t s64_base;       // slot_s64 index of the segment's first S_64 word (a multiple of 4)
     uint32_t rec_base;       // slot index of the segment's first channel record (even: 16-byte aligned)
-    uint32_t pad[2];
+    int32_t nv;              // >= 0: its noise vectors are block nv of the job's nvec
+    uint32_t pad;
 };
 
 // One job: a sign program over the signs R of every shot-word of one state.
@@ -86,7 +84,16 @@ struct FrameJobDev {
     uint32_t max_rand, stage_u32, max_ops, max_scratch, max_slots;
     uint32_t n_ctab, n_thr, n_surv, stage_tabs, pad2;
     int32_t *err;  // set to kFrameErrWait when a bounded wait gave up (the run's results are void)
+    // Noise vectors: for the nnv ranges with channels (range index
+    // nv_range[v]), the XOR that the range's channel outcomes make on the
+    // signs of shot-word k: nvec[(v * w + k) * Wp + row], Wp = W rounded up
+    // to even (16-byte rows).
+    u64 *nvec;
+    const int32_t *nv_range;
+    int32_t nnv;
+    int32_t pad3;
 };
+__host__ __device__ inline int64_t frame_wp(int64_t n) { return (2 * n + 2) & ~(int64_t)1; }
 
 // A sign CTA gives up on an asynchronous copy after this many polls of its
 // barrier (each poll may suspend the thread for a while), sets the job's
@@ -95,43 +102,60 @@ constexpr uint32_t kFrameWaitLimit = 1u << 22;
 constexpr int32_t kFrameErrWait = 1;
 
 // Shared-memory layout of the sign kernel for one job (byte offsets):
-// signs (W rows, the zero row, kWinRows sink rows), random outcomes, staged
-// tab words, staged ops, F_LINEAR's new rows, two buffers of channel
-// records and two of their S_64 words (the range's, the next one's being
-// fetched), the channel tables, the hit rows, a chunk of hits (outcome
-// masks, first staged row, row count, prefix of the counts), per-warp sums,
-// the hit list (count, staged row words, then channel and first draw of
-// each hit), the barriers of the bulk copies (channel records: two, staged
-// ops and tab words: one).
+// signs (W rows, the zero row, kWinRows sink rows), random outcomes, two
+// buffers of staged tab words and ops (the range's, the next one's being
+// fetched; buffer b's ops follow its tab words), F_LINEAR's new rows, two
+// noise-vector buffers, the barriers of the bulk copies (noise vectors: two,
+// staged tab words and ops: two).
 struct FrameSmem {
-    size_t out, tab, ops, nw, slot, s64, tabs, row, hm, hrow, hlen, hpre, wsum, hit, bar, total;
+    size_t out, tab, tabsz, nw, nv, bar, total;
 };
 __host__ __device__ inline size_t frame_align16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline FrameSmem frame_smem_layout(const FrameJobDev &j) {
     FrameSmem L;
     L.out = (size_t)(2 * j.n + 2 + kWinRows) * 8;
     L.tab = frame_align16(L.out + (size_t)j.max_rand * 8);
-    L.ops = L.tab + (size_t)j.stage_u32 * 4;
-    L.nw = L.ops + (size_t)j.max_ops * 16;
-    L.slot = frame_align16(L.nw + (size_t)j.max_scratch * 8);
-    L.s64 = frame_align16(L.slot + (size_t)2 * ((j.max_slots + 1) & ~1u) * sizeof(FrameSlotDev));
-    L.tabs = frame_align16(L.s64 + (size_t)2 * ((j.max_slots + 3) & ~3u) * 4);
-    L.row = frame_align16(L.tabs + (j.stage_tabs ? (size_t)j.n_ctab * sizeof(FrameChanTab) + (size_t)j.n_thr * 8 +
-                                                       (size_t)j.n_surv * 4
-                                                 : 0));
-    L.hm = L.row + (size_t)kFrameRowStage * 4;
-    L.hrow = L.hm + (size_t)kFrameHitChunk * 32;
-    L.hlen = L.hrow + (size_t)kFrameHitChunk * 4;
-    L.hpre = L.hlen + (size_t)kFrameHitChunk * 4;
-    L.wsum = L.hpre + (size_t)kFrameHitChunk * 4;
-    L.hit = L.wsum + 16 * 4;
-    L.bar = frame_align16(L.hit + (size_t)(2 * j.max_slots + 2) * 4);
+    L.tabsz = (size_t)j.stage_u32 * 4 + (size_t)j.max_ops * 16;  // one buffer
+    L.nw = L.tab + 2 * L.tabsz;
+    L.nv = frame_align16(L.nw + (size_t)j.max_scratch * 8);
+    L.bar = L.nv + (j.nnv > 0 ? (size_t)2 * (size_t)frame_wp(j.n) * 8 : 0);
     L.total = L.bar + 32;
     return L;
 }
 
 // Shared memory the sign kernel needs for a job.
 inline size_t frame_job_smem(const FrameJobDev &j) { return frame_smem_layout(j).total; }
+
+// The noise kernel runs kNoiseWarps warps a CTA and takes the hits of its
+// range kNoiseChunk (one per thread) at a time.
+constexpr int kNoiseWarps = 4;
+constexpr uint32_t kNoiseChunk = 32 * kNoiseWarps;
+// The noise kernel asks for at least this much shared memory a CTA, which
+// keeps it to six CTAs an SM.
+constexpr size_t kNoiseSmemFloor = 36 * 1024;
+
+// Shared-memory layout of the noise kernel for one job: the noise vector
+// being summed (Wp words), a chunk of hits (outcome masks, first row entry,
+// row count, prefix of the counts), per-warp sums, the channel tables when
+// staged, the hit list (count, then channel and first draw of each hit).
+struct NoiseSmem {
+    size_t hm, ht0, hlen, hpre, wsum, tabs, hit, total;
+};
+__host__ __device__ inline NoiseSmem noise_smem_layout(const FrameJobDev &j) {
+    NoiseSmem L;
+    L.hm = (size_t)frame_wp(j.n) * 8;
+    L.ht0 = L.hm + (size_t)kNoiseChunk * 32;
+    L.hlen = L.ht0 + (size_t)kNoiseChunk * 4;
+    L.hpre = L.hlen + (size_t)kNoiseChunk * 4;
+    L.wsum = L.hpre + (size_t)kNoiseChunk * 4;
+    L.tabs = L.wsum + 16 * 4;
+    L.hit = frame_align16(L.tabs + (j.stage_tabs ? (size_t)j.n_ctab * sizeof(FrameChanTab) + (size_t)j.n_thr * 8 +
+                                                       (size_t)j.n_surv * 4
+                                                 : 0));
+    L.total = L.hit + (size_t)(2 * j.max_slots + 2) * 4;
+    return L;
+}
+inline size_t noise_job_smem(const FrameJobDev &j) { return noise_smem_layout(j).total; }
 
 // One job of the x / z broadcast: X and Z of every (row, qubit) pair and
 // shot-word := the shared bits xz ([W][2][nw64]).
@@ -151,18 +175,23 @@ inline int64_t broadcast_chunks(int64_t n, int64_t w) {
 }
 
 // A table of jobs on the device: jobs[njobs], cta0[njobs + 1] (first CTA of
-// each job in the sign kernel, prefix sums of w) and chunk0[njobs + 1] (first
-// broadcast chunk of each job, prefix sums of broadcast_chunks).
+// each job in the sign kernel, prefix sums of w), ncta0[njobs + 1] (first CTA
+// of each job in the noise kernel, prefix sums of nnv * w) and chunk0[njobs +
+// 1] (first broadcast chunk of each job, prefix sums of broadcast_chunks).
 struct FrameTable {
     const FrameJobDev *jobs = nullptr;
     const BroadcastJobDev *bjobs = nullptr;
     const int64_t *cta0 = nullptr;
+    const int64_t *ncta0 = nullptr;
     const int64_t *chunk0 = nullptr;
     int32_t njobs = 0;
-    int64_t ctas = 0, chunks = 0;  // totals
-    size_t smem = 0;               // largest frame_job_smem of the table
+    int64_t ctas = 0, nctas = 0, chunks = 0;  // totals
+    size_t smem = 0;                          // largest frame_job_smem of the table
+    size_t nsmem = 0;                         // largest noise_job_smem of the table
 };
 
+// The noise vectors of every job (nothing when no job has channels).
+int launch_noise_vectors(cudaStream_t st, const FrameTable &t);
 // Sign-kernel warps per CTA the launch uses (4 or 8; 0 = 8).
 int launch_frame_run(cudaStream_t st, const FrameTable &t, int warps);
 // The x / z broadcast of every job; ctas_per_sm 0 = 2 (room for the sign

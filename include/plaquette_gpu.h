@@ -239,6 +239,15 @@ typedef struct ps_circuit ps_circuit;
  * first_record .. first_record + num_measurements - 1). */
 ps_status ps_circuit_compile(ps_state *h, const ps_op *ops, uint64_t nops, const float *params, uint64_t nparams,
                              const ps_circuit_options *opts, ps_circuit **out);
+/* The compile cache (no counterpart in the reference): the shot-independent
+ * host work of ps_circuit_compile -- segment schedules, the measurement
+ * plan, the shared-x/z sign program -- is kept per process for the most
+ * recent 128 distinct (qubit count, options, op table, parameter table)
+ * keys, so a circuit compiled again (a served or batched job of a shape seen
+ * before) only allocates, uploads and captures.  Counts since the last
+ * clear; any pointer may be NULL. */
+ps_status ps_compile_cache_stats(uint64_t *hits, uint64_t *misses, uint64_t *entries);
+ps_status ps_compile_cache_clear(void);
 /* Forced random draws for the circuit's measurements: num_measurements rows
  * of ceil(batch/8) bytes, or NULL to return to Philox draws. */
 ps_status ps_circuit_set_forced(ps_circuit *c, const uint8_t *forced_all);
@@ -369,6 +378,7 @@ typedef struct {
 
 typedef struct {
     uint64_t submitted, completed, failed, queued, active;
+    uint64_t cancelled;              /* taken out of the queue by ps_server_cancel */
     uint64_t shot_gates_completed;
     uint64_t pool_bytes, pool_peak_bytes;
     double p50_latency_s, p99_latency_s, mean_latency_s, max_latency_s;
@@ -387,6 +397,10 @@ ps_status ps_server_wait(ps_server *s, uint64_t job_id, double timeout_s, ps_job
 ps_status ps_server_copy_records(ps_server *s, uint64_t job_id, uint64_t *results, uint64_t *determined);
 /* Drops the finished job's host records. */
 ps_status ps_server_release(ps_server *s, uint64_t job_id);
+/* Takes a job that is still queued out of the queue; waiting for it then
+ * reports PS_E_STATE.  A job already admitted runs to its end (its kernels
+ * are on the device): PS_E_STATE. */
+ps_status ps_server_cancel(ps_server *s, uint64_t job_id);
 /* Waits until no job is queued or active (timeout_s < 0: no limit). */
 ps_status ps_server_drain(ps_server *s, double timeout_s);
 /* Latency percentiles over every job completed so far. */

@@ -393,7 +393,7 @@ struct SrvJob {
     size_t bytes = 0;
     uint64_t shot_gates = 0;
     double t_submit = 0, t_admit = 0, t_done = 0;
-    uint64_t retry_after = UINT64_MAX;  // re-admit only after this many completions
+    uint64_t retry_after = UINT64_MAX;  // re-admit only after this many jobs finished
     bool done = false;
     int status = OK;
     std::string err;
@@ -417,7 +417,8 @@ struct ps_server {
     size_t reserved = 0;
     int active = 0;
     bool stop = false;
-    uint64_t next_id = 1, submitted = 0, completed = 0, failed = 0, shot_gates = 0;
+    uint64_t next_id = 1, submitted = 0, completed = 0, failed = 0, cancelled = 0, shot_gates = 0;
+    uint64_t finished = 0;  // completed + failed: the jobs that gave their memory back
     std::vector<double> latencies;
     double first_submit = -1.0, last_done = 0.0;
     std::vector<std::thread> workers;
@@ -432,7 +433,7 @@ SrvJob *pick_job(ps_server *s, double now) {
     if (s->active >= s->opts.max_active) return nullptr;
     for (size_t i = 0; i < s->queue.size(); ++i) {
         SrvJob *j = s->queue[i];
-        const bool waiting_retry = j->retry_after != UINT64_MAX && s->completed <= j->retry_after;
+        const bool waiting_retry = j->retry_after != UINT64_MAX && s->finished <= j->retry_after;
         if (!waiting_retry && s->reserved + j->bytes <= s->pool.cap) {
             s->queue.erase(s->queue.begin() + (std::ptrdiff_t)i);
             return j;
@@ -494,21 +495,21 @@ void worker_main(ps_server *s) {
             s->active--;
             if (rc == E_NOMEM && s->active > 0) {
                 // The pool is fragmented right now: wait for another job to finish.
-                j->retry_after = s->completed;
+                j->retry_after = s->finished;
                 j->err.clear();
                 s->queue.push_front(j);
             } else {
                 j->status = rc;
                 j->t_done = seconds_since(s->t0);
                 j->done = true;
+                s->finished++;
                 if (rc == OK) {
                     s->completed++;
                     s->shot_gates += j->shot_gates;
                     s->latencies.push_back(j->t_done - j->t_submit);
                     s->last_done = std::max(s->last_done, j->t_done);
                 } else {
-                    s->failed++;
-                    s->completed++;
+                    s->failed++;  // its latency is not counted
                 }
             }
         }
@@ -635,6 +636,29 @@ ps_status ps_server_release(ps_server *s, uint64_t job_id) {
     return OK;
 }
 
+ps_status ps_server_cancel(ps_server *s, uint64_t job_id) {
+    ps_enter(__func__, __LINE__);
+    if (!s) return fail(E_ARG, "null server");
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->jobs.find(job_id);
+        if (it == s->jobs.end()) return fail(E_RANGE, "unknown job " + std::to_string(job_id));
+        SrvJob *j = it->second.get();
+        auto q = std::find(s->queue.begin(), s->queue.end(), j);
+        if (q == s->queue.end())
+            return fail(E_STATE, "job " + std::to_string(job_id) + " is not queued (already admitted or done)");
+        s->queue.erase(q);
+        j->status = E_STATE;
+        j->err = "cancelled before it was admitted";
+        j->t_done = seconds_since(s->t0);
+        j->done = true;
+        s->cancelled++;
+    }
+    s->cv_work.notify_all();
+    s->cv_done.notify_all();
+    return OK;
+}
+
 ps_status ps_server_drain(ps_server *s, double timeout_s) {
     ps_enter(__func__, __LINE__);
     if (!s) return fail(E_ARG, "null server");
@@ -655,6 +679,7 @@ ps_status ps_server_get_stats(ps_server *s, ps_server_stats *out) {
     out->submitted = s->submitted;
     out->completed = s->completed;
     out->failed = s->failed;
+    out->cancelled = s->cancelled;
     out->queued = s->queue.size();
     out->active = (uint64_t)s->active;
     out->shot_gates_completed = s->shot_gates;

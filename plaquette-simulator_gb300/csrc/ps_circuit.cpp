@@ -6,6 +6,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <deque>
+#include <memory>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -87,6 +89,67 @@ template <class T> int upload(ps_state *h, std::vector<void *> &owned, const std
     PS_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
     *out = static_cast<T *>(p);
     return OK;
+}
+
+// ---- compile cache ------------------------------------------------------
+// The host-side products of compiling one circuit -- the plan's steps, the
+// fused segments' schedules, the measurement list and the shared-x/z sign
+// program -- depend on the qubit count, the options, whether the state is a
+// valid tableau, and the op and parameter tables, but not on the shots, the
+// seed or any device memory.  They are kept per process (the most recent
+// kPlanCacheMax), so that compiling a circuit again (a served or batched
+// job of a shape seen before) only allocates, uploads and captures.
+struct PlanCacheEntry {
+    std::vector<Step> steps;
+    std::vector<SegHost> segs;      // host fields only (no device pointers)
+    std::vector<MeasOp> meas;       // without record or forced pointers
+    std::vector<int32_t> meas_op;
+    bool has_frame = false;
+    FrameProgram fprog;
+};
+constexpr size_t kPlanCacheMax = 128;
+std::mutex g_plan_mu;
+std::map<std::string, std::shared_ptr<const PlanCacheEntry>> g_plan;
+std::deque<std::string> g_plan_order;  // insertion order, oldest first
+uint64_t g_plan_hits = 0, g_plan_misses = 0;
+
+std::string plan_key(const ps_state *h, const ps_circuit_options &o, const std::vector<ps_op> &ops, const float *params,
+                     uint64_t nparams) {
+    std::string k;
+    auto put = [&](const void *p, size_t n) { k.append(static_cast<const char *>(p), n); };
+    const int64_t n = h->n;
+    const int32_t valid = h->valid ? 1 : 0;
+    const uint64_t nops = ops.size();
+    put(&n, sizeof n);
+    put(&valid, sizeof valid);
+    put(&o, sizeof o);
+    put(&nops, sizeof nops);
+    if (nops) put(ops.data(), nops * sizeof(ps_op));
+    put(&nparams, sizeof nparams);
+    if (nparams) put(params, nparams * sizeof(float));
+    return k;
+}
+
+std::shared_ptr<const PlanCacheEntry> plan_lookup(const std::string &key) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_plan.find(key);
+    if (it == g_plan.end()) {
+        ++g_plan_misses;
+        return nullptr;
+    }
+    ++g_plan_hits;
+    return it->second;
+}
+
+void plan_store(const std::string &key, std::shared_ptr<const PlanCacheEntry> e) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (g_plan.count(key)) return;
+    g_plan[key] = std::move(e);
+    g_plan_order.push_back(key);
+    while (g_plan_order.size() > kPlanCacheMax) {
+        g_plan.erase(g_plan_order.front());
+        g_plan_order.pop_front();
+    }
 }
 
 }  // namespace
@@ -1251,7 +1314,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         c->d_masks = (u64 *)p;
     }
 
-    // ---- plan
+    // ---- plan (from the cache when this circuit was compiled before)
+    const std::string pkey = plan_key(h, c->opts, ops, params, nparams);
+    const std::shared_ptr<const PlanCacheEntry> cached = fused ? plan_lookup(pkey) : nullptr;
+    std::shared_ptr<PlanCacheEntry> fresh;
     auto add_meas = [&](size_t i, int reset) {
         MeasOp m{};
         m.q = ops[i].a;
@@ -1291,6 +1357,17 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             }
             c->steps.push_back(s);
         }
+    } else if (cached) {
+        c->steps = cached->steps;
+        c->segs = cached->segs;
+        c->meas = cached->meas;
+        c->meas_op = cached->meas_op;
+        for (size_t m = 0; m < c->meas.size(); ++m) {  // this compile's records
+            const Record &r = h->recs[(size_t)c->rec_ids[(size_t)rec_of[(size_t)c->meas_op[m]]]];
+            c->meas[m].res = r.res;
+            c->meas[m].det = r.det;
+        }
+        for (const SegHost &sg : c->segs) max_slots = std::max(max_slots, sg.slots.size());
     } else {
         std::vector<std::pair<int64_t, int32_t>> pending;  // deferred reset X: (qubit, record)
         size_t i = 0;
@@ -1325,6 +1402,12 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             }
             i = j;
         }
+        fresh = std::make_shared<PlanCacheEntry>();
+        fresh->steps = c->steps;
+        fresh->segs = c->segs;
+        fresh->meas = c->meas;
+        for (MeasOp &m : fresh->meas) m.res = m.det = nullptr;
+        fresh->meas_op = c->meas_op;
     }
     pick_tile(c);
     if (fused) {
@@ -1402,7 +1485,9 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     if (fused && c->opts.per_shot_xz == 0 && h->n > 0 && frame_smem_bytes(h->n) <= kSegSmemMax) {
         bool ok = true;
         for (const ps_op &o : ops) ok &= o.code != OP_H_IF && o.code != OP_S_IF;
-        if (ok) {
+        if (ok && cached && cached->has_frame) {
+            c->fprog = cached->fprog;
+        } else if (ok) {
             FrameBuilder fb(h->n);
             for (const Step &s : c->steps) {
                 if (s.kind == K_SEGMENT) {
@@ -1435,6 +1520,12 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             c->fprog.tab.insert(c->fprog.tab.end(), 4, 0u);  // padding: staged ranges round up to 16 bytes
             if (c->fprog.slot_off.empty()) c->fprog.slot_off.push_back(0);
             if (c->fprog.rand_meas.empty()) c->fprog.rand_meas.push_back(0);
+            if (fresh) {
+                fresh->has_frame = true;
+                fresh->fprog = c->fprog;
+            }
+        }
+        if (ok) {
             if (upload(h, c->owned, c->fprog.ops, &c->d_fops) || upload(h, c->owned, c->fprog.tab, &c->d_ftab) ||
                 upload(h, c->owned, c->fprog.xz, &c->d_fxz) ||
                 upload(h, c->owned, c->fprog.rand_meas, &c->d_frand))
@@ -1560,7 +1651,26 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         int rc = capture_graphs(c);
         if (rc != OK) return bail(rc);
     }
+    if (fresh) plan_store(pkey, fresh);
     *out = c;
+    return OK;
+}
+
+ps_status ps_compile_cache_stats(uint64_t *hits, uint64_t *misses, uint64_t *entries) {
+    ps_enter(__func__, __LINE__);
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (hits) *hits = g_plan_hits;
+    if (misses) *misses = g_plan_misses;
+    if (entries) *entries = g_plan.size();
+    return OK;
+}
+
+ps_status ps_compile_cache_clear(void) {
+    ps_enter(__func__, __LINE__);
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    g_plan.clear();
+    g_plan_order.clear();
+    g_plan_hits = g_plan_misses = 0;
     return OK;
 }
 

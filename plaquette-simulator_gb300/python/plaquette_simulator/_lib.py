@@ -58,6 +58,8 @@ _SIGS = {
     "ps_record_qubit": (C.c_int, [_vp, _u64, _pu64]),
     "ps_reset_qubit": (C.c_int, [_vp, _u64, _vp, _pu64]),
     "ps_pauli_channel_1": (C.c_int, [_vp, _u64, _vp]),
+    "ps_compile_cache_stats": (C.c_int, [_pu64, _pu64, _pu64]),
+    "ps_compile_cache_clear": (C.c_int, []),
     "ps_pauli_channel_2": (C.c_int, [_vp, _u64, _u64, _vp]),
     "ps_pauli_channel_1_noalloc": (C.c_int, [_vp, _u64, _vp]),
     "ps_circuit_compile": (C.c_int, [_vp, _vp, _u64, _vp, _u64, _vp, _pp]),
@@ -83,6 +85,7 @@ _SIGS = {
     "ps_server_copy_records": (C.c_int, [_vp, _u64, _vp, _vp]),
     "ps_server_release": (C.c_int, [_vp, _u64]),
     "ps_server_drain": (C.c_int, [_vp, C.c_double]),
+    "ps_server_cancel": (C.c_int, [_vp, _u64]),
     "ps_server_get_stats": (C.c_int, [_vp, _vp]),
     "ps_server_now": (C.c_int, [_vp, C.POINTER(C.c_double)]),
     "ps_server_destroy": (C.c_int, [_vp]),

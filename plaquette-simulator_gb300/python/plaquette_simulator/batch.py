@@ -157,7 +157,8 @@ class JobResult(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
-                ("queued", C.c_uint64), ("active", C.c_uint64), ("shot_gates_completed", C.c_uint64),
+                ("queued", C.c_uint64), ("active", C.c_uint64), ("cancelled", C.c_uint64),
+                ("shot_gates_completed", C.c_uint64),
                 ("pool_bytes", C.c_uint64), ("pool_peak_bytes", C.c_uint64), ("p50_latency_s", C.c_double),
                 ("p99_latency_s", C.c_double), ("mean_latency_s", C.c_double), ("max_latency_s", C.c_double),
                 ("first_submit_s", C.c_double), ("last_done_s", C.c_double)]
@@ -201,6 +202,11 @@ class Server:
     def release(self, job_id: int) -> None:
         check(self._L.ps_server_release(self._h, job_id))
         self._jobs.pop(job_id, None)
+
+    def cancel(self, job_id: int) -> None:
+        """Take a job that is still queued out of the queue (an admitted job
+        runs to its end: RuntimeError)."""
+        check(self._L.ps_server_cancel(self._h, job_id))
 
     def drain(self, timeout_s: float = -1.0) -> None:
         check(self._L.ps_server_drain(self._h, timeout_s))

@@ -186,3 +186,17 @@ class CompiledCircuit:
             except Exception:
                 pass
             self._h = None
+
+
+def compile_cache_stats() -> dict:
+    """Hits, misses and entries of the process-wide compile cache
+    (ps_compile_cache_stats): a circuit compiled again reuses the
+    shot-independent host work of its first compile."""
+    L = _lib.load()
+    h, m, e = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    check(L.ps_compile_cache_stats(C.byref(h), C.byref(m), C.byref(e)))
+    return {"hits": h.value, "misses": m.value, "entries": e.value}
+
+
+def compile_cache_clear() -> None:
+    check(_lib.load().ps_compile_cache_clear())

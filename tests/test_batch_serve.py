@@ -156,3 +156,66 @@ def test_server_d25_job_matches_oracle(ps, O):
         ores, odet = o.record(k)
         assert np.array_equal(gres[k], ores), f"record {k}"
         assert np.array_equal(gdet[k], odet), f"record {k}"
+
+
+@pytest.mark.gpu
+def test_server_failing_job_counted_apart(ps):
+    """A job that fails on its worker (its circuit flips on a record that is
+    not measured yet: the compile refuses it) is reported failed, not
+    completed, leaves no latency behind, and the jobs around it still give
+    the records they give alone."""
+    from plaquette_simulator import _lib
+    from plaquette_simulator.batch import Job, Server
+    from plaquette_simulator import circuits as C
+    good = _small_jobs()[:3]
+    bad_c = C.Circuit(3)
+    bad_c.h(0)
+    bad_c.h_if(1, 5)
+    bad_c.m(0)
+    bad = Job(bad_c, 64, 99, 3, 0.0)
+    with Server(hbm_budget_bytes=1 << 30, max_active=2) as srv:
+        ids = [srv.submit(j) for j in good[:2]] + [srv.submit(bad)] + [srv.submit(good[2])]
+        srv.drain(120.0)
+        with pytest.raises(_lib.PlaquetteError) as e:
+            srv.wait(ids[2], 0.0)
+        assert e.value.status == _lib.PS_E_ARG
+        got = [srv.records(i) for i in ids[:2] + ids[3:]]
+        st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == 3 and st["submitted"] == 4
+    for job, (res, det) in zip(good, got):
+        alone = _alone(ps, job)[0]
+        assert np.array_equal(res, alone[0]) and np.array_equal(det, alone[1])
+
+
+@pytest.mark.gpu
+def test_server_cancel_queued_job(ps):
+    """A job cancelled while queued is never admitted and reports
+    PS_E_STATE; one already admitted cannot be cancelled and runs to its
+    end.  One slot, so the later submissions queue behind the first."""
+    from plaquette_simulator import _lib
+    from plaquette_simulator.batch import Job, Server
+    from plaquette_simulator import circuits as C
+    first = Job(C.surface_code_memory(9, 9, p=1e-3), 16384, 7, 9, 1e-3)
+    later = _small_jobs()[:3]
+    with Server(hbm_budget_bytes=4 << 30, max_active=1) as srv:
+        i0 = srv.submit(first)
+        ids = [srv.submit(j) for j in later]
+        try:
+            srv.cancel(ids[2])
+            cancelled = True
+        except _lib.PlaquetteError as e:  # admitted already: allowed only with the state error
+            assert e.status == _lib.PS_E_STATE
+            cancelled = False
+        with pytest.raises(_lib.PlaquetteError) as e:
+            srv.cancel(i0 + 1000)
+        assert e.value.status == _lib.PS_E_RANGE
+        srv.drain(120.0)
+        st = srv.stats()
+        if cancelled:
+            with pytest.raises(_lib.PlaquetteError) as e:
+                srv.wait(ids[2], 0.0)
+            assert e.value.status == _lib.PS_E_STATE
+            assert st["cancelled"] == 1 and st["completed"] == 3
+        else:
+            assert st["cancelled"] == 0 and st["completed"] == 4
+        assert st["failed"] == 0

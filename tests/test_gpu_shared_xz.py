@@ -248,3 +248,31 @@ def test_shared_xz_edge_cases(ps, O, name):
     o = O.Oracle(circ.num_qubits, B, seed=31)
     o.run(circ.op_array(), circ.param_array())
     _check(st, o, cc.first_record, circ.num_measurements())
+
+
+def test_compile_cache_reuses_plans(ps, O):
+    """A circuit compiled again (another state, other shots, another seed)
+    takes its host plan from the compile cache and still matches the oracle
+    bit for bit; a changed parameter table is a different key."""
+    from plaquette_simulator import circuits as C
+    from plaquette_simulator.circuit import CompiledCircuit, compile_cache_clear, compile_cache_stats
+    compile_cache_clear()
+    circ = C.surface_code_memory(3, 3, p=0.02)
+    for k, (B, seed) in enumerate([(130, 5), (64, 6), (200, 7)]):
+        st = ps.CliffordState(circ.num_qubits, B, seed, True)
+        cc = CompiledCircuit(circ, st, fused=True, graph=True)
+        cc.run(reset=True)
+        st.synchronize()
+        o = O.Oracle(circ.num_qubits, B, seed=seed)
+        o.run(circ.op_array(), circ.param_array())
+        gx, gz, gr = st.device_to_host_numpy()
+        ox, oz, orr = o.tableau()
+        assert np.array_equal(gx, ox) and np.array_equal(gz, oz) and np.array_equal(gr, orr)
+        for rid in range(circ.num_measurements()):
+            assert np.array_equal(st.record(cc.first_record + rid)[0], o.record(rid)[0])
+        stats = compile_cache_stats()
+        assert stats["misses"] == 1 and stats["hits"] == k
+    other = C.surface_code_memory(3, 3, p=0.03)
+    st = ps.CliffordState(other.num_qubits, 64, 1, True)
+    CompiledCircuit(other, st, fused=True, graph=True)
+    assert compile_cache_stats()["misses"] == 2

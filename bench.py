@@ -51,12 +51,32 @@ def parse():
     ap.add_argument("--cpu-shots", type=int, default=0, help="shots of the CPU sample (0 = auto)")
     ap.add_argument("--batch-jobs", type=int, default=64,
                     help="uneven surface-code jobs in the one-launch batch leg (0 = skip)")
-    ap.add_argument("--serve-seconds", type=float, default=1.0,
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="seconds of Poisson arrivals in the serving leg (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving leg: arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="serving leg: HBM admission budget")
     ap.add_argument("--serve-drain-s", type=float, default=180.0, help="serving leg: longest wait for the backlog")
     return ap.parse_args()
+
+
+# DRAM bytes (read + written) per shot-word of one x / z broadcast launch of
+# the d = 15 circuit, from an ncu capture at 16,384 shots (256 shot-words):
+# two launches averaged 0.166 MB read + 1589.37 MB written.
+BCAST_DRAM_BYTES_D15_PER_WORD = (0.166e6 + 1589.37e6) / 256
+
+
+def noisy_ranges(circ) -> int:
+    """Runs of non-measurement ops that hold a Pauli channel: the ranges
+    the noise kernel writes a vector for."""
+    from plaquette_simulator import circuits as C
+    n, seen = 0, False
+    for code, _a, _b, _c in circ.ops:
+        if code in (C.OP_M, C.OP_R):
+            n += seen
+            seen = False
+        elif code in (C.OP_PAULI1, C.OP_PAULI2):
+            seen = True
+    return n + seen
 
 
 def workload_circuit(name):
@@ -123,6 +143,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def host_cpu():
+    """The host's core count and CPU model (lscpu), for the CPU baselines."""
+    info = {"cores": os.cpu_count() or 1, "model": None}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                info["model"] = ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return info
+
+
 # ------------------------------------------------------------- CPU legs
 def cpu_sample(circ, seed: int, shots: int):
     """Time the CPU port of the reference's algorithm (oracle/, int32 tableau,
@@ -146,6 +179,7 @@ def cpu_baseline(circ, seed, requested_shots=0):
         shots = int(min(512, max(64, shots * 10.0 / max(secs, 1e-3))) // 64 * 64) or 64
         secs, threads = cpu_sample(circ, seed, shots)
     return {"value": gates * shots / secs, "unit": "shot-gates/s", "cores": threads, "kind": "port",
+            "cpu_model": host_cpu()["model"],
             "sample": f"{shots} shots of the same circuit ({gates} gates/shot) on the C restatement of the "
                       f"reference's algorithm in its int32 layout, OpenMP over {threads} threads: {secs:.2f} s"}
 
@@ -182,6 +216,7 @@ def run_reference(args):
                                f"p={meta['p']} Z-basis", "num_qubits": circ.num_qubits, "shots": shots,
                    "gates_per_shot": gates, "sample_shots": sample},
         "cpu_baseline": {"value": value, "unit": "shot-gates/s", "cores": threads, "kind": "port",
+                         "cpu_model": host_cpu()["model"],
                          "sample": f"{sample} shots per step of the {shots}-shot workload"},
         "e2e": {"value": value, "unit": "shot-gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "noiseless": {"value": quiet.num_gates() * sample / qsec, "unit": "shot-gates/s",
@@ -251,6 +286,8 @@ def serving_leg(args, rank):
     jobs = uneven_surface_jobs(len(arrivals), seed=24680 + rank, distances=tuple(range(3, 22, 2)) + (25,),
                                job_seed_base=100000)
     offered = sum(j.shot_gates() for j in jobs)
+    from plaquette_simulator.circuit import compile_cache_stats
+    cache0 = compile_cache_stats()
     with Server(hbm_budget_bytes=int(args.serve_budget_gb * 1e9), max_active=16, autotune=False) as srv:
         t0 = srv.now()
         ids = []
@@ -275,6 +312,8 @@ def serving_leg(args, rank):
                         {"d": j.distance, "shots": j.shots})
         st = srv.stats()
     span = max(1e-9, st["last_done_s"] - st["first_submit_s"])
+    cache1 = compile_cache_stats()
+    hits, misses = cache1["hits"] - cache0["hits"], cache1["misses"] - cache0["misses"]
     return {"workload": f"Poisson arrivals at {args.serve_rate:g} jobs/s for {args.serve_seconds:g} s, "
                         "rotated surface-code memory jobs d in {3..21, 25} (d rounds), shots log-uniform in "
                         f"[256, 65536], admission by device bytes against {args.serve_budget_gb:g} GB",
@@ -286,7 +325,52 @@ def serving_leg(args, rank):
             "offered_jobs_per_s": len(ids) / args.serve_seconds,
             "achieved_jobs_per_s": st["completed"] / span, "submit_span_s": submit_end,
             "pool_peak_gb": st["pool_peak_bytes"] / 1e9, "max_active": 16,
+            "compile_cache": {"hits": hits, "misses": misses,
+                              "hit_rate": hits / max(1, hits + misses)},
             "errors": {k: v[:4] for k, v in errors.items()}}
+
+
+def compile_leg(circ, shots, first_shot, seed, gates, world, torch):
+    """The host work the timed steps leave out.  compile_ms: ps_circuit_compile
+    of the workload on a fresh state, with the compile cache cleared (cold)
+    and again (cached).  cold_e2e: one whole sampling job from nothing -- a
+    fresh state, the cold compile (graph capture included), one run, every
+    record copied to host memory, everything freed -- as shot-gates/s over
+    its wall time; cached_e2e: the same with the compile cache warm."""
+    import numpy as np
+    from plaquette_simulator import CliffordState
+    from plaquette_simulator.circuit import CompiledCircuit, compile_cache_clear
+
+    def one_job(clear):
+        if clear:
+            compile_cache_clear()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = CliffordState(circ.num_qubits, shots, seed + 1, True)
+        st.set_shot_offset(first_shot)
+        t1 = time.perf_counter()
+        cc = CompiledCircuit(circ, st, fused=True, graph=True)
+        t2 = time.perf_counter()
+        cc.run(reset=True)
+        nm = int(cc.stats["num_measurements"])
+        w_words = (((shots + 63) // 64) + 1) & ~1
+        res = np.empty((nm, w_words), np.uint64)
+        det = np.empty_like(res)
+        cc.copy_records_words(res, det)
+        del cc, st
+        t3 = time.perf_counter()
+        return (t2 - t1) * 1e3, (t3 - t0)
+
+    cold_ms, cold_s = one_job(True)
+    cached_ms, cached_s = one_job(False)
+    return {"compile_ms_cold": cold_ms, "compile_ms_cached": cached_ms,
+            "cold_e2e": {"value": gates * shots * world / cold_s, "unit": "shot-gates/s", "seconds": cold_s,
+                         "what": "fresh state + cold compile (cache cleared, graph capture) + one run + all "
+                                 "records to host + free"},
+            "cached_e2e": {"value": gates * shots * world / cached_s, "unit": "shot-gates/s", "seconds": cached_s,
+                           "what": "the same with the compile cache warm (a job of a circuit seen before)"},
+            "note": "the headline value and e2e time repeated runs of one compiled circuit: compile is outside "
+                    "their timed region and reported here"}
 
 
 # ---------------------------------------------------------------- ours
@@ -399,11 +483,15 @@ def main():
         #    words per measurement);
         #  x / z broadcast: the x and z words of every row, qubit and
         #    shot-word written once.
+        #  channel noise: the XOR vector of every range with channels and
+        #    every shot-word written once (W rounded up to even words).
         kind_bytes = {
             "sign_program": W * w_words * 8 + 2 * nm * w_words * 8,
             "xz_broadcast": 2 * W * n_q * w_words * 8,
+            "channel_sample": noisy_ranges(circ) * w_words * (W + 1) // 2 * 2 * 8,
         }
-        kernel_of = {"sign_program": "frame_run_kernel", "xz_broadcast": "broadcast_jobs_kernel"}
+        kernel_of = {"sign_program": "frame_run_kernel", "xz_broadcast": "broadcast_jobs_kernel",
+                     "channel_sample": "noise_vec_kernel"}
     else:
         meas_bytes = fused.measure_bytes(reset=True)
         seg_bytes = float(fused.stats["segment_bytes"])
@@ -415,9 +503,14 @@ def main():
     traffic = None
     if dom == "segment" and meta["distance"] == 15:
         # DRAM bytes per segment launch from one ncu capture of the d=15
-        # circuit at 32 shot-words (profiles/dram_traffic_surface_d15_s2048.md:
-        # 207.1 MB read + 147.9 MB written), scaled by shot-words.
+        # circuit at 32 shot-words (207.1 MB read + 147.9 MB written),
+        # scaled by shot-words.
         traffic = (207.1e6 + 147.9e6) / 32 * w_words
+    elif dom == "xz_broadcast" and meta["distance"] == 15 and BCAST_DRAM_BYTES_D15_PER_WORD:
+        # DRAM bytes of one broadcast launch from an ncu capture of the d=15
+        # workload at 16,384 shots (dram__bytes_read.sum +
+        # dram__bytes_write.sum), per shot-word.
+        traffic = BCAST_DRAM_BYTES_D15_PER_WORD * w_words
     roofline = {"bound": "hbm", "kernel": kernel_of[dom],
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s",
@@ -444,7 +537,9 @@ def main():
                    "num_qubits": circ.num_qubits, "shots": shots, "gates_per_shot": gates,
                    "tableau_bytes": 3 * (2 * circ.num_qubits + 1) * circ.num_qubits * ((shots + 63) // 64) * 8,
                    "l2": "no flush needed: the 2.48 GB tableau (1.65 GB of it the x/z rewritten every step) is larger than the 129 MB L2",
-                   "parallelism": f"shots split over {world} GPU(s), {shots} per GPU"},
+                   "parallelism": f"shots split over {world} GPU(s), {shots} per GPU",
+                   "steps": "repeated sampling runs (fresh draws, full tableau and records written) of one "
+                            "compiled circuit; compile time and a cold job are reported under compile"},
         # the per-shot plan's reset adds init_zero_kernel; shared-x/z runs start from zero signs in the sign kernel
         "gpu_launches": int(fused.stats["launches_per_run"]) + (0 if shared else 1),
         "clocks": clocks,
@@ -459,6 +554,7 @@ def main():
         "algorithmic_bytes_per_step": {k: float(v) for k, v in kind_bytes.items()},
     }
 
+    line["compile"] = compile_leg(circ, shots, first_shot, seed, gates, world, torch)
     if not args.no_plain and shared:
         per_shot = CompiledCircuit(circ, st, fused=True, graph=True, shared_xz=False)
         per_shot.run(reset=True)

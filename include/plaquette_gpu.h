@@ -219,8 +219,9 @@ typedef struct {
                              shot's tableau                                   */
     int32_t frame_warps; /* shared-x/z runs: sign-kernel warps per shot-word, 4
                              or 8 (0 = auto)                                  */
-    int32_t bcast_ctas;  /* shared-x/z runs: x / z broadcast CTAs per SM (0 =
-                             auto); the rest of each SM runs the sign kernel  */
+    int32_t bcast_ctas;  /* shared-x/z runs: x / z broadcast CTAs (8 warps)
+                             per SM (0 = auto: 1); the rest of each SM runs
+                             the noise and sign kernels                       */
 } ps_circuit_options;
 
 typedef struct {

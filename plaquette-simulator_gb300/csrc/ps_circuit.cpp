@@ -56,6 +56,7 @@ struct Step {
     int32_t count = 0;      // K_CHANNEL: 3 / 15; K_MEAS: number of ops
     int32_t first = 0;      // K_MEAS: first MeasOp; K_SEGMENT: segment index; K_CHANNEL: thr offset
     uint32_t event = 0;     // K_CHANNEL event offset
+    int32_t table = 0;      // K_CHANNEL: its channel table (survival products, estimate factors)
 };
 
 struct SegHost {
@@ -168,6 +169,8 @@ struct ps_circuit {
     RunParams *d_params = nullptr;
     uint64_t *d_thr = nullptr;
     std::vector<uint64_t> thr_host; // the distinct channel tables (host copy of d_thr)
+    uint32_t *d_psurv = nullptr;    // plain form: survival products of each distinct table, 64 words each
+    std::vector<ChannelEst> pest;   // plain form: estimate factors of each distinct table
     u64 **d_recs = nullptr;
     u64 *d_masks = nullptr;         // plain-mode channel masks (4w)
     u64 *d_forced = nullptr;        // [nm][w]
@@ -825,8 +828,8 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
             break;
         case K_CHANNEL:
             rc = timed(P_CHANNEL, [&] {
-                return launch_channel_rp(st, h, s.a, s.b, c->d_thr + s.first, s.count, s.event, c->d_params,
-                                         c->d_masks);
+                return launch_channel_apply(st, h, s.a, s.b, c->d_thr + s.first, s.count, c->d_psurv + 64 * s.table,
+                                            c->pest[(size_t)s.table], s.event, c->d_params);
             });
             break;
         case K_MEAS:
@@ -1059,7 +1062,8 @@ int capture_graphs(ps_circuit *c) {
         }
         if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
         c->graph[reset] = g;
-        e = cudaGraphInstantiate(&c->exec[reset], g, 0);
+        // node priorities kept: the broadcast's CTAs go first
+        e = cudaGraphInstantiateWithFlags(&c->exec[reset], g, cudaGraphInstantiateFlagUseNodePriority);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     }
     return OK;
@@ -1332,6 +1336,8 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         c->meas_op.push_back((int32_t)i);
     };
     size_t max_slots = 0;
+    std::map<int32_t, int32_t> ptable;  // plain form: thr offset -> distinct table
+    std::vector<uint32_t> psurv;
     if (!fused) {
         for (size_t i = 0; i < ops.size(); ++i) {
             const ps_op &o = ops[i];
@@ -1348,6 +1354,15 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 s.count = o.code == OP_PAULI2 ? 15 : 3;
                 s.first = thr_off[i];
                 s.event = event_of[i];
+                auto tt = ptable.find(thr_off[i]);
+                if (tt == ptable.end()) {  // survival products and estimate factors of a new table
+                    tt = ptable.emplace(thr_off[i], (int32_t)c->pest.size()).first;
+                    const uint64_t total = thr[(size_t)(thr_off[i] + s.count - 1)];
+                    c->pest.push_back(channel_est_factors(total, s.count));
+                    psurv.resize(psurv.size() + 64, 0u);
+                    channel_surv_table(total, &psurv[psurv.size() - 64]);
+                }
+                s.table = tt->second;
             } else {
                 s.kind = K_GATE;
                 s.code = o.code;
@@ -1408,6 +1423,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         fresh->meas = c->meas;
         for (MeasOp &m : fresh->meas) m.res = m.det = nullptr;
         fresh->meas_op = c->meas_op;
+    }
+    if (!fused) {
+        if (psurv.empty()) psurv.assign(64, 0u);
+        if (upload(h, c->owned, psurv, &c->d_psurv) != OK) return bail(E_CUDA);
     }
     pick_tile(c);
     if (fused) {
@@ -1566,14 +1585,15 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 job.slot = dsl;
                 job.slot_s64 = ds64;
                 job.slot_event = dev;
-                {
+                {  // the error word (offset 0) and the broadcast's counters (offsets 16, 24)
                     void *pe = nullptr;
-                    if (dev_alloc(h, &pe, sizeof(int32_t)) != OK) return bail(E_NOMEM);
+                    if (dev_alloc(h, &pe, 32) != OK) return bail(E_NOMEM);
                     c->owned.push_back(pe);
                     c->d_ferr = static_cast<int32_t *>(pe);
-                    if (cudaMemsetAsync(pe, 0, sizeof(int32_t), h->stream) != cudaSuccess)
+                    if (cudaMemsetAsync(pe, 0, 32, h->stream) != cudaSuccess)
                         return bail(cuda_fail(cudaGetLastError(), "cudaMemsetAsync"));
                     job.err = c->d_ferr;
+                    c->ftable.bctr = reinterpret_cast<unsigned long long *>(static_cast<char *>(pe) + 16);
                 }
                 job.ctab = dct;
                 job.surv = dsv;
@@ -1626,7 +1646,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             st.num_measure_phases++;
             st.launches_per_run += 1;
         } else if (s.kind == K_CHANNEL) {
-            st.launches_per_run += s.count == 15 ? 3 : 2;
+            st.launches_per_run += 1;
         } else {
             st.launches_per_run += 1;
         }

@@ -486,31 +486,50 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
 // c + warps, ...; in a one-job table the wide form's (row, qubit) advances by
 // a constant step, so only the first pair takes a division.  The stores are
 // streaming (evict first): the broadcast passes 1.65 GB through L2 at
-// d = 15 and must not evict the tables of the kernels beside it.
-__global__ void __launch_bounds__(256) broadcast_jobs_kernel(const BroadcastJobDev *__restrict__ jobs, int njobs,
-                                                             const int64_t *__restrict__ chunk0, int64_t chunks) {
+// d = 15 and must not evict the tables of the kernels beside it.  At most
+// 32 registers a thread: two broadcast CTAs (16K registers) fit on an SM
+// beside six noise CTAs (48K) or two sign CTAs (40K).
+__global__ void __launch_bounds__(256, 8) broadcast_jobs_kernel(const BroadcastJobDev *__restrict__ jobs, int njobs,
+                                                             const int64_t *__restrict__ chunk0, int64_t chunks,
+                                                             unsigned long long *ctr) {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const int64_t c0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (njobs == 1 && (jobs[0].w >> 1) >= 16) {
+    if (njobs == 1 && (jobs[0].w >> 1) >= 16 && ctr) {
+        // Warps take kBcastBatch chunks at a time from a counter, so CTAs
+        // that reach their SMs late (beside the other kernels of the run)
+        // take less of the work.  The last CTA to finish puts the counter
+        // back to zero for the next launch.
         const BroadcastJobDev &B = jobs[0];
         const int64_t hw = B.w >> 1, n = B.n;
-        const int64_t drow = warps / n, dq = warps - drow * n;
-        int64_t row = c0 / n, q = c0 - row * n;
-        for (int64_t c = c0; c < chunks; c += warps) {
-            const u64 xb = (B.xz[(row * 2 + 0) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-            const u64 zb = (B.xz[(row * 2 + 1) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-            const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
-            u64 *xo = B.X + c * B.w, *zo = B.Z + c * B.w;
-            for (int64_t kp = lane; kp < hw; kp += 32) {
-                __stcs(reinterpret_cast<ulonglong2 *>(xo + 2 * kp), xv);
-                __stcs(reinterpret_cast<ulonglong2 *>(zo + 2 * kp), zv);
+        for (;;) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(ctr, 1ull);
+            const int64_t base = (int64_t)__shfl_sync(0xFFFFFFFFu, b, 0) * kBcastBatch;
+            if (base >= chunks) break;
+            const int64_t end = base + kBcastBatch < chunks ? base + kBcastBatch : chunks;
+            int64_t row = base / n, q = base - row * n;
+            for (int64_t c = base; c < end; ++c) {
+                const u64 xb = (B.xz[(row * 2 + 0) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+                const u64 zb = (B.xz[(row * 2 + 1) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+                const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
+                u64 *xo = B.X + c * B.w, *zo = B.Z + c * B.w;
+                for (int64_t kp = lane; kp < hw; kp += 32) {
+                    __stcs(reinterpret_cast<ulonglong2 *>(xo + 2 * kp), xv);
+                    __stcs(reinterpret_cast<ulonglong2 *>(zo + 2 * kp), zv);
+                }
+                if (++q == n) {
+                    q = 0;
+                    ++row;
+                }
             }
-            q += dq;
-            row += drow;
-            if (q >= n) {
-                q -= n;
-                ++row;
+        }
+        __syncthreads();  // every warp of the CTA is past its last counter fetch
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(ctr + 1, 1ull) == (unsigned long long)gridDim.x - 1) {
+                atomicExch(ctr, 0ull);
+                atomicExch(ctr + 1, 0ull);
             }
         }
         return;
@@ -545,6 +564,7 @@ __global__ void __launch_bounds__(256) broadcast_jobs_kernel(const BroadcastJobD
 
 int g_frame_sms = 0;
 int g_prio_greatest = 1;  // 1: not looked up yet (priorities are <= 0)
+int g_prio_least = 0;
 
 // Both kernels of a run ask for the largest shared-memory carveout.  An SM
 // changes its L1 / shared split only when it is idle, so a broadcast left to
@@ -567,6 +587,7 @@ int prio_greatest() {
     if (g_prio_greatest == 1) {
         int least = 0, greatest = 0;
         PS_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        g_prio_least = least;
         g_prio_greatest = greatest;
     }
     return OK;
@@ -581,8 +602,8 @@ int launch_frame_fw(cudaStream_t st, const FrameTable &t) {
     int rc = same_carveout((const void *)frame_run_kernel<FW>);
     if (rc == OK) rc = prio_greatest();
     if (rc != OK) return rc;
-    // The sign kernel is the plan's critical path: launched at the highest
-    // priority, its CTAs go ahead of the broadcast's queued CTAs.
+    // The sign kernel runs at the lowest priority: it fills what the
+    // broadcast's CTAs leave of each SM.
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)t.ctas);
     cfg.blockDim = dim3(32 * FW);
@@ -590,7 +611,7 @@ int launch_frame_fw(cudaStream_t st, const FrameTable &t) {
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributePriority;
-    attr[0].val.priority = g_prio_greatest;
+    attr[0].val.priority = g_prio_least;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     PS_CUDA(cudaLaunchKernelEx(&cfg, frame_run_kernel<FW>, t.jobs, (int)t.njobs, t.cta0));
@@ -608,8 +629,7 @@ int launch_noise_vectors(cudaStream_t st, const FrameTable &t) {
     if (t.njobs <= 0 || t.nctas <= 0) return OK;
     if (t.nsmem > kSegSmemMax) return fail(E_ARG, "channel noise does not fit in shared memory");
     // At most six noise CTAs an SM (8K registers each): the broadcast's two
-    // CTAs (16K registers) always find room beside them, whichever of the
-    // two kernels reaches the SMs first.
+    // CTAs (16K registers) find room beside them.
     const size_t smem = std::max<size_t>(t.nsmem, kNoiseSmemFloor);
     if (t.nctas > 0x7FFFFFFFll) return fail(E_ARG, "channel noise: too many (range, shot-word) pairs in one launch");
     const void *kern = (const void *)noise_vec_kernel<kNoiseWarps>;
@@ -627,8 +647,8 @@ int launch_noise_vectors(cudaStream_t st, const FrameTable &t) {
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributePriority;  // on the critical path too, ahead of the sign kernel
-    attr[0].val.priority = g_prio_greatest;
+    attr[0].id = cudaLaunchAttributePriority;  // like the sign kernel: what the broadcast leaves
+    attr[0].val.priority = g_prio_least;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     PS_CUDA(cudaLaunchKernelEx(&cfg, noise_vec_kernel<kNoiseWarps>, t.jobs, (int)t.njobs, t.ncta0));
@@ -659,9 +679,24 @@ int launch_broadcast_jobs(cudaStream_t st, const FrameTable &t, int ctas_per_sm)
         const int rc = same_carveout((const void *)broadcast_jobs_kernel);
         if (rc != OK) return rc;
     }
-    const int per = ctas_per_sm > 0 ? ctas_per_sm : 2;
+    int rc = prio_greatest();
+    if (rc != OK) return rc;
+    const int per = ctas_per_sm > 0 ? ctas_per_sm : 1;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((t.chunks + 7) / 8, (int64_t)g_frame_sms * per));
-    broadcast_jobs_kernel<<<(unsigned)blocks, 256, 0, st>>>(t.bjobs, t.njobs, t.chunk0, t.chunks);
+    // The broadcast is the run's longest kernel and its CTAs stay to the
+    // end: launched at the highest priority, they reach every SM before the
+    // noise and sign CTAs fill them.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = g_prio_greatest;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PS_CUDA(cudaLaunchKernelEx(&cfg, broadcast_jobs_kernel, t.bjobs, (int)t.njobs, t.chunk0, t.chunks, t.bctr));
     PS_CUDA(cudaGetLastError());
     return OK;
 }

@@ -188,14 +188,20 @@ struct FrameTable {
     int64_t ctas = 0, nctas = 0, chunks = 0;  // totals
     size_t smem = 0;                          // largest frame_job_smem of the table
     size_t nsmem = 0;                         // largest noise_job_smem of the table
+    // two zeroed words (the broadcast's chunk counter and finished-CTA
+    // count; zero again after every launch); null: a static chunk split
+    unsigned long long *bctr = nullptr;
 };
+// Broadcast chunks a warp takes from the counter at a time.
+constexpr int64_t kBcastBatch = 8;
 
 // The noise vectors of every job (nothing when no job has channels).
 int launch_noise_vectors(cudaStream_t st, const FrameTable &t);
 // Sign-kernel warps per CTA the launch uses (4 or 8; 0 = 8).
 int launch_frame_run(cudaStream_t st, const FrameTable &t, int warps);
-// The x / z broadcast of every job; ctas_per_sm 0 = 2 (room for the sign
-// kernel beside it on every SM).
+// The x / z broadcast of every job; ctas_per_sm 0 = 1 (eight warps an SM
+// write at close to the copy rate and leave the noise and sign kernels
+// most of each SM and of the memory system).
 int launch_broadcast_jobs(cudaStream_t st, const FrameTable &t, int ctas_per_sm);
 
 }  // namespace ps

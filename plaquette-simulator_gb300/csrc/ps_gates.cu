@@ -142,6 +142,53 @@ __global__ void __launch_bounds__(256) sign_flip_kernel(const u64 *__restrict__ 
     st2(R + i * w + k, r.a, r.b);
 }
 
+// The per-op channel of compiled plain runs in one launch: a CTA takes 8
+// shot-words and a block of 64 rows, samples the words first
+// (channel_word_est: the same draws as every other form; threads 0..7; the
+// CTAs of other row blocks draw the same), then flips their signs over its
+// rows, two words a thread (16-byte accesses, four threads a row).
+template <int TWO>
+__global__ void __launch_bounds__(256) channel_apply_kernel(const u64 *__restrict__ X, const u64 *__restrict__ Z,
+                                                           u64 *__restrict__ R, int64_t n, int64_t W, int64_t w,
+                                                           int64_t a, int64_t b, uint32_t event_off,
+                                                           const RunParams *__restrict__ rp,
+                                                           const uint64_t *__restrict__ thr, int count,
+                                                           const uint32_t *__restrict__ surv, ChannelEst est) {
+    __shared__ u64 sm[4][8];
+    const int64_t k0 = (int64_t)blockIdx.x * 8;
+    const int t = threadIdx.x;
+    if (t < 8) {
+        ChannelWord m{0ull, 0ull, 0ull, 0ull};
+        if (k0 + t < w)
+            m = channel_word_est(rp->seed, rp->event_base + event_off, rp->word_base + (uint64_t)(k0 + t), thr, count,
+                                 surv, est);
+        sm[0][t] = m.fxa;
+        sm[1][t] = m.fza;
+        sm[2][t] = m.fxb;
+        sm[3][t] = m.fzb;
+    }
+    __syncthreads();
+    const int64_t i0 = (int64_t)blockIdx.y * 64, i1 = i0 + 64 < W ? i0 + 64 : W;
+    for (int64_t it = t; it < (i1 - i0) * 4; it += blockDim.x) {
+        const int64_t i = i0 + (it >> 2);
+        const int p = (int)(it & 3);
+        const int64_t k = k0 + 2 * p;
+        if (k >= w) continue;
+        W2 r = ld2(R + i * w + k);
+        const int64_t oa = (i * n + a) * w + k;
+        const W2 xa = ld2(X + oa), za = ld2(Z + oa);
+        r.a ^= (sm[0][2 * p] & za.a) ^ (sm[1][2 * p] & xa.a);
+        r.b ^= (sm[0][2 * p + 1] & za.b) ^ (sm[1][2 * p + 1] & xa.b);
+        if (TWO) {
+            const int64_t ob = (i * n + b) * w + k;
+            const W2 xb = ld2(X + ob), zb = ld2(Z + ob);
+            r.a ^= (sm[2][2 * p] & zb.a) ^ (sm[3][2 * p] & xb.a);
+            r.b ^= (sm[2][2 * p + 1] & zb.b) ^ (sm[3][2 * p + 1] & xb.b);
+        }
+        st2(R + i * w + k, r.a, r.b);
+    }
+}
+
 inline int blocks_for(int64_t threads) { return (int)((threads + 255) / 256); }
 
 }  // namespace
@@ -182,6 +229,20 @@ int launch_channel_rp(cudaStream_t st, ps_state *h, int64_t a, int64_t b, const 
             sign_flip_kernel<<<blocks_for(work), 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, b,
                                                                 masks + 2 * h->w, masks + 3 * h->w);
     }
+    PS_CUDA(cudaGetLastError());
+    return OK;
+}
+
+int launch_channel_apply(cudaStream_t st, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,
+                         const uint32_t *dev_surv, ChannelEst est, uint32_t event_off, const RunParams *rp) {
+    if (h->n == 0 || h->w == 0) return OK;
+    const dim3 grid((unsigned)((h->w + 7) / 8), (unsigned)((h->W + 63) / 64));
+    if (count == 15)
+        channel_apply_kernel<1><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, b, event_off, rp, dev_thr,
+                                                      count, dev_surv, est);
+    else
+        channel_apply_kernel<0><<<grid, 256, 0, st>>>(h->X, h->Z, h->R, h->n, h->W, h->w, a, 0, event_off, rp, dev_thr,
+                                                      count, dev_surv, est);
     PS_CUDA(cudaGetLastError());
     return OK;
 }

@@ -163,6 +163,10 @@ size_t frame_smem_bytes(int64_t n);
 constexpr size_t kFrameStageMax = 100 * 1024;
 
 // ps_gates.cu (compiled-circuit form of the per-op kernels)
+// The channel of a compiled plain run in one launch (sampling and sign
+// flips); dev_surv: its table's survival products (channel_surv_table).
+int launch_channel_apply(cudaStream_t st, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,
+                         const uint32_t *dev_surv, ChannelEst est, uint32_t event_off, const RunParams *rp);
 int launch_channel_rp(cudaStream_t stream, ps_state *h, int64_t a, int64_t b, const uint64_t *dev_thr, int count,
                       uint32_t event_off, const RunParams *rp, u64 *dev_masks);
 int launch_gate_on(cudaStream_t stream, ps_state *h, int32_t code, int64_t a, int64_t b, const u64 *flag);

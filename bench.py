@@ -318,6 +318,7 @@ def serving_leg(args, rank):
                         "rotated surface-code memory jobs d in {3..21, 25} (d rounds), shots log-uniform in "
                         f"[256, 65536], admission by device bytes against {args.serve_budget_gb:g} GB",
             "jobs": len(ids), "completed": st["completed"], "failed": st["failed"], "drained": drained,
+            "tableau_jobs": st["tableau_jobs"],
             "p50_latency_s": st["p50_latency_s"], "p99_latency_s": st["p99_latency_s"],
             "mean_latency_s": st["mean_latency_s"], "max_latency_s": st["max_latency_s"],
             "value": st["shot_gates_completed"] / span, "unit": "shot-gates/s",

@@ -357,7 +357,10 @@ ps_status ps_batch_destroy(ps_batch *b);
  * back to it without device-wide synchronisation.  A job's measurement
  * records are copied to host memory when it finishes and stay there until
  * ps_server_release.  Results are the same as the job run alone: every job
- * starts from |0...0> and draws from its own seed. */
+ * starts from |0...0> and draws from its own seed.  A job with no gate that
+ * depends on a measurement record holds only its signs, records and noise
+ * vectors on the device (no per-shot tableaux: its x / z are the same in
+ * every shot and only its records are returned). */
 typedef struct {
     uint64_t hbm_budget_bytes;  /* device region for all admitted jobs        */
     int32_t max_active;         /* jobs on the device at once (0 = 16)        */
@@ -380,6 +383,7 @@ typedef struct {
 typedef struct {
     uint64_t submitted, completed, failed, queued, active;
     uint64_t cancelled;              /* taken out of the queue by ps_server_cancel */
+    uint64_t tableau_jobs;           /* completed jobs that held per-shot tableaux */
     uint64_t shot_gates_completed;
     uint64_t pool_bytes, pool_peak_bytes;
     double p50_latency_s, p99_latency_s, mean_latency_s, max_latency_s;

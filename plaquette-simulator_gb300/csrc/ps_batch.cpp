@@ -99,12 +99,17 @@ uint64_t count_gates(const ps_op *ops, uint64_t nops) {
 }
 
 // Upper bound of the device bytes a fused job takes: tableau, records, the
-// channel-outcome scratch of its largest segment, schedule tables.
-size_t job_device_bytes(const ps_job_desc &j) {
+// channel-outcome scratch of its largest segment, schedule tables.  Signs
+// only (a sampling job of the request loop): the signs, records, the noise
+// vectors of the shared-x/z plan (one [shot-word][row] block for each run of
+// gates holding a channel) and its tables (a channel's rows taken as at most
+// 128 words, the usual case; an allocation beyond the estimate fails as a
+// full pool and the job is admitted again later).
+size_t job_device_bytes(const ps_job_desc &j, bool signs_only) {
     int64_t w = ((int64_t)j.shots + 63) / 64;
     w = (w + 1) & ~int64_t(1);
     if (w == 0) w = 2;
-    size_t nm = 0, nch = 0, seg_ch = 0, max_ch = 0;
+    size_t nm = 0, nch = 0, seg_ch = 0, max_ch = 0, noisy_runs = 0;
     for (uint64_t i = 0; i < j.nops; ++i) {
         const int32_t c = j.ops[i].code;
         if (is_meas_code(c)) {
@@ -112,17 +117,32 @@ size_t job_device_bytes(const ps_job_desc &j) {
             seg_ch = 0;
         } else if (is_channel_code(c)) {
             ++nch;
+            if (seg_ch == 0) ++noisy_runs;
             max_ch = std::max(max_ch, ++seg_ch);
         }
     }
     const size_t W = (size_t)w;
-    size_t b = state_bytes((int64_t)j.num_qubits, (int64_t)j.shots);
-    b += 2 * nm * W * 8;                                             // records
-    b += std::max<size_t>(1, max_ch) * W * (sizeof(NoiseEntry) + 32) + W * 4;  // outcome scratch
+    size_t b = state_bytes((int64_t)j.num_qubits, (int64_t)j.shots, signs_only);
+    b += 2 * nm * W * 8;  // records
+    if (signs_only) {
+        const size_t wp = (2 * (size_t)j.num_qubits + 2) & ~(size_t)1;
+        b += noisy_runs * W * wp * 8;                      // noise vectors
+        b += nch * (128 * 4 + 32) + (size_t)j.nops * 64;  // channel rows and records, program
+    } else {
+        b += std::max<size_t>(1, max_ch) * W * (sizeof(NoiseEntry) + 32) + W * 4;  // outcome scratch
+    }
     b += 4 * W * 8 + 64;                                             // masks, params
     b += (size_t)j.nops * 128 + nch * 15 * 8 + nm * sizeof(MeasOp);  // schedules
     b += 64 * 256 + (1u << 20);                                      // granules, slack
     return b;
+}
+
+// A job runs on a signs-only state when no gate depends on a measurement
+// record (its x / z are the same in every shot).
+bool signs_only_job(const ps_job_desc &j) {
+    for (uint64_t i = 0; i < j.nops; ++i)
+        if (j.ops[i].code == OP_H_IF || j.ops[i].code == OP_S_IF) return false;
+    return j.num_qubits > 0;
 }
 
 int check_job(const ps_job_desc &j, uint64_t index) {
@@ -394,6 +414,8 @@ struct SrvJob {
     uint64_t shot_gates = 0;
     double t_submit = 0, t_admit = 0, t_done = 0;
     uint64_t retry_after = UINT64_MAX;  // re-admit only after this many jobs finished
+    bool signs_only = false;            // run on a signs-only state (records are all it returns)
+    size_t full_bytes = 0;              // device bytes with per-shot tableaux
     bool done = false;
     int status = OK;
     std::string err;
@@ -418,6 +440,7 @@ struct ps_server {
     int active = 0;
     bool stop = false;
     uint64_t next_id = 1, submitted = 0, completed = 0, failed = 0, cancelled = 0, shot_gates = 0;
+    uint64_t tableau_jobs = 0;
     uint64_t finished = 0;  // completed + failed: the jobs that gave their memory back
     std::vector<double> latencies;
     double first_submit = -1.0, last_done = 0.0;
@@ -443,18 +466,23 @@ SrvJob *pick_job(ps_server *s, double now) {
     return nullptr;
 }
 
+// run_job: the circuit needs per-shot tableaux after all; admit the job
+// again with them.
+constexpr int kNeedTableau = 1 << 20;
+
 // Runs one admitted job on the calling worker thread: state from the pool,
 // fused compile, one run from |0...0>, records to host, everything returned.
 int run_job(ps_server *s, SrvJob *j) {
     ps_state *h = new ps_state;
     ps_circuit *c = nullptr;
-    int rc = state_alloc(h, (int64_t)j->n, (int64_t)j->shots, j->seed, &s->pool);
+    int rc = state_alloc(h, (int64_t)j->n, (int64_t)j->shots, j->seed, &s->pool, j->signs_only);
     if (rc == OK) {
         h->valid = true;
         ps_circuit_options co{};
         co.mode = PS_MODE_FUSED;
         co.use_graph = 0;
         rc = ps_circuit_compile(h, j->ops.data(), j->ops.size(), j->params.data(), j->params.size(), &co, &c);
+        if (rc == E_STATE && j->signs_only) rc = kNeedTableau;
     }
     if (rc == OK && s->opts.autotune) rc = ps_circuit_autotune(c, nullptr, nullptr);
     if (rc == OK) rc = ps_circuit_run(c, 1);
@@ -493,7 +521,20 @@ void worker_main(ps_server *s) {
             std::lock_guard<std::mutex> lk(s->mu);
             s->reserved -= j->bytes;
             s->active--;
-            if (rc == E_NOMEM && s->active > 0) {
+            if (rc == kNeedTableau && j->full_bytes <= s->pool.cap) {
+                j->signs_only = false;
+                j->bytes = j->full_bytes;
+                j->err.clear();
+                s->queue.push_front(j);
+            } else if (rc == kNeedTableau) {
+                j->status = E_NOMEM;
+                j->err = "job needs " + std::to_string(j->full_bytes >> 20) +
+                         " MiB of per-shot tableaux, more than the whole HBM budget";
+                j->t_done = seconds_since(s->t0);
+                j->done = true;
+                s->finished++;
+                s->failed++;
+            } else if (rc == E_NOMEM && s->active > 0) {
                 // The pool is fragmented right now: wait for another job to finish.
                 j->retry_after = s->finished;
                 j->err.clear();
@@ -505,6 +546,7 @@ void worker_main(ps_server *s) {
                 s->finished++;
                 if (rc == OK) {
                     s->completed++;
+                    if (!j->signs_only) s->tableau_jobs++;
                     s->shot_gates += j->shot_gates;
                     s->latencies.push_back(j->t_done - j->t_submit);
                     s->last_done = std::max(s->last_done, j->t_done);
@@ -564,7 +606,9 @@ ps_status ps_server_submit(ps_server *s, const ps_job_desc *job, uint64_t *job_i
     j->n = job->num_qubits;
     j->shots = job->shots;
     j->seed = job->seed;
-    j->bytes = job_device_bytes(*job);
+    j->signs_only = signs_only_job(*job);
+    j->full_bytes = job_device_bytes(*job, false);
+    j->bytes = job_device_bytes(*job, j->signs_only);
     j->shot_gates = count_gates(job->ops, job->nops) * job->shots;
     if (j->bytes > s->pool.cap)
         return fail(E_NOMEM, "job needs " + std::to_string(j->bytes >> 20) + " MiB, more than the whole HBM budget");
@@ -680,6 +724,7 @@ ps_status ps_server_get_stats(ps_server *s, ps_server_stats *out) {
     out->completed = s->completed;
     out->failed = s->failed;
     out->cancelled = s->cancelled;
+    out->tableau_jobs = s->tableau_jobs;
     out->queued = s->queue.size();
     out->active = (uint64_t)s->active;
     out->shot_gates_completed = s->shot_gates;

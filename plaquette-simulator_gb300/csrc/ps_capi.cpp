@@ -423,9 +423,10 @@ ps_status ps_record_qubit(const ps_state *h, uint64_t id, uint64_t *out) {
 
 ps_status ps_pauli_channel_1(ps_state *h, uint64_t q, const float p[3]) {
     ENTER();
+    if (!p) return fail(E_ARG, "null probabilities");
+    TRY(check_channel_probs(p, 3));
     CHECK_HANDLE(h);
     CHECK_QUBIT(h, q);
-    if (!p) return fail(E_ARG, "null probabilities");
     uint64_t thr[4];
     channel_thresholds(p, 3, thr);
     return launch_pauli_channel(h, (int64_t)q, 0, thr, 3);
@@ -433,9 +434,10 @@ ps_status ps_pauli_channel_1(ps_state *h, uint64_t q, const float p[3]) {
 
 ps_status ps_pauli_channel_1_noalloc(ps_state *h, uint64_t q, const float p[3]) {
     ENTER();
+    if (!p) return fail(E_ARG, "null probabilities");
+    TRY(check_channel_probs(p, 3));
     CHECK_HANDLE(h);
     CHECK_QUBIT(h, q);
-    if (!p) return fail(E_ARG, "null probabilities");
     uint64_t thr[4];
     channel_thresholds(p, 3, thr);
     return launch_pauli_channel_noalloc(h, (int64_t)q, thr);
@@ -443,11 +445,12 @@ ps_status ps_pauli_channel_1_noalloc(ps_state *h, uint64_t q, const float p[3]) 
 
 ps_status ps_pauli_channel_2(ps_state *h, uint64_t a, uint64_t b, const float p[15]) {
     ENTER();
+    if (!p) return fail(E_ARG, "null probabilities");
+    TRY(check_channel_probs(p, 15));
     CHECK_HANDLE(h);
     CHECK_QUBIT(h, a);
     CHECK_QUBIT(h, b);
     if (a == b) return fail(E_ARG, "two-qubit channel needs distinct qubits");
-    if (!p) return fail(E_ARG, "null probabilities");
     uint64_t thr[16];
     channel_thresholds(p, 15, thr);
     return launch_pauli_channel(h, (int64_t)a, (int64_t)b, thr, 15);

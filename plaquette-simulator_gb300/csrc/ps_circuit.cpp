@@ -860,9 +860,10 @@ int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profil
 // the caller uploads: ranges, channel records, channel tables, survival
 // products): one range per launch range of the program, and the
 // shared-memory layout.  A range's ops and measurement tab words are staged
-// in shared memory while the staging buffers stay within kFrameStageMax;
-// ranges that would need more read them from global memory.  E_ARG: the
-// program does not fit this kernel (the per-shot plan runs instead).
+// in shared memory while the staging buffers stay within kFrameStageMax and
+// the sign kernel's shared memory; ranges that would need more read them
+// from global memory.  E_ARG: the program does not fit this kernel (the
+// per-shot plan runs instead).
 int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev> &ranges,
                      std::vector<FrameSlotDev> &slots, std::vector<uint32_t> &s64, std::vector<uint32_t> &events,
                      std::vector<int32_t> &nv_range, std::vector<FrameChanTab> &ctabs,
@@ -968,7 +969,13 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
     job.n_surv = (uint32_t)surv.size();
     job.nnv = (int32_t)nv_range.size();
     job.stage_tabs = (size_t)job.n_ctab * sizeof(FrameChanTab) + (size_t)job.n_thr * 8 + (size_t)job.n_surv * 4 <= kFrameTabStage ? 1u : 0u;
-    // staging: drop the largest staged range until the buffers fit
+    // staging: drop the largest staged range until the buffers fit, each
+    // within kFrameStageMax and both within what the rest of the sign
+    // kernel's shared memory leaves
+    job.stage_u32 = 0;
+    job.max_ops = 0;
+    const size_t rest = frame_job_smem(job) + 64;  // + alignment of the two buffers
+    const size_t stage_max = rest < kSegSmemMax ? std::min(kFrameStageMax, (kSegSmemMax - rest) / 2 & ~(size_t)15) : 0;
     std::vector<char> on(ranges.size(), 1);
     for (;;) {
         uint32_t tab = 0, nops = 0;
@@ -985,7 +992,7 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
         }
         job.stage_u32 = tab;
         job.max_ops = nops;
-        if (worst == ranges.size() || (size_t)tab * 4 + (size_t)nops * sizeof(FrameOp) <= kFrameStageMax) break;
+        if (worst == ranges.size() || (size_t)tab * 4 + (size_t)nops * sizeof(FrameOp) <= stage_max) break;
         on[worst] = 0;
     }
     for (size_t i = 0; i < ranges.size(); ++i) ranges[i].stage = on[i] ? 1u : 0u;
@@ -1006,7 +1013,7 @@ int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
         if (prof && rc == OK && prof->end() != OK) return E_CUDA;
         return rc;
     };
-    if (prof || !c->fstream) {
+    if (prof || !c->fstream || c->ftable.chunks == 0) {
         int rc = timed(P_SAMPLE, [&] { return launch_noise_vectors(st, c->ftable); });
         if (rc == OK) rc = timed(P_FRAME, [&] { return launch_frame_run(st, c->ftable, c->opts.frame_warps); });
         if (rc != OK) return rc;
@@ -1045,6 +1052,7 @@ int capture_graphs(ps_circuit *c) {
         if (c->graph[reset]) cudaGraphDestroy(c->graph[reset]);
         c->exec[reset] = nullptr;
         c->graph[reset] = nullptr;
+        if (reset == 0 && c->h->signs_only) continue;  // runs only from |0...0>
         cudaStream_t cs;
         PS_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
@@ -1252,6 +1260,8 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         set_error(msg);  // keep the failing step's message
         return rc;
     };
+    if (h->signs_only && (!fused || c->opts.per_shot_xz))
+        return bail(fail(E_STATE, "a signs-only state runs only the fused shared-x/z plan"));
 
     // ---- validate ops, assign events / records / thresholds
     std::vector<uint32_t> event_of(ops.size(), 0);
@@ -1272,10 +1282,14 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         }
         if (o.code == OP_M && o.c >= 0 && (uint64_t)o.c >= nparams)
             return bail(fail(E_ARG, "op " + std::to_string(i) + ": bias index out of range"));
+        if (o.code == OP_M && o.c >= 0 && !(params[o.c] >= 0.0f && params[o.c] <= 1.0f))
+            return bail(fail(E_ARG, "op " + std::to_string(i) + ": bias is not a number in [0, 1]"));
         if (is_channel(o.code)) {
             const int cnt = o.code == OP_PAULI2 ? 15 : 3;
             if (o.c < 0 || (uint64_t)o.c + cnt > nparams)
                 return bail(fail(E_ARG, "op " + std::to_string(i) + ": channel parameters out of range"));
+            if (check_channel_probs(params + o.c, cnt) != OK)
+                return bail(fail(E_ARG, "op " + std::to_string(i) + ": " + ps_last_error()));
             uint64_t t[16];
             channel_thresholds(params + o.c, cnt, t);
             // one copy of each distinct table (the same probabilities on
@@ -1429,7 +1443,7 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         if (upload(h, c->owned, psurv, &c->d_psurv) != OK) return bail(E_CUDA);
     }
     pick_tile(c);
-    if (fused) {
+    if (fused && !h->signs_only) {  // per-shot channel scratch (a signs-only state never runs that plan)
         c->entry_cap = (int32_t)std::max<size_t>(1, max_slots);
         void *p = nullptr;
         if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * sizeof(NoiseEntry)) != OK)
@@ -1616,10 +1630,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 c->ftable.njobs = 1;
                 c->ftable.ctas = h->w;
                 c->ftable.nctas = ncta0[1];
-                c->ftable.chunks = chunk0[1];
+                c->ftable.chunks = h->signs_only ? 0 : chunk0[1];  // signs only: no x / z to write
                 c->ftable.smem = frame_job_smem(job);
                 c->ftable.nsmem = job.nnv > 0 ? noise_job_smem(job) : 0;
-                if (cudaStreamCreateWithFlags(&c->fstream, cudaStreamNonBlocking) != cudaSuccess)
+                if (!h->signs_only && cudaStreamCreateWithFlags(&c->fstream, cudaStreamNonBlocking) != cudaSuccess)
                     return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
                 for (cudaEvent_t &e : c->fev)
                     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
@@ -1628,6 +1642,8 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
             }
         }
     }
+    if (h->signs_only && !c->frame_ok)
+        return bail(fail(E_STATE, "the circuit needs per-shot tableaux, which a signs-only state does not hold"));
 
     // ---- stats
     ps_circuit_stats &st = c->stats;
@@ -1727,6 +1743,7 @@ ps_status ps_circuit_run(ps_circuit *c, int reset_state) {
     ps_enter(__func__, __LINE__);
     if (!c) return fail(E_ARG, "null circuit");
     ps_state *h = c->h;
+    if (h->signs_only && !reset_state) return fail(E_STATE, "a signs-only state runs only from |0...0>");
     const RunParams p = begin_run(c, reset_state != 0);
     set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base, p.word_base);
     PS_CUDA(cudaGetLastError());
@@ -1763,6 +1780,7 @@ ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *rand
     ps_enter(__func__, __LINE__);
     if (!c || !random_branch || !rows) return fail(E_ARG, "null argument");
     ps_state *h = c->h;
+    if (h->signs_only) return fail(E_STATE, "measurement statistics need per-shot tableaux");
     const size_t nm = c->meas.size();
     if (nm == 0) return OK;
     int32_t *d = nullptr;
@@ -1811,7 +1829,7 @@ ps_status ps_circuit_autotune(ps_circuit *c, ps_circuit_options *chosen, double 
     ps_enter(__func__, __LINE__);
     if (!c) return fail(E_ARG, "null circuit");
     if (tune_ms) *tune_ms = 0.0;
-    if (c->opts.mode == PS_MODE_FUSED) {
+    if (c->opts.mode == PS_MODE_FUSED && !c->h->signs_only) {  // the per-shot plan's tiles
         int rc = autotune(c, tune_ms);
         if (rc != OK) return rc;
         c->stats.seg_rows = c->opts.seg_rows;

@@ -3,6 +3,8 @@
 // of all W rows.  This is the drop-in for the reference's per-gate
 // parallel_for launches (CliffordState.hpp:348-531) and the baseline the
 // fused circuit form is measured against.
+#include <cuda.h>
+
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -247,6 +249,13 @@ int launch_channel_apply(cudaStream_t st, ps_state *h, int64_t a, int64_t b, con
     return OK;
 }
 
+int check_channel_probs(const float *p, int count) {
+    for (int k = 0; k < count; ++k)
+        if (!std::isfinite(p[k]) || p[k] < 0.0f || p[k] > 1.0f)
+            return fail(E_ARG, "channel probability " + std::to_string(k) + " is not a number in [0, 1]");
+    return OK;
+}
+
 void channel_thresholds(const float *p, int count, uint64_t *thr) {
     double cum = 0.0;
     for (int k = 0; k < count; ++k) {
@@ -317,20 +326,55 @@ __global__ void noalloc_set_thresholds(uint64_t *thr, uint64_t t0, uint64_t t1, 
     thr[3] = s64;
 }
 
-// Device address of the array, looked up once per device on the first call
-// made with that device current (so that first call should not happen during
-// stream capture).
+// Id of the current CUDA context, 0 when it cannot be had (no context yet,
+// or a driver without cuCtxGetId).  The driver calls are fetched through the
+// runtime, so the library does not link the driver library itself.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(p);
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the array, kept per device together with the id of the
+// context it was looked up in: a context torn down and created again (after
+// cudaDeviceReset) loads the module again, possibly elsewhere, and gets a
+// new id, so the address is looked up again.  Without an id the address is
+// looked up on every call.  A lookup should not happen during stream
+// capture.
 std::mutex g_noalloc_mu;
 void *g_noalloc_ptr[64] = {nullptr};
+unsigned long long g_noalloc_ctx[64] = {0};
 
 int noalloc_scratch(int dev, u64 **out) {
     if (dev < 0 || dev >= 64) return fail(E_ARG, "device index out of range");
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_noalloc_ptr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
         g_noalloc_ptr[dev] = p;
+        g_noalloc_ctx[dev] = current_context_id();  // the lookup made the context current if it was not
     }
     *out = static_cast<u64 *>(g_noalloc_ptr[dev]);
     return OK;

@@ -99,6 +99,10 @@ struct ps_state {
     bool valid = false;
     // Device memory source: nullptr = cudaMalloc / cudaFree, else a pool.
     ps::DevPool *pool = nullptr;
+    // Signs only: X and Z are not allocated.  Such a state runs only
+    // compiled circuits whose shared-x/z plan runs from |0...0> and gives
+    // only measurement records (the sampling jobs of the request loop).
+    bool signs_only = false;
 };
 
 namespace ps {
@@ -109,7 +113,7 @@ void ps_enter(const char *method, int line);
 // Device memory of a state and of everything compiled for it.
 int dev_alloc(ps_state *h, void **p, size_t bytes);
 void dev_free(ps_state *h, void *p);
-int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed, DevPool *pool = nullptr);
+int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed, DevPool *pool = nullptr, bool signs_only = false);
 // Raises a kernel's dynamic shared-memory limit to the device's opt-in
 // maximum, once per (kernel, device).  The limit is a process-wide property
 // of the kernel, so it is only ever raised: launches from other host threads
@@ -135,6 +139,11 @@ int launch_pauli_channel(ps_state *h, int64_t a, int64_t b, const uint64_t *thre
 // A Pauli channel's table (channel_word) from its float probabilities:
 // count + 1 entries.
 void channel_thresholds(const float *p, int count, uint64_t *thr);
+// E_ARG unless every probability is finite and in [0, 1].  A table whose
+// sum passes 1 is kept: its cumulative thresholds stop at 1, so the
+// outcomes past that point are cut short in table order (the oracle and
+// the committed fixtures define this).
+int check_channel_probs(const float *p, int count);
 
 // ps_measure.cu
 struct RunParams;
@@ -180,7 +189,7 @@ RunParams circuit_begin_run(ps_circuit *c, bool reset);           // host bookke
 RunParams *circuit_params_dev(ps_circuit *c);                     // device run parameters
 ps_state *circuit_state(ps_circuit *c);
 // ps_state.cu: device bytes state_alloc takes.
-size_t state_bytes(int64_t n, int64_t S);
+size_t state_bytes(int64_t n, int64_t S, bool signs_only = false);
 }  // namespace ps
 
 namespace ps {

@@ -151,8 +151,9 @@ void dev_free(ps_state *h, void *p) {
         cudaFree(p);
 }
 
-int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed, DevPool *pool) {
+int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed, DevPool *pool, bool signs_only) {
     h->n = n;
+    h->signs_only = signs_only;
     h->S = S;
     h->W = 2 * n + 1;
     h->pool = pool;
@@ -165,7 +166,7 @@ int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed, DevPool *pool) 
     PS_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t plane = (size_t)h->W * (size_t)(n > 0 ? n : 1) * (size_t)w * sizeof(u64);
     void *px = nullptr, *pz = nullptr, *pr = nullptr;
-    if (dev_alloc(h, &px, plane) != OK || dev_alloc(h, &pz, plane) != OK ||
+    if ((!signs_only && (dev_alloc(h, &px, plane) != OK || dev_alloc(h, &pz, plane) != OK)) ||
         dev_alloc(h, &pr, (size_t)h->W * w * sizeof(u64)) != OK) {
         dev_free(h, px);
         dev_free(h, pz);
@@ -184,12 +185,12 @@ int state_alloc(ps_state *h, int64_t n, int64_t S, int64_t seed, DevPool *pool) 
 }
 
 // Bytes state_alloc takes for a state of n qubits and S shots.
-size_t state_bytes(int64_t n, int64_t S) {
+size_t state_bytes(int64_t n, int64_t S, bool signs_only) {
     int64_t w = (S + 63) / 64;
     w = (w + 1) & ~int64_t(1);
     if (w == 0) w = 2;
     const size_t W = 2 * (size_t)n + 1;
-    return 2 * W * (size_t)(n > 0 ? n : 1) * (size_t)w * 8 + W * (size_t)w * 8 + 5 * (size_t)w * 8;
+    return (signs_only ? 0 : 2 * W * (size_t)(n > 0 ? n : 1) * (size_t)w * 8) + W * (size_t)w * 8 + 5 * (size_t)w * 8;
 }
 
 void state_free(ps_state *h) {

@@ -158,6 +158,7 @@ class JobResult(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("queued", C.c_uint64), ("active", C.c_uint64), ("cancelled", C.c_uint64),
+                ("tableau_jobs", C.c_uint64),
                 ("shot_gates_completed", C.c_uint64),
                 ("pool_bytes", C.c_uint64), ("pool_peak_bytes", C.c_uint64), ("p50_latency_s", C.c_double),
                 ("p99_latency_s", C.c_double), ("mean_latency_s", C.c_double), ("max_latency_s", C.c_double),

@@ -133,10 +133,44 @@ def test_server_refuses_job_over_budget(ps):
     from plaquette_simulator import _lib
     from plaquette_simulator.batch import Server
     job = _small_jobs()[4]
-    with Server(hbm_budget_bytes=4 << 20, max_active=2) as srv:
+    with Server(hbm_budget_bytes=1 << 20, max_active=2) as srv:
         with pytest.raises(_lib.PlaquetteError) as e:
             srv.submit(job)
         assert e.value.status == _lib.PS_E_NOMEM
+
+
+@pytest.mark.gpu
+def test_server_signs_only_and_feed_forward_jobs(ps):
+    """A job with no record-controlled gate holds no per-shot tableaux while
+    admitted: its device bytes stay far below its x / z planes alone.  A job
+    with one (H on a measured record) keeps them.  Both give the records
+    they give alone, in either order of admission."""
+    from plaquette_simulator.batch import Job, Server
+    from plaquette_simulator import circuits as C
+    plain = Job(C.surface_code_memory(9, 3, p=1e-3), 8192, 21, 9, 1e-3)
+    ffc = C.Circuit(3)
+    ffc.h(0)
+    ffc.m(0)
+    ffc.h_if(1, 0)
+    ffc.cx(1, 2)
+    ffc.m(1)
+    ffc.m(2)
+    ff = Job(ffc, 4096, 22, 3, 0.0)
+    for order in ((plain, ff), (ff, plain)):
+        with Server(hbm_budget_bytes=1 << 30, max_active=2) as srv:
+            ids = [srv.submit(j) for j in order]
+            got = [srv.records(i) for i in ids]
+            infos = [srv.wait(i) for i in ids]
+        for job, (res, det), info in zip(order, got, infos):
+            n = job.num_qubits
+            w = ((job.shots + 63) // 64 + 1) & ~1
+            planes = 2 * (2 * n + 1) * n * w * 8
+            if job is plain:
+                assert info["device_bytes"] < planes // 4, (info["device_bytes"], planes)
+            else:
+                assert info["device_bytes"] >= planes
+            alone = _alone(ps, job)[0]
+            assert np.array_equal(res, alone[0]) and np.array_equal(det, alone[1])
 
 
 @pytest.mark.gpu

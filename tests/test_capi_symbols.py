@@ -39,6 +39,36 @@ def test_last_error_and_version_without_gpu():
     assert b"Error in Plaquette" in lib.ps_last_error()
 
 
+def test_channel_probabilities_checked_on_the_host():
+    """Pauli-channel probabilities are checked before the handle (and before
+    any device work): each finite and in [0, 1].  A table summing past 1 is
+    taken (its cumulative thresholds stop at 1).  A null handle with valid
+    probabilities fails on the handle instead."""
+    import build as psbuild
+    lib = ctypes.CDLL(psbuild.build())
+    lib.ps_last_error.restype = ctypes.c_char_p
+    P3, P15 = ctypes.c_float * 3, ctypes.c_float * 15
+    nan, inf = float("nan"), float("inf")
+    for fn in (lib.ps_pauli_channel_1, lib.ps_pauli_channel_1_noalloc):
+        for bad in ((nan, 0, 0), (-0.1, 0, 0), (0, 1.5, 0), (0, 0, inf), (0, -inf, 0)):
+            assert fn(None, ctypes.c_uint64(0), P3(*bad)) == 1, bad
+            assert b"probabilit" in lib.ps_last_error(), bad
+        for good in ((0.0, 0.0, 0.0), (0.1, 0.2, 0.3), (1.0, 0.0, 0.0), (1 / 3, 1 / 3, 1 / 3), (0.5, 0.4, 0.2)):
+            assert fn(None, ctypes.c_uint64(0), P3(*good)) == 1
+            assert b"probabilit" not in lib.ps_last_error(), good
+    bad15 = [0.0] * 15
+    bad15[7] = nan
+    assert lib.ps_pauli_channel_2(None, ctypes.c_uint64(0), ctypes.c_uint64(1), P15(*bad15)) == 1
+    assert b"probabilit" in lib.ps_last_error()
+    neg = [0.01] * 15
+    neg[14] = -1e-3
+    assert lib.ps_pauli_channel_2(None, ctypes.c_uint64(0), ctypes.c_uint64(1), P15(*neg)) == 1
+    assert b"probability 14" in lib.ps_last_error()
+    ok15 = [0.07] * 15  # sums to 1.05: taken
+    assert lib.ps_pauli_channel_2(None, ctypes.c_uint64(0), ctypes.c_uint64(1), P15(*ok15)) == 1
+    assert b"probabilit" not in lib.ps_last_error()
+
+
 def test_product_has_no_oracle_dependency():
     """The CUDA library and the Python package never reference the oracle."""
     pkg = os.path.join(ROOT, "plaquette-simulator_gb300")

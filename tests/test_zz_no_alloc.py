@@ -45,6 +45,24 @@ def test_noalloc_channel_matches_allocating_entry_point(ps):
         assert ref.event_counter() == new.event_counter()
 
 
+def test_noalloc_channel_at_the_size_limit(ps):
+    """The largest batch it takes: 64 * 8192 shots, exactly 8192 shot-words,
+    so the outcome masks fill the whole array behind the threshold slots."""
+    from plaquette_simulator import _lib
+    L = _lib.load()
+    n, shots, seed = 1, 64 * 8192, 777
+    ref = _prepare(ps, n, shots, seed)
+    new = _prepare(ps, n, shots, seed)
+    for probs in ((0.3, 0.2, 0.1), (0.05, 0.0, 0.6)):
+        p = np.asarray(probs, dtype=np.float32)
+        _lib.check(L.ps_pauli_channel_1(ref.handle, 0, p.ctypes.data_as(C.c_void_p)))
+        _lib.check(L.ps_pauli_channel_1_noalloc(new.handle, 0, p.ctypes.data_as(C.c_void_p)))
+        new.synchronize()
+        for a, b in zip(ref.device_to_host_numpy(), new.device_to_host_numpy()):
+            assert np.array_equal(a, b)
+        assert ref.event_counter() == new.event_counter()
+
+
 def test_noalloc_channel_rejects_oversized_batch(ps):
     from plaquette_simulator import _lib
     L = _lib.load()

@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving leg: arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="serving leg: HBM admission budget")
     ap.add_argument("--serve-drain-s", type=float, default=180.0, help="serving leg: longest wait for the backlog")
+    ap.add_argument("--capacity-rate", type=float, default=2000.0,
+                    help="capacity leg: arrivals per second (the same job mix, well above the serving rate)")
+    ap.add_argument("--capacity-seconds", type=float, default=10.0,
+                    help="capacity leg: seconds of arrivals (0 = skip)")
     return ap.parse_args()
 
 
@@ -231,9 +235,11 @@ def run_reference(args):
 # ------------------------------------------------------- batch and serving
 def batch_leg(args, rank, torch):
     """64 uneven surface-code jobs (d in 3..21, d rounds, shots log-uniform in
-    [256, 65536], p in {1e-4, 1e-3, 5e-3}) in ONE graph launch per run, tiles
-    chosen by the autotuner; beside it the same compiled jobs run one after
-    another."""
+    [256, 65536], p in {1e-4, 1e-3, 5e-3}) in ONE graph launch per run: one
+    job table, so the noise vectors, sign programs and x / z broadcasts of
+    all jobs are three kernel launches, with the sign-kernel warps and
+    broadcast CTAs chosen by timing the table; beside it the same compiled
+    jobs run one after another."""
     from plaquette_simulator.batch import Batch, uneven_surface_jobs
     from plaquette_simulator.circuit import CompiledCircuit
     jobs = uneven_surface_jobs(args.batch_jobs, seed=12345 + 7919 * rank)
@@ -263,32 +269,69 @@ def batch_leg(args, rank, torch):
         cc.run(reset=True)
         b._L.ps_device_synchronize()
     seq_ms = (time.perf_counter() - t1) * 1e3
-    shapes = sorted({(jobs[j].distance, *b.job_options(j).values()) for j in range(len(jobs))})
+    others = sorted({(jobs[j].distance, *b.job_options(j).values()) for j in range(len(jobs))}) \
+        if b.stats["table_jobs"] < len(jobs) else []
     out = {"workload": f"{len(jobs)} uneven rotated surface-code memory jobs, d uniform in 3..21 (d rounds), "
-                       "shots log-uniform in [256, 65536], p in {1e-4, 1e-3, 5e-3}, one CUDA graph launch",
+                       "shots log-uniform in [256, 65536], p in {1e-4, 1e-3, 5e-3}, one CUDA graph launch "
+                       "over one job table",
            "value": sg / (ms / 1e3), "unit": "shot-gates/s", "ms_per_run": ms, "runs": k,
            "shot_gates_per_run": sg, "tableau_gb": b.stats["tableau_bytes"] / 1e9,
            "launches_per_run": b.stats["launches_per_run"], "setup_s": setup_s,
            "compile_ms": b.stats["compile_ms"], "tune_ms": b.stats["tune_ms"],
            "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / ms,
-           "tiles": [{"d": s[0], "seg_rows": s[1], "seg_words": s[2], "seg_threads": s[3], "meas_words": s[4]}
-                     for s in shapes]}
+           "table": {"jobs": b.stats["table_jobs"], "frame_warps": b.stats["frame_warps"],
+                     "bcast_ctas": b.stats["bcast_ctas"]},
+           # per-shot tiles only matter for jobs outside the table
+           "per_shot_tiles": [{"d": s[0], "seg_rows": s[1], "seg_words": s[2], "seg_threads": s[3],
+                               "meas_words": s[4]} for s in others]}
     del seq
     b.close()
     return out
 
 
-def serving_leg(args, rank):
+def serving_leg(args, rank, rate=None, seconds=None):
     """Poisson arrivals of sampling jobs (sizes as the batch leg plus d=25),
-    admitted by tableau bytes against an HBM budget; p50/p99 latency."""
+    admitted by device bytes against an HBM budget; p50/p99 latency."""
     from plaquette_simulator.batch import Server, poisson_arrivals, uneven_surface_jobs
-    arrivals = poisson_arrivals(args.serve_rate, args.serve_seconds, seed=12345 + rank)
+    rate = args.serve_rate if rate is None else rate
+    seconds = args.serve_seconds if seconds is None else seconds
+    arrivals = poisson_arrivals(rate, seconds, seed=12345 + rank)
     jobs = uneven_surface_jobs(len(arrivals), seed=24680 + rank, distances=tuple(range(3, 22, 2)) + (25,),
                                job_seed_base=100000)
     offered = sum(j.shot_gates() for j in jobs)
     from plaquette_simulator.circuit import compile_cache_stats
     cache0 = compile_cache_stats()
+    import queue
+    errors = {}
     with Server(hbm_budget_bytes=int(args.serve_budget_gb * 1e9), max_active=16, autotune=False) as srv:
+        # A client thread takes each job's result as it finishes and releases
+        # its host records (as a caller that consumes its results would), so
+        # host memory holds only the jobs in flight.
+        from plaquette_simulator import _lib
+        done_q = queue.Queue()
+        stop = threading.Event()
+
+        def consume():
+            while not stop.is_set():
+                item = done_q.get()
+                if item is None:
+                    return
+                i, j = item
+                while not stop.is_set():
+                    try:
+                        srv.wait(i, 0.5)
+                        srv.release(i)
+                        break
+                    except _lib.PlaquetteError as e:
+                        if e.status == _lib.PS_E_TIMEOUT:
+                            continue
+                        # a failed job: keep one message per kind
+                        errors.setdefault(str(e).split("Error in Plaquette:")[-1].strip()[:160], []).append(
+                            {"d": j.distance, "shots": j.shots})
+                        break
+
+        client = threading.Thread(target=consume, daemon=True)
+        client.start()
         t0 = srv.now()
         ids = []
         for t, j in zip(arrivals, jobs):
@@ -296,25 +339,22 @@ def serving_leg(args, rank):
             if dt > 0:
                 time.sleep(dt)
             ids.append(srv.submit(j))
+            done_q.put((ids[-1], j))
         submit_end = srv.now() - t0
+        done_q.put(None)
         drained = True
         try:
             srv.drain(args.serve_drain_s)
         except Exception:
             drained = False
-        errors = {}
-        if drained:
-            for i, j in zip(ids, jobs):
-                try:
-                    srv.wait(i, 0.0)
-                except Exception as e:  # a failed job: keep one message per kind
-                    errors.setdefault(str(e).split("Error in Plaquette:")[-1].strip()[:160], []).append(
-                        {"d": j.distance, "shots": j.shots})
+        client.join(timeout=30.0 if drained else 0.0)
+        stop.set()  # the server closes only after its client is done with it
+        client.join()
         st = srv.stats()
     span = max(1e-9, st["last_done_s"] - st["first_submit_s"])
     cache1 = compile_cache_stats()
     hits, misses = cache1["hits"] - cache0["hits"], cache1["misses"] - cache0["misses"]
-    return {"workload": f"Poisson arrivals at {args.serve_rate:g} jobs/s for {args.serve_seconds:g} s, "
+    return {"workload": f"Poisson arrivals at {rate:g} jobs/s for {seconds:g} s, "
                         "rotated surface-code memory jobs d in {3..21, 25} (d rounds), shots log-uniform in "
                         f"[256, 65536], admission by device bytes against {args.serve_budget_gb:g} GB",
             "jobs": len(ids), "completed": st["completed"], "failed": st["failed"], "drained": drained,
@@ -322,8 +362,8 @@ def serving_leg(args, rank):
             "p50_latency_s": st["p50_latency_s"], "p99_latency_s": st["p99_latency_s"],
             "mean_latency_s": st["mean_latency_s"], "max_latency_s": st["max_latency_s"],
             "value": st["shot_gates_completed"] / span, "unit": "shot-gates/s",
-            "offered_shot_gates_per_s": offered / args.serve_seconds,
-            "offered_jobs_per_s": len(ids) / args.serve_seconds,
+            "offered_shot_gates_per_s": offered / seconds,
+            "offered_jobs_per_s": len(ids) / seconds,
             "achieved_jobs_per_s": st["completed"] / span, "submit_span_s": submit_end,
             "pool_peak_gb": st["pool_peak_bytes"] / 1e9, "max_active": 16,
             "compile_cache": {"hits": hits, "misses": misses,
@@ -585,6 +625,10 @@ def main():
         line["serving"] = serving_leg(args, rank)
         line["p50_latency_s"] = line["serving"]["p50_latency_s"]
         line["p99_latency_s"] = line["serving"]["p99_latency_s"]
+    if args.capacity_seconds > 0:
+        # the same job mix offered far above the serving rate: what the
+        # server completes per second once it is the bottleneck
+        line["serving_capacity"] = serving_leg(args, rank, args.capacity_rate, args.capacity_seconds)
 
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(circ, seed, args.cpu_shots)

@@ -232,6 +232,9 @@ typedef struct {
     int32_t seg_rows, seg_words, seg_threads, meas_words;
     int32_t resident_segments;      /* segments in the register-resident form */
     int32_t shared_xz;              /* 1: runs from |0...0> use the shared-x/z plan */
+    int32_t frame_warps, bcast_ctas; /* shared-x/z knobs in use (sign-kernel warps
+                                        per shot-word, broadcast CTAs per SM) */
+    int32_t pad;
 } ps_circuit_stats;
 
 typedef struct ps_circuit ps_circuit;
@@ -331,6 +334,10 @@ typedef struct {
     uint64_t tableau_bytes;       /* device bytes of all job tableaux        */
     uint64_t launches_per_run;    /* kernels in one batch run                 */
     double compile_ms, tune_ms;
+    uint64_t table_jobs;          /* jobs in the shared-x/z job table: three
+                                     launches in all for them                */
+    int32_t frame_warps, bcast_ctas; /* the table's knobs (sign-kernel warps
+                                        per shot-word, broadcast CTAs per SM) */
 } ps_batch_stats;
 
 typedef struct ps_batch ps_batch;

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/plaquette_gpu.h"
+#include "ps_frame_dev.h"
 #include "ps_internal.h"
 #include "ps_segment.cuh"
 
@@ -181,19 +182,33 @@ struct ps_batch {
     RunParams **d_dst = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // Jobs that run the shared-x/z plan share one job table: each of its
+    // kernels (noise vectors, signs, x / z broadcast) is one launch for all
+    // of them.  The others run their own plans on branches.
+    std::vector<size_t> table_jobs;  // job indices, in table order
+    std::vector<char> in_table;      // [job]
+    ps::FrameTable table;
+    std::vector<void *> table_mem;
+    cudaStream_t side = nullptr;
+    cudaEvent_t tfork = nullptr, tjoin = nullptr;
+    int frame_warps = 8, bcast_ctas = 1;
 };
 
 namespace ps {
 namespace {
 
-// Root scatter node, then every job on its own branch, joined back.
+// Root scatter node, then the job table's kernels on the main stream and
+// every other job on its own branch, joined back.
 int enqueue_batch(ps_batch *b) {
     const int nj = (int)b->circs.size();
     batch_params_kernel<<<1, 256, 0, b->stream>>>(b->d_dst, b->d_vals, nj);
     PS_CUDA(cudaGetLastError());
     PS_CUDA(cudaEventRecord(b->fork, b->stream));
+    if (!b->table_jobs.empty())
+        TRY(frame_table_enqueue(b->table, b->stream, b->side, b->tfork, b->tjoin, b->frame_warps, b->bcast_ctas));
     for (size_t k = 0; k < b->order.size(); ++k) {
         const size_t j = b->order[k];
+        if (b->in_table[j]) continue;
         PS_CUDA(cudaStreamWaitEvent(b->branches[k], b->fork, 0));
         TRY(circuit_enqueue(b->circs[j], b->branches[k], true));
         PS_CUDA(cudaEventRecord(b->joins[k], b->branches[k]));
@@ -258,8 +273,11 @@ ps_status ps_batch_create(const ps_job_desc *jobs, uint64_t njobs, const ps_batc
             return bail(rcs[j]);
         }
     b->stats.compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (b->opts.autotune) {
+    if (b->opts.autotune) {  // the per-shot plans (jobs of the table are tuned together below)
         for (uint64_t j = 0; j < njobs; ++j) {
+            FrameJobDev fjd{};
+            BroadcastJobDev bjd{};
+            if (circuit_frame_job(b->circs[j], &fjd, &bjd)) continue;
             double ms = 0.0;
             int rc = ps_circuit_autotune(b->circs[j], nullptr, &ms);
             if (rc != OK) return bail(rc);
@@ -282,9 +300,71 @@ ps_status ps_batch_create(const ps_job_desc *jobs, uint64_t njobs, const ps_batc
     std::iota(b->order.begin(), b->order.end(), size_t(0));
     std::stable_sort(b->order.begin(), b->order.end(), [&](size_t x, size_t y) { return work[x] > work[y]; });
 
+    // ---- the job table of the shared-x/z jobs (largest first)
+    b->in_table.assign(njobs, 0);
+    {
+        std::vector<FrameJobDev> fj;
+        std::vector<BroadcastJobDev> bj;
+        std::vector<int64_t> cta0{0}, ncta0{0}, chunk0{0};
+        for (size_t j : b->order) {
+            FrameJobDev job{};
+            BroadcastJobDev bjob{};
+            if (!circuit_frame_job(b->circs[j], &job, &bjob)) continue;
+            b->in_table[j] = 1;
+            b->table_jobs.push_back(j);
+            fj.push_back(job);
+            bj.push_back(bjob);
+            cta0.push_back(cta0.back() + job.w);
+            ncta0.push_back(ncta0.back() + (int64_t)job.nnv * job.w);
+            chunk0.push_back(chunk0.back() + broadcast_chunks(job.n, job.w));
+            b->table.smem = std::max(b->table.smem, frame_job_smem(job));
+            if (job.nnv > 0) b->table.nsmem = std::max(b->table.nsmem, noise_job_smem(job));
+        }
+        if (!fj.empty()) {
+            auto up = [&](const void *src, size_t bytes, void **dst) -> int {
+                if (cudaMalloc(dst, std::max<size_t>(bytes, 16)) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaMalloc");
+                b->table_mem.push_back(*dst);
+                PS_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+                return OK;
+            };
+            void *p[6] = {};
+            const unsigned long long zero[2] = {0ull, 0ull};  // the broadcast's counters
+            int rc = up(fj.data(), fj.size() * sizeof(FrameJobDev), &p[0]);
+            if (rc == OK) rc = up(zero, sizeof zero, &p[5]);
+            if (rc == OK) rc = up(bj.data(), bj.size() * sizeof(BroadcastJobDev), &p[1]);
+            if (rc == OK) rc = up(cta0.data(), cta0.size() * sizeof(int64_t), &p[2]);
+            if (rc == OK) rc = up(ncta0.data(), ncta0.size() * sizeof(int64_t), &p[3]);
+            if (rc == OK) rc = up(chunk0.data(), chunk0.size() * sizeof(int64_t), &p[4]);
+            if (rc != OK) return bail(rc);
+            b->table.jobs = static_cast<const FrameJobDev *>(p[0]);
+            b->table.bjobs = static_cast<const BroadcastJobDev *>(p[1]);
+            b->table.cta0 = static_cast<const int64_t *>(p[2]);
+            b->table.ncta0 = static_cast<const int64_t *>(p[3]);
+            b->table.chunk0 = static_cast<const int64_t *>(p[4]);
+            b->table.bctr = static_cast<unsigned long long *>(p[5]);
+            b->table.njobs = (int32_t)fj.size();
+            b->table.ctas = cta0.back();
+            b->table.nctas = ncta0.back();
+            b->table.chunks = chunk0.back();
+            // the table's launches stand for its jobs' own
+            for (size_t j : b->table_jobs) {
+                ps_circuit_stats cs{};
+                ps_circuit_get_stats(b->circs[j], &cs);
+                b->stats.launches_per_run -= cs.launches_per_run;
+            }
+            b->stats.launches_per_run += 1 + (b->table.nctas > 0 ? 1 : 0) + (b->table.chunks > 0 ? 1 : 0);
+        }
+        b->stats.table_jobs = fj.size();
+    }
+
     // ---- streams, parameter staging
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+        return bail(cuda_fail(cudaGetLastError(), "stream/event"));
+    if (!b->table_jobs.empty() &&
+        (cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaEventCreateWithFlags(&b->tfork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&b->tjoin, cudaEventDisableTiming) != cudaSuccess))
         return bail(cuda_fail(cudaGetLastError(), "stream/event"));
     b->branches.assign(njobs, nullptr);
     b->joins.assign(njobs, nullptr);
@@ -306,6 +386,21 @@ ps_status ps_batch_create(const ps_job_desc *jobs, uint64_t njobs, const ps_batc
         if (cudaMemcpy(b->d_dst, dst.data(), njobs * sizeof(RunParams *), cudaMemcpyHostToDevice) != cudaSuccess)
             return bail(cuda_fail(cudaGetLastError(), "cudaMemcpy"));
     }
+    // ---- the table's knobs, timed on the table itself
+    if (b->opts.autotune && !b->table_jobs.empty()) {
+        const auto tt = std::chrono::steady_clock::now();
+        std::vector<RunParams> cur(njobs);
+        for (uint64_t j = 0; j < njobs; ++j) cur[j] = circuit_current_params(b->circs[j]);
+        if (cudaMemcpy(b->d_vals, cur.data(), njobs * sizeof(RunParams), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(cuda_fail(cudaGetLastError(), "cudaMemcpy"));
+        batch_params_kernel<<<1, 256, 0, b->stream>>>(b->d_dst, b->d_vals, (int)njobs);
+        int rc = frame_table_tune(b->table, b->stream, b->side, b->tfork, b->tjoin, &b->frame_warps, &b->bcast_ctas,
+                                  nullptr);
+        if (rc != OK) return bail(rc);
+        b->stats.tune_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tt).count();
+    }
+    b->stats.frame_warps = b->frame_warps;
+    b->stats.bcast_ctas = b->bcast_ctas;
     // ---- one graph for the whole batch
     if (b->opts.use_graph) {
         cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
@@ -318,7 +413,7 @@ ps_status ps_batch_create(const ps_job_desc *jobs, uint64_t njobs, const ps_batc
         }
         if (e2 != cudaSuccess) return bail(cuda_fail(e2, "cudaStreamEndCapture"));
         b->graph = g;
-        e = cudaGraphInstantiate(&b->exec, g, 0);
+        e = cudaGraphInstantiateWithFlags(&b->exec, g, cudaGraphInstantiateFlagUseNodePriority);
         if (e != cudaSuccess) return bail(cuda_fail(e, "cudaGraphInstantiate"));
     }
     *out = b;
@@ -391,6 +486,10 @@ ps_status ps_batch_destroy(ps_batch *b) {
         if (b->copied[r]) cudaEventDestroy(b->copied[r]);
     }
     if (b->fork) cudaEventDestroy(b->fork);
+    if (b->tfork) cudaEventDestroy(b->tfork);
+    if (b->tjoin) cudaEventDestroy(b->tjoin);
+    if (b->side) cudaStreamDestroy(b->side);
+    for (void *p : b->table_mem) cudaFree(p);
     cudaFree(b->d_vals);
     cudaFree(b->d_dst);
     if (b->stream) cudaStreamDestroy(b->stream);

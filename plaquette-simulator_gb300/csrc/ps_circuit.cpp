@@ -198,6 +198,8 @@ struct ps_circuit {
     // sign-kernel launch and one x / z broadcast beside it on a side stream.
     FrameTable ftable;
     int32_t *d_ferr = nullptr;       // the sign kernel's error word (a bounded wait gave up)
+    FrameJobDev fjob{};              // host copies of the one-job table's entries (batches gather them)
+    BroadcastJobDev fbjob{};
     cudaStream_t fstream = nullptr;  // the broadcast's side stream
     cudaEvent_t fev[2] = {nullptr, nullptr};
     cudaGraph_t graph[2] = {nullptr, nullptr};      // [reset_state]
@@ -1006,31 +1008,82 @@ int frame_job_ranges(ps_circuit *c, FrameJobDev &job, std::vector<FrameRangeDev>
 // broadcast of the final x / z bits (host-known, so it needs nothing else)
 // beside them on a side stream, joined back at the end.  Profiled, the three
 // run one after the other.
-int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventPair() {
+        if (cudaEventCreate(&a) != cudaSuccess) a = nullptr;
+        if (cudaEventCreate(&b) != cudaSuccess) b = nullptr;
+    }
+    ~EventPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+    bool ok() const { return a && b; }
+};
+
+int enqueue_frame_table(const FrameTable &t, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                        int warps, int bctas, Profiler *prof) {
     auto timed = [&](int kind, auto &&launch) -> int {
         if (prof && prof->begin(kind) != OK) return E_CUDA;
         int rc = launch();
         if (prof && rc == OK && prof->end() != OK) return E_CUDA;
         return rc;
     };
-    if (prof || !c->fstream || c->ftable.chunks == 0) {
-        int rc = timed(P_SAMPLE, [&] { return launch_noise_vectors(st, c->ftable); });
-        if (rc == OK) rc = timed(P_FRAME, [&] { return launch_frame_run(st, c->ftable, c->opts.frame_warps); });
+    if (prof || !side || t.chunks == 0) {
+        int rc = timed(P_SAMPLE, [&] { return launch_noise_vectors(st, t); });
+        if (rc == OK) rc = timed(P_FRAME, [&] { return launch_frame_run(st, t, warps); });
         if (rc != OK) return rc;
-        return timed(P_BROADCAST, [&] { return launch_broadcast_jobs(st, c->ftable, c->opts.bcast_ctas); });
+        return timed(P_BROADCAST, [&] { return launch_broadcast_jobs(st, t, bctas); });
     }
-    // The broadcast runs beside the noise vectors and the sign program.
-    // (Whatever runs beside its stream of stores slows down two- to
-    // three-fold; of the orders measured this one ends first.)
-    PS_CUDA(cudaEventRecord(c->fev[0], st));
-    PS_CUDA(cudaStreamWaitEvent(c->fstream, c->fev[0], 0));
-    int rc = launch_broadcast_jobs(c->fstream, c->ftable, c->opts.bcast_ctas);
-    if (rc == OK) rc = launch_noise_vectors(st, c->ftable);
+    // The broadcast runs beside the noise vectors and the sign program, at
+    // the highest priority, so that its CTAs hold their SMs from the start.
+    PS_CUDA(cudaEventRecord(fork, st));
+    PS_CUDA(cudaStreamWaitEvent(side, fork, 0));
+    int rc = launch_broadcast_jobs(side, t, bctas);
+    if (rc == OK) rc = launch_noise_vectors(st, t);
     if (rc != OK) return rc;
-    rc = launch_frame_run(st, c->ftable, c->opts.frame_warps);
+    rc = launch_frame_run(st, t, warps);
     if (rc != OK) return rc;
-    PS_CUDA(cudaEventRecord(c->fev[1], c->fstream));
-    PS_CUDA(cudaStreamWaitEvent(st, c->fev[1], 0));
+    PS_CUDA(cudaEventRecord(join, side));
+    PS_CUDA(cudaStreamWaitEvent(st, join, 0));
+    return OK;
+}
+
+int enqueue_frame(ps_circuit *c, cudaStream_t st, Profiler *prof) {
+    return enqueue_frame_table(c->ftable, st, c->fstream, c->fev[0], c->fev[1], c->opts.frame_warps,
+                               c->opts.bcast_ctas, prof);
+}
+
+// The fastest (sign-kernel warps, broadcast CTAs per SM) for a table: each
+// candidate runs twice (the first warms up), timed with events on st.  The
+// run parameters must be on the device already; the signs, records, noise
+// vectors and x / z the runs write are left behind.
+int tune_frame_table(const FrameTable &t, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                     int *warps, int *bctas, double *best_ms) {
+    EventPair ev;
+    if (!ev.ok()) return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+    float best = 3.0e38f;
+    const int wc[] = {8, 4};
+    const int bc[] = {1, 2};
+    for (int fw : wc)
+        for (int b : bc) {
+            if (t.chunks == 0 && b != 1) continue;  // no broadcast
+            float ms = 0.f;
+            for (int rep = 0; rep < 2; ++rep) {
+                PS_CUDA(cudaEventRecord(ev.a, st));
+                int rc = enqueue_frame_table(t, st, side, fork, join, fw, b, nullptr);
+                if (rc != OK) return rc;
+                PS_CUDA(cudaEventRecord(ev.b, st));
+                PS_CUDA(cudaEventSynchronize(ev.b));
+                PS_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+            }
+            if (ms < best) {
+                best = ms;
+                *warps = fw;
+                *bctas = b;
+            }
+        }
+    if (best_ms) *best_ms = best;
     return OK;
 }
 
@@ -1093,6 +1146,50 @@ RunParams begin_run(ps_circuit *c, bool reset) {
 }
 
 // ---- autotuner ---------------------------------------------------------
+// Shared-x/z knobs, cached per process by (qubits, shot-words, noise ranges,
+// broadcast or not).
+struct FrameTuneKey {
+    int64_t n, w, nctas;
+    bool bcast;
+    bool operator<(const FrameTuneKey &o) const {
+        if (n != o.n) return n < o.n;
+        if (w != o.w) return w < o.w;
+        if (nctas != o.nctas) return nctas < o.nctas;
+        return bcast < o.bcast;
+    }
+};
+std::mutex g_ftune_mu;
+std::map<FrameTuneKey, std::pair<int, int>> g_ftune_cache;
+
+int autotune_frame(ps_circuit *c, double *tune_ms) {
+    ps_state *h = c->h;
+    const auto t0 = std::chrono::steady_clock::now();
+    const FrameTuneKey key{h->n, h->w, c->ftable.nctas, c->ftable.chunks > 0};
+    {
+        std::lock_guard<std::mutex> lk(g_ftune_mu);
+        auto it = g_ftune_cache.find(key);
+        if (it != g_ftune_cache.end()) {
+            c->opts.frame_warps = it->second.first;
+            c->opts.bcast_ctas = it->second.second;
+            if (tune_ms) *tune_ms = 0.0;
+            return OK;
+        }
+    }
+    set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, (uint64_t)h->seed, h->events, (uint64_t)h->word_base);
+    PS_CUDA(cudaGetLastError());
+    int fw = 8, bc = 1;
+    int rc = tune_frame_table(c->ftable, h->stream, c->fstream, c->fev[0], c->fev[1], &fw, &bc, nullptr);
+    if (rc != OK) return rc;
+    c->opts.frame_warps = fw;
+    c->opts.bcast_ctas = bc;
+    {
+        std::lock_guard<std::mutex> lk(g_ftune_mu);
+        g_ftune_cache[key] = {fw, bc};
+    }
+    if (tune_ms) *tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return OK;
+}
+
 struct TuneKey {
     int64_t n, w;
     int nq;
@@ -1633,6 +1730,8 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 c->ftable.chunks = h->signs_only ? 0 : chunk0[1];  // signs only: no x / z to write
                 c->ftable.smem = frame_job_smem(job);
                 c->ftable.nsmem = job.nnv > 0 ? noise_job_smem(job) : 0;
+                c->fjob = job;
+                c->fbjob = bj;
                 if (!h->signs_only && cudaStreamCreateWithFlags(&c->fstream, cudaStreamNonBlocking) != cudaSuccess)
                     return bail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
                 for (cudaEvent_t &e : c->fev)
@@ -1670,7 +1769,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     st.launches_per_run += 1;  // run-parameter update
     if (c->frame_ok) {  // runs from |0...0>: the parameters, the sign kernel, the broadcast
         st.shared_xz = 1;
-        st.launches_per_run = c->ftable.nctas > 0 ? 4 : 3;
+        // parameters, noise vectors (when there are channels), signs, broadcast (unless signs only)
+        st.launches_per_run = 2 + (c->ftable.nctas > 0 ? 1 : 0) + (c->ftable.chunks > 0 ? 1 : 0);
+        st.frame_warps = c->opts.frame_warps > 0 ? c->opts.frame_warps : 8;
+        st.bcast_ctas = c->opts.bcast_ctas > 0 ? c->opts.bcast_ctas : 1;
     }
     st.seg_rows = c->opts.seg_rows;
     st.seg_words = c->opts.seg_words;
@@ -1829,6 +1931,14 @@ ps_status ps_circuit_autotune(ps_circuit *c, ps_circuit_options *chosen, double 
     ps_enter(__func__, __LINE__);
     if (!c) return fail(E_ARG, "null circuit");
     if (tune_ms) *tune_ms = 0.0;
+    if (c->opts.mode == PS_MODE_FUSED && c->frame_ok) {  // the shared-x/z kernels that runs from |0...0> use
+        double ms = 0.0;
+        int rc = autotune_frame(c, &ms);
+        if (rc != OK) return rc;
+        if (tune_ms) *tune_ms += ms;
+        c->stats.frame_warps = c->opts.frame_warps;
+        c->stats.bcast_ctas = c->opts.bcast_ctas;
+    }
     if (c->opts.mode == PS_MODE_FUSED && !c->h->signs_only) {  // the per-shot plan's tiles
         int rc = autotune(c, tune_ms);
         if (rc != OK) return rc;
@@ -1923,6 +2033,28 @@ ps_status ps_circuit_destroy(ps_circuit *c) {
 
 namespace ps {
 int circuit_enqueue(ps_circuit *c, cudaStream_t st, bool reset) { return enqueue_plan(c, st, reset); }
+int frame_table_enqueue(const FrameTable &t, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                        int warps, int bctas) {
+    return enqueue_frame_table(t, st, side, fork, join, warps, bctas, nullptr);
+}
+int frame_table_tune(const FrameTable &t, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                     int *warps, int *bctas, double *best_ms) {
+    return tune_frame_table(t, st, side, fork, join, warps, bctas, best_ms);
+}
+bool circuit_frame_job(const ps_circuit *c, FrameJobDev *job, BroadcastJobDev *bjob) {
+    if (!c->frame_ok || c->force_per_shot) return false;
+    *job = c->fjob;
+    *bjob = c->fbjob;
+    return true;
+}
+RunParams circuit_current_params(const ps_circuit *c) {
+    RunParams p;
+    p.seed = (uint64_t)c->h->seed;
+    p.event_base = c->h->events;
+    p.word_base = (uint64_t)c->h->word_base;
+    p.pad = 0;
+    return p;
+}
 RunParams circuit_begin_run(ps_circuit *c, bool reset) { return begin_run(c, reset); }
 RunParams *circuit_params_dev(ps_circuit *c) { return c->d_params; }
 ps_state *circuit_state(ps_circuit *c) { return c->h; }

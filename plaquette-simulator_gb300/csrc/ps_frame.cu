@@ -479,48 +479,89 @@ __global__ void __launch_bounds__(32 * FW, 24 / FW) frame_run_kernel(const Frame
     for (int64_t i = tid; i < W; i += NT) J.R[i * w + k] = sR[i];
 }
 
-// x / z of every shot from the shared bits.  A warp takes one chunk: one
-// (row, qubit) pair of a job whose rows are at least 32 words wide (lanes
-// over 16-byte word pairs), or 32 / (w/2) pairs of a narrower one.  Chunks
-// of a job are consecutive (chunk0).  A warp steps through its chunks c,
-// c + warps, ...; in a one-job table the wide form's (row, qubit) advances by
-// a constant step, so only the first pair takes a division.  The stores are
-// streaming (evict first): the broadcast passes 1.65 GB through L2 at
-// d = 15 and must not evict the tables of the kernels beside it.  At most
-// 32 registers a thread: two broadcast CTAs (16K registers) fit on an SM
-// beside six noise CTAs (48K) or two sign CTAs (40K).
+// One (row, qubit) chunk c of job B (local index `local`) by one warp: a
+// whole row of shot-words when the row is at least 32 words wide, else
+// 32 / (w/2) pairs side by side.
+__device__ __forceinline__ void broadcast_chunk(const BroadcastJobDev &B, int64_t local, int lane) {
+    const int64_t hw = B.w >> 1, pairs = (2 * B.n + 1) * B.n;
+    int64_t rq, kp0, step;
+    if (hw >= 16) {
+        rq = local;
+        kp0 = lane;
+        step = 32;
+    } else {
+        const int per = 32 / (int)hw;
+        rq = local * per + lane / (int)hw;
+        kp0 = lane % (int)hw;
+        step = hw;
+        if (lane >= per * (int)hw || rq >= pairs) return;
+    }
+    const int64_t row = rq / B.n, q = rq - row * B.n;
+    const u64 xb = (B.xz[(row * 2 + 0) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+    const u64 zb = (B.xz[(row * 2 + 1) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+    const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
+    u64 *xo = B.X + rq * B.w, *zo = B.Z + rq * B.w;
+    for (int64_t kp = kp0; kp < hw; kp += step) {
+        __stcs(reinterpret_cast<ulonglong2 *>(xo + 2 * kp), xv);
+        __stcs(reinterpret_cast<ulonglong2 *>(zo + 2 * kp), zv);
+    }
+}
+
+// The x / z broadcast of every job of a table: X and Z of each (row, qubit)
+// pair and shot-word := the shared bits.  Stores are streaming (evict
+// first): the broadcast passes 1.65 GB through L2 at d = 15 and must not
+// evict the tables of the kernels beside it.  At most 32 registers a
+// thread: two broadcast CTAs (16K registers) fit on an SM beside six noise
+// CTAs (48K) or two sign CTAs (40K).
+//
+// With a counter (ctr), warps take kBcastBatch chunks at a time from it, so
+// CTAs that reach their SMs late (beside the other kernels of the run) take
+// less of the work; the last CTA to finish puts the counter back to zero
+// for the next launch.  Without one, warp i takes chunks i, i + warps, ...
+// ONE: a table of one job (no job lookup).
+template <bool ONE>
 __global__ void __launch_bounds__(256, 8) broadcast_jobs_kernel(const BroadcastJobDev *__restrict__ jobs, int njobs,
                                                              const int64_t *__restrict__ chunk0, int64_t chunks,
                                                              unsigned long long *ctr) {
     const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const int64_t c0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (njobs == 1 && (jobs[0].w >> 1) >= 16 && ctr) {
-        // Warps take kBcastBatch chunks at a time from a counter, so CTAs
-        // that reach their SMs late (beside the other kernels of the run)
-        // take less of the work.  The last CTA to finish puts the counter
-        // back to zero for the next launch.
-        const BroadcastJobDev &B = jobs[0];
-        const int64_t hw = B.w >> 1, n = B.n;
+    if (ctr) {
         for (;;) {
             unsigned long long b = 0;
             if (lane == 0) b = atomicAdd(ctr, 1ull);
             const int64_t base = (int64_t)__shfl_sync(0xFFFFFFFFu, b, 0) * kBcastBatch;
             if (base >= chunks) break;
             const int64_t end = base + kBcastBatch < chunks ? base + kBcastBatch : chunks;
-            int64_t row = base / n, q = base - row * n;
-            for (int64_t c = base; c < end; ++c) {
-                const u64 xb = (B.xz[(row * 2 + 0) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-                const u64 zb = (B.xz[(row * 2 + 1) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-                const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
-                u64 *xo = B.X + c * B.w, *zo = B.Z + c * B.w;
-                for (int64_t kp = lane; kp < hw; kp += 32) {
-                    __stcs(reinterpret_cast<ulonglong2 *>(xo + 2 * kp), xv);
-                    __stcs(reinterpret_cast<ulonglong2 *>(zo + 2 * kp), zv);
-                }
-                if (++q == n) {
-                    q = 0;
-                    ++row;
+            int64_t c = base;
+            while (c < end) {  // the batch's chunks, job by job
+                const int j = ONE ? 0 : job_of(chunk0, njobs, c);
+                const BroadcastJobDev &B = jobs[j];
+                const int64_t first = ONE ? 0 : __ldg(chunk0 + j), last = ONE ? chunks : __ldg(chunk0 + j + 1);
+                const int64_t jend = end < last ? end : last;
+                if (jend <= c) break;  // (chunk0 increases: never taken)
+                if ((B.w >> 1) >= 16) {  // whole rows: step (row, qubit) without dividing
+                    const int hw = (int)(B.w >> 1), n = (int)B.n;
+                    const int64_t lc = c - first, row = lc / n, nw64 = B.nw64;
+                    int q = (int)(lc - row * n);
+                    const uint64_t *xr = B.xz + row * 2 * nw64;  // the row's x bits, then its z bits
+                    ulonglong2 *xo = reinterpret_cast<ulonglong2 *>(B.X + lc * B.w);
+                    ulonglong2 *zo = reinterpret_cast<ulonglong2 *>(B.Z + lc * B.w);
+                    for (; c < jend; ++c) {
+                        const u64 xb = (xr[q >> 6] >> (q & 63)) & 1ull, zb = (xr[nw64 + (q >> 6)] >> (q & 63)) & 1ull;
+                        const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb),
+                                         zv = make_ulonglong2(0ull - zb, 0ull - zb);
+                        for (int kp = lane; kp < hw; kp += 32) {
+                            __stcs(xo + kp, xv);
+                            __stcs(zo + kp, zv);
+                        }
+                        xo += hw;
+                        zo += hw;
+                        if (++q == n) {
+                            q = 0;
+                            xr += 2 * nw64;
+                        }
+                    }
+                } else {
+                    for (; c < jend; ++c) broadcast_chunk(B, c - first, lane);
                 }
             }
         }
@@ -534,31 +575,11 @@ __global__ void __launch_bounds__(256, 8) broadcast_jobs_kernel(const BroadcastJ
         }
         return;
     }
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t c0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     for (int64_t c = c0; c < chunks; c += warps) {
-        const int j = njobs > 1 ? job_of(chunk0, njobs, c) : 0;
-        const BroadcastJobDev &B = jobs[j];
-        const int64_t hw = B.w >> 1, pairs = (2 * B.n + 1) * B.n, local = c - chunk0[j];
-        int64_t rq, kp0, step;
-        if (hw >= 16) {
-            rq = local;
-            kp0 = lane;
-            step = 32;
-        } else {
-            const int per = 32 / (int)hw;
-            rq = local * per + lane / (int)hw;
-            kp0 = lane % (int)hw;
-            step = hw;
-            if (lane >= per * (int)hw || rq >= pairs) continue;
-        }
-        const int64_t row = rq / B.n, q = rq - row * B.n;
-        const u64 xb = (B.xz[(row * 2 + 0) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-        const u64 zb = (B.xz[(row * 2 + 1) * B.nw64 + (q >> 6)] >> (q & 63)) & 1ull;
-        const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb), zv = make_ulonglong2(0ull - zb, 0ull - zb);
-        u64 *xo = B.X + rq * B.w, *zo = B.Z + rq * B.w;
-        for (int64_t kp = kp0; kp < hw; kp += step) {
-            __stcs(reinterpret_cast<ulonglong2 *>(xo + 2 * kp), xv);
-            __stcs(reinterpret_cast<ulonglong2 *>(zo + 2 * kp), zv);
-        }
+        const int j = ONE ? 0 : job_of(chunk0, njobs, c);
+        broadcast_chunk(jobs[j], c - chunk0[j], lane);
     }
 }
 
@@ -676,7 +697,8 @@ int launch_broadcast_jobs(cudaStream_t st, const FrameTable &t, int ctas_per_sm)
         PS_CUDA(cudaDeviceGetAttribute(&g_frame_sms, cudaDevAttrMultiProcessorCount, dev));
     }
     {
-        const int rc = same_carveout((const void *)broadcast_jobs_kernel);
+        int rc = same_carveout((const void *)broadcast_jobs_kernel<true>);
+        if (rc == OK) rc = same_carveout((const void *)broadcast_jobs_kernel<false>);
         if (rc != OK) return rc;
     }
     int rc = prio_greatest();
@@ -696,7 +718,10 @@ int launch_broadcast_jobs(cudaStream_t st, const FrameTable &t, int ctas_per_sm)
     attr[0].val.priority = g_prio_greatest;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    PS_CUDA(cudaLaunchKernelEx(&cfg, broadcast_jobs_kernel, t.bjobs, (int)t.njobs, t.chunk0, t.chunks, t.bctr));
+    if (t.njobs == 1)
+        PS_CUDA(cudaLaunchKernelEx(&cfg, broadcast_jobs_kernel<true>, t.bjobs, (int)t.njobs, t.chunk0, t.chunks, t.bctr));
+    else
+        PS_CUDA(cudaLaunchKernelEx(&cfg, broadcast_jobs_kernel<false>, t.bjobs, (int)t.njobs, t.chunk0, t.chunks, t.bctr));
     PS_CUDA(cudaGetLastError());
     return OK;
 }

@@ -199,6 +199,21 @@ constexpr int64_t kBcastBatch = 8;
 int launch_noise_vectors(cudaStream_t st, const FrameTable &t);
 // Sign-kernel warps per CTA the launch uses (4 or 8; 0 = 8).
 int launch_frame_run(cudaStream_t st, const FrameTable &t, int warps);
+// ps_circuit.cpp: a run of every job of a table from |0...0> (run
+// parameters on the device already): the broadcast on `side` (forked from
+// st with `fork`, joined back with `join`) beside the noise vectors and the
+// sign program on st; side = nullptr runs the three in order on st.
+int frame_table_enqueue(const FrameTable &t, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                        int warps, int bctas);
+// The fastest (sign-kernel warps, broadcast CTAs per SM) for a table, by
+// timing each candidate's run; the tableaux and records are left holding
+// the timed runs' data.
+int frame_table_tune(const FrameTable &t, cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join,
+                     int *warps, int *bctas, double *best_ms);
+// A compiled circuit's entries for a batch's table (false: the circuit does
+// not run the shared-x/z plan).
+bool circuit_frame_job(const ps_circuit *c, FrameJobDev *job, BroadcastJobDev *bjob);
+
 // The x / z broadcast of every job; ctas_per_sm 0 = 1 (eight warps an SM
 // write at close to the copy rate and leave the noise and sign kernels
 // most of each SM and of the memory system).

@@ -187,6 +187,7 @@ namespace ps {
 int circuit_enqueue(ps_circuit *c, cudaStream_t st, bool reset);  // the plan, on any stream
 RunParams circuit_begin_run(ps_circuit *c, bool reset);           // host bookkeeping of one run
 RunParams *circuit_params_dev(ps_circuit *c);                     // device run parameters
+RunParams circuit_current_params(const ps_circuit *c);             // the next run's, without taking them
 ps_state *circuit_state(ps_circuit *c);
 // ps_state.cu: device bytes state_alloc takes.
 size_t state_bytes(int64_t n, int64_t S, bool signs_only = false);

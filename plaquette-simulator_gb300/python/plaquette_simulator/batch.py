@@ -74,7 +74,8 @@ class BatchOptions(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("num_jobs", C.c_uint64), ("shot_gates_per_run", C.c_uint64), ("tableau_bytes", C.c_uint64),
-                ("launches_per_run", C.c_uint64), ("compile_ms", C.c_double), ("tune_ms", C.c_double)]
+                ("launches_per_run", C.c_uint64), ("compile_ms", C.c_double), ("tune_ms", C.c_double),
+                ("table_jobs", C.c_uint64), ("frame_warps", C.c_int32), ("bcast_ctas", C.c_int32)]
 
 
 class Batch:

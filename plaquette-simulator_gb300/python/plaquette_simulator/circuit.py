@@ -37,7 +37,8 @@ class CircuitStats(C.Structure):
                 ("num_measure_phases", C.c_uint64), ("launches_per_run", C.c_uint64),
                 ("first_record", C.c_uint64), ("segment_bytes", C.c_double), ("seg_rows", C.c_int32),
                 ("seg_words", C.c_int32), ("seg_threads", C.c_int32), ("meas_words", C.c_int32),
-                ("resident_segments", C.c_int32), ("shared_xz", C.c_int32)]
+                ("resident_segments", C.c_int32), ("shared_xz", C.c_int32),
+                ("frame_warps", C.c_int32), ("bcast_ctas", C.c_int32), ("pad", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

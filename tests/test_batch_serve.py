@@ -88,6 +88,60 @@ def test_batch_jobs_match_alone(ps, autotune, graph):
     b.close()
 
 
+def _tableau(L, state, n, shots):
+    import ctypes as C
+    W = 2 * n + 1
+    x = np.empty((shots, W, n), dtype=np.int32)
+    z = np.empty_like(x)
+    r = np.empty((shots, W), dtype=np.int32)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    assert L.ps_device_to_host(state, p(x), p(z), p(r)) == 0
+    return x, z, r
+
+
+@pytest.mark.gpu
+def test_batch_table_beside_branch_jobs(ps):
+    """Jobs of the shared-x/z plan share one job table (three kernels for
+    all of them, knobs tuned on the table); a feed-forward job runs its
+    per-shot plan on a branch beside them.  Every job's records and final
+    tableau equal the job run alone."""
+    from plaquette_simulator import _lib
+    from plaquette_simulator.batch import Batch, Job
+    from plaquette_simulator import circuits as C
+    from plaquette_simulator.circuit import CompiledCircuit
+    ffc = C.Circuit(4)
+    ffc.h(0)
+    ffc.m(0)
+    ffc.s_if(1, 0)
+    ffc.h(1)
+    ffc.cx(1, 2)
+    ffc.pauli1(3, 0.1, 0.1, 0.1)
+    ffc.m(1)
+    ffc.m(2)
+    ffc.m(3)
+    jobs = _small_jobs()[:4] + [Job(ffc, 300, 77, 2, 0.1)]
+    b = Batch(jobs, autotune=True, graph=True)
+    assert b.stats["table_jobs"] == 4
+    assert b.stats["frame_warps"] in (4, 8) and b.stats["bcast_ctas"] in (1, 2)
+    b.run()
+    L = _lib.load()
+    for j, job in enumerate(jobs):
+        res, det = b.records(j)
+        st = ps.CliffordState(job.num_qubits, job.shots, job.seed, True)
+        cc = CompiledCircuit(job.circuit, st, fused=True, graph=True)
+        cc.run(reset=True)
+        nm = job.circuit.num_measurements()
+        w = ((job.shots + 63) // 64 + 1) & ~1
+        ares, adet = np.zeros((nm, w), np.uint64), np.zeros((nm, w), np.uint64)
+        cc.copy_records_words(ares, adet)
+        assert np.array_equal(res, ares) and np.array_equal(det, adet), f"job {j}"
+        _, state = b._job(j)
+        got = _tableau(L, state, job.num_qubits, job.shots)
+        for a, g in zip(st.device_to_host_numpy(), got):
+            assert np.array_equal(a, g), f"job {j}: tableau"
+    b.close()
+
+
 @pytest.mark.gpu
 def test_batch_job_matches_oracle(ps, O):
     from plaquette_simulator.batch import Batch

@@ -437,6 +437,23 @@ ps_status ps_get_device_tableau(const ps_state *h, void **x, void **z, void **r,
  * snapshotting a shot range of a large state.  Waits for the stream. */
 ps_status ps_copy_tableau_words(ps_state *h, uint64_t first_word, uint64_t nwords, uint64_t *x, uint64_t *z,
                                 uint64_t *r);
+/* The counterpart of ps_copy_tableau_words: loads packed words [first_word,
+ * first_word + nwords) of x, z ([2n+1][n][nwords]) and r ([2n+1][nwords])
+ * from host memory (any pointer may be NULL: that plane is kept).  With the
+ * event counter (ps_set_event_counter) it resumes a state snapshotted by
+ * ps_copy_tableau_words, shot range by shot range: the import path of
+ * HostToDevice (CliffordState.hpp:207-231) in the packed layout, without
+ * the int32 expansion.  Waits for the copy. */
+ps_status ps_load_tableau_words(ps_state *h, uint64_t first_word, uint64_t nwords, const uint64_t *x,
+                                const uint64_t *z, const uint64_t *r);
+/* DeviceToDevice (CliffordState.hpp:268-274): copies packed device planes of
+ * the same geometry (another state's ps_get_device_tableau, whose work must
+ * be finished) into h's tableau.  Waits for the copy. */
+ps_status ps_device_to_device(ps_state *h, const void *x, const void *z, const void *r);
+/* Device pointers of record `id` (packed words, ps_get_device_tableau's
+ * word count): the counterpart of Measurement::measurement_results_device /
+ * measurement_determined_device (CliffordState.hpp:36-37). */
+ps_status ps_get_record_device(ps_state *h, uint64_t id, void **results, void **determined);
 
 #ifdef __cplusplus
 }

@@ -484,8 +484,10 @@ ps_status ps_copy_tableau_words(ps_state *h, uint64_t first_word, uint64_t nword
                                 uint64_t *r) {
     ENTER();
     CHECK_HANDLE(h);
-    if (first_word + nwords > (uint64_t)h->w) return fail(E_RANGE, "word range outside the state");
+    if (nwords > (uint64_t)h->w || first_word > (uint64_t)h->w - nwords)
+        return fail(E_RANGE, "word range outside the state");
     if (nwords == 0 || h->n == 0) return OK;
+    if (h->signs_only && (x || z)) return fail(E_STATE, "a signs-only state holds no x / z");
     const size_t width = nwords * sizeof(u64), spitch = (size_t)h->w * sizeof(u64);
     const size_t rows = (size_t)h->W * (size_t)h->n;
     if (x) PS_CUDA(cudaMemcpy2DAsync(x, width, h->X + first_word, spitch, width, rows, cudaMemcpyDeviceToHost, h->stream));
@@ -494,6 +496,49 @@ ps_status ps_copy_tableau_words(ps_state *h, uint64_t first_word, uint64_t nword
         PS_CUDA(cudaMemcpy2DAsync(r, width, h->R + first_word, spitch, width, (size_t)h->W, cudaMemcpyDeviceToHost,
                                   h->stream));
     PS_CUDA(cudaStreamSynchronize(h->stream));
+    return OK;
+}
+
+ps_status ps_load_tableau_words(ps_state *h, uint64_t first_word, uint64_t nwords, const uint64_t *x,
+                                const uint64_t *z, const uint64_t *r) {
+    ENTER();
+    CHECK_HANDLE(h);
+    if (nwords > (uint64_t)h->w || first_word > (uint64_t)h->w - nwords)
+        return fail(E_RANGE, "word range outside the state");
+    if (h->signs_only) return fail(E_STATE, "a signs-only state holds no x / z");
+    if (nwords == 0 || h->n == 0) return OK;
+    h->valid = false;  // not known to come from |0...0> through gates and measurements
+    const size_t width = nwords * sizeof(u64), dpitch = (size_t)h->w * sizeof(u64);
+    const size_t rows = (size_t)h->W * (size_t)h->n;
+    if (x) PS_CUDA(cudaMemcpy2DAsync(h->X + first_word, dpitch, x, width, width, rows, cudaMemcpyHostToDevice, h->stream));
+    if (z) PS_CUDA(cudaMemcpy2DAsync(h->Z + first_word, dpitch, z, width, width, rows, cudaMemcpyHostToDevice, h->stream));
+    if (r)
+        PS_CUDA(cudaMemcpy2DAsync(h->R + first_word, dpitch, r, width, width, (size_t)h->W, cudaMemcpyHostToDevice,
+                                  h->stream));
+    PS_CUDA(cudaStreamSynchronize(h->stream));  // the host buffers may go once this returns
+    return OK;
+}
+
+ps_status ps_device_to_device(ps_state *h, const void *x, const void *z, const void *r) {
+    ENTER();
+    CHECK_HANDLE(h);
+    if (!x || !z || !r) return fail(E_ARG, "null device plane");
+    if (h->signs_only) return fail(E_STATE, "a signs-only state holds no x / z");
+    h->valid = false;
+    const size_t plane = (size_t)h->W * (size_t)(h->n > 0 ? h->n : 1) * (size_t)h->w * sizeof(u64);
+    PS_CUDA(cudaMemcpyAsync(h->X, x, plane, cudaMemcpyDeviceToDevice, h->stream));
+    PS_CUDA(cudaMemcpyAsync(h->Z, z, plane, cudaMemcpyDeviceToDevice, h->stream));
+    PS_CUDA(cudaMemcpyAsync(h->R, r, (size_t)h->W * (size_t)h->w * sizeof(u64), cudaMemcpyDeviceToDevice, h->stream));
+    PS_CUDA(cudaStreamSynchronize(h->stream));
+    return OK;
+}
+
+ps_status ps_get_record_device(ps_state *h, uint64_t id, void **results, void **determined) {
+    ENTER();
+    CHECK_HANDLE(h);
+    if (id >= h->recs.size()) return fail(E_RANGE, "Measurement id is out of range.");
+    if (results) *results = h->recs[(size_t)id].res;
+    if (determined) *determined = h->recs[(size_t)id].det;
     return OK;
 }
 

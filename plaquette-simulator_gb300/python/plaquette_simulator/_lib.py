@@ -93,6 +93,9 @@ _SIGS = {
     "ps_get_stream": (C.c_int, [_vp, _pp]),
     "ps_get_device_tableau": (C.c_int, [_vp, _pp, _pp, _pp, _pu64]),
     "ps_copy_tableau_words": (C.c_int, [_vp, _u64, _u64, _vp, _vp, _vp]),
+    "ps_load_tableau_words": (C.c_int, [_vp, _u64, _u64, _vp, _vp, _vp]),
+    "ps_device_to_device": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "ps_get_record_device": (C.c_int, [_vp, _u64, _pp, _pp]),
 }
 
 _lib = None

@@ -266,5 +266,42 @@ class CliffordState:
         check(self._L.ps_copy_tableau_words(self._h, first_word, nwords, _ptr(x), _ptr(z), _ptr(r)))
         return x, z, r
 
+    def load_tableau_words(self, first_word: int, x=None, z=None, r=None) -> None:
+        """Loads packed words starting at first_word (the layout tableau_words
+        returns; a plane left None is kept)."""
+        n, W = self.get_num_qubits(), 2 * self.get_num_qubits() + 1
+        planes = [None if a is None else np.ascontiguousarray(a, dtype=np.uint64) for a in (x, z, r)]
+        nwords = next((a.shape[-1] for a in planes if a is not None), 0)
+        for a, shape in zip(planes, ((W, n, nwords), (W, n, nwords), (W, nwords))):
+            if a is not None and a.shape != shape:
+                raise ValueError(f"packed plane of shape {a.shape}, expected {shape}")
+        check(self._L.ps_load_tableau_words(self._h, first_word, nwords,
+                                            *(None if a is None else _ptr(a) for a in planes)))
+
+    def snapshot(self) -> dict:
+        """Everything a later resume needs: the packed tableau of every shot
+        and the event counter (the draws continue from it)."""
+        x, z, r = self.tableau_words(0, self.words())
+        return {"num_qubits": self.get_num_qubits(), "batch_size": self.get_batch_size(),
+                "seed": self.get_seed(), "shot_offset": self.shot_offset(),
+                "events": self.event_counter(), "x": x, "z": z, "r": r}
+
+    @classmethod
+    def resume(cls, snap: dict) -> "CliffordState":
+        """A new state holding a snapshot (records are not part of it)."""
+        st = cls(snap["num_qubits"], snap["batch_size"], snap["seed"], True)
+        if snap.get("shot_offset", 0):
+            st.set_shot_offset(snap["shot_offset"])
+        st.load_tableau_words(0, snap["x"], snap["z"], snap["r"])
+        st.set_event_counter(snap["events"])
+        return st
+
+    def words(self) -> int:
+        """64-shot words per tableau column (the batch rounded up to an even
+        number of words)."""
+        w = C.c_uint64()
+        check(self._L.ps_get_device_tableau(self._h, None, None, None, C.byref(w)))
+        return w.value
+
     def synchronize(self) -> None:
         check(self._L.ps_synchronize(self._h))

@@ -402,6 +402,27 @@ ps_status ps_server_create(const ps_server_options *opts, ps_server **out);
 /* Copies the job description and queues it; never blocks on the device.
  * A job larger than the whole budget is refused with PS_E_NOMEM. */
 ps_status ps_server_submit(ps_server *s, const ps_job_desc *job, uint64_t *job_id);
+/* Park / resume of served jobs (no counterpart in the reference; its import
+ * path is HostToDevice, CliffordState.hpp:207-231).  A job submitted with a
+ * parked tableau -- x, z ([2n+1][n][words]) and r ([2n+1][words]) packed
+ * words of every shot, words = ceil(shots / 64) rounded up to even, as
+ * ps_copy_tableau_words gives them -- and event counter starts from them
+ * instead of |0...0> and runs its circuit without reset; with keep_tableau
+ * its final tableau and event counter are kept for ps_server_copy_tableau.
+ * A long job can so leave the device between its parts: each part is a job
+ * that resumes the last one's tableau, and the parts' records are those of
+ * the whole job run on one state. */
+typedef struct {
+    const uint64_t *x, *z, *r;  /* parked tableau (all NULL: start from |0...0>) */
+    uint64_t events;            /* its event counter                            */
+    int32_t keep_tableau;       /* 1: keep the final tableau for ps_server_copy_tableau */
+    int32_t pad;
+} ps_job_park;
+ps_status ps_server_submit_parked(ps_server *s, const ps_job_desc *job, const ps_job_park *park, uint64_t *job_id);
+/* The final tableau (the layout above) and event counter of a finished job
+ * submitted with keep_tableau (any pointer may be NULL). */
+ps_status ps_server_copy_tableau(ps_server *s, uint64_t job_id, uint64_t *x, uint64_t *z, uint64_t *r,
+                                 uint64_t *events);
 /* Waits up to timeout_s (< 0: no limit) for the job; PS_E_TIMEOUT if it is
  * not done by then. */
 ps_status ps_server_wait(ps_server *s, uint64_t job_id, double timeout_s, ps_job_result *out);

@@ -423,6 +423,7 @@ ps_status ps_batch_create(const ps_job_desc *jobs, uint64_t njobs, const ps_batc
 ps_status ps_batch_run(ps_batch *b) {
     ps_enter(__func__, __LINE__);
     if (!b) return fail(E_ARG, "null batch");
+    NvtxRange range("ps batch run");
     const int slot = b->ring_pos;
     b->ring_pos = (b->ring_pos + 1) % ps_batch::RING;
     PS_CUDA(cudaEventSynchronize(b->copied[slot]));  // the slot's previous copy has been read
@@ -515,6 +516,11 @@ struct SrvJob {
     uint64_t retry_after = UINT64_MAX;  // re-admit only after this many jobs finished
     bool signs_only = false;            // run on a signs-only state (records are all it returns)
     size_t full_bytes = 0;              // device bytes with per-shot tableaux
+    // park / resume: start from a parked tableau (packed words of every
+    // shot) and event counter instead of |0...0>; keep the final ones
+    bool resume = false, keep = false;
+    std::vector<uint64_t> in_x, in_z, in_r, out_x, out_z, out_r;
+    uint64_t in_events = 0, out_events = 0;
     bool done = false;
     int status = OK;
     std::string err;
@@ -572,11 +578,20 @@ constexpr int kNeedTableau = 1 << 20;
 // Runs one admitted job on the calling worker thread: state from the pool,
 // fused compile, one run from |0...0>, records to host, everything returned.
 int run_job(ps_server *s, SrvJob *j) {
+    NvtxRange range("ps served job " + std::to_string(j->id));
     ps_state *h = new ps_state;
     ps_circuit *c = nullptr;
     int rc = state_alloc(h, (int64_t)j->n, (int64_t)j->shots, j->seed, &s->pool, j->signs_only);
+    if (rc == OK && j->resume) {  // the parked tableau and event counter
+        const size_t plane = j->in_x.size() * sizeof(uint64_t), rb = j->in_r.size() * sizeof(uint64_t);
+        cudaError_t e = cudaMemcpyAsync(h->X, j->in_x.data(), plane, cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h->Z, j->in_z.data(), plane, cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h->R, j->in_r.data(), rb, cudaMemcpyHostToDevice, h->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "resume copy");
+        h->events = j->in_events;
+    }
     if (rc == OK) {
-        h->valid = true;
+        h->valid = !j->resume;
         ps_circuit_options co{};
         co.mode = PS_MODE_FUSED;
         co.use_graph = 0;
@@ -584,7 +599,7 @@ int run_job(ps_server *s, SrvJob *j) {
         if (rc == E_STATE && j->signs_only) rc = kNeedTableau;
     }
     if (rc == OK && s->opts.autotune) rc = ps_circuit_autotune(c, nullptr, nullptr);
-    if (rc == OK) rc = ps_circuit_run(c, 1);
+    if (rc == OK) rc = ps_circuit_run(c, j->resume ? 0 : 1);
     if (rc == OK) {
         ps_circuit_stats cs{};
         ps_circuit_get_stats(c, &cs);
@@ -594,6 +609,18 @@ int run_job(ps_server *s, SrvJob *j) {
         j->det.assign(j->nm * j->words, 0);
         uint64_t wds = 0;
         rc = ps_circuit_copy_records(c, j->res.data(), j->det.data(), &wds);
+    }
+    if (rc == OK && j->keep) {  // park: the final tableau and event counter to host memory
+        const size_t plane = (size_t)h->W * (size_t)h->n * (size_t)h->w, rw = (size_t)h->W * (size_t)h->w;
+        j->out_x.resize(plane);
+        j->out_z.resize(plane);
+        j->out_r.resize(rw);
+        cudaError_t e = cudaMemcpyAsync(j->out_x.data(), h->X, plane * 8, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(j->out_z.data(), h->Z, plane * 8, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(j->out_r.data(), h->R, rw * 8, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "park copy");
+        j->out_events = h->events;
     }
     if (rc != OK) j->err = ps_last_error();
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -642,6 +669,9 @@ void worker_main(ps_server *s) {
                 j->status = rc;
                 j->t_done = seconds_since(s->t0);
                 j->done = true;
+                std::vector<uint64_t>().swap(j->in_x);  // the parked input is no longer needed
+                std::vector<uint64_t>().swap(j->in_z);
+                std::vector<uint64_t>().swap(j->in_r);
                 s->finished++;
                 if (rc == OK) {
                     s->completed++;
@@ -696,16 +726,35 @@ ps_status ps_server_create(const ps_server_options *opts, ps_server **out) {
 }
 
 ps_status ps_server_submit(ps_server *s, const ps_job_desc *job, uint64_t *job_id) {
+    return ps_server_submit_parked(s, job, nullptr, job_id);
+}
+
+ps_status ps_server_submit_parked(ps_server *s, const ps_job_desc *job, const ps_job_park *park, uint64_t *job_id) {
     ps_enter(__func__, __LINE__);
     if (!s || !job) return fail(E_ARG, "null argument");
     TRY(check_job(*job, 0));
+    if (park && ((park->x != nullptr) != (park->z != nullptr) || (park->x != nullptr) != (park->r != nullptr)))
+        return fail(E_ARG, "a parked tableau needs x, z and r");
     auto j = std::make_unique<SrvJob>();
+    if (park) {
+        j->keep = park->keep_tableau != 0;
+        if (park->x) {
+            int64_t w = ((int64_t)job->shots + 63) / 64;
+            w = (w + 1) & ~int64_t(1);
+            const size_t W = 2 * (size_t)job->num_qubits + 1, plane = W * (size_t)job->num_qubits * (size_t)w;
+            j->resume = true;
+            j->in_x.assign(park->x, park->x + plane);
+            j->in_z.assign(park->z, park->z + plane);
+            j->in_r.assign(park->r, park->r + W * (size_t)w);
+            j->in_events = park->events;
+        }
+    }
     j->ops.assign(job->ops, job->ops + job->nops);
     if (job->params && job->nparams) j->params.assign(job->params, job->params + job->nparams);
     j->n = job->num_qubits;
     j->shots = job->shots;
     j->seed = job->seed;
-    j->signs_only = signs_only_job(*job);
+    j->signs_only = !j->resume && !j->keep && signs_only_job(*job);
     j->full_bytes = job_device_bytes(*job, false);
     j->bytes = job_device_bytes(*job, j->signs_only);
     j->shot_gates = count_gates(job->ops, job->nops) * job->shots;
@@ -765,6 +814,24 @@ ps_status ps_server_copy_records(ps_server *s, uint64_t job_id, uint64_t *result
     if (j->status != OK) return fail(j->status, "job failed: " + j->err);
     if (results) std::memcpy(results, j->res.data(), j->res.size() * sizeof(uint64_t));
     if (determined) std::memcpy(determined, j->det.data(), j->det.size() * sizeof(uint64_t));
+    return OK;
+}
+
+ps_status ps_server_copy_tableau(ps_server *s, uint64_t job_id, uint64_t *x, uint64_t *z, uint64_t *r,
+                                 uint64_t *events) {
+    ps_enter(__func__, __LINE__);
+    if (!s) return fail(E_ARG, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job_id);
+    if (it == s->jobs.end()) return fail(E_RANGE, "unknown job id");
+    SrvJob *j = it->second.get();
+    if (!j->done) return fail(E_STATE, "job not finished");
+    if (j->status != OK) return fail(j->status, "job failed: " + j->err);
+    if (!j->keep) return fail(E_STATE, "the job was not submitted to keep its tableau");
+    if (x) std::memcpy(x, j->out_x.data(), j->out_x.size() * sizeof(uint64_t));
+    if (z) std::memcpy(z, j->out_z.data(), j->out_z.size() * sizeof(uint64_t));
+    if (r) std::memcpy(r, j->out_r.data(), j->out_r.size() * sizeof(uint64_t));
+    if (events) *events = j->out_events;
     return OK;
 }
 

@@ -1029,20 +1029,40 @@ int enqueue_frame_table(const FrameTable &t, cudaStream_t st, cudaStream_t side,
         if (prof && rc == OK && prof->end() != OK) return E_CUDA;
         return rc;
     };
+    NvtxRange range("ps shared-x/z run (" + std::to_string(t.njobs) + " jobs)");
     if (prof || !side || t.chunks == 0) {
-        int rc = timed(P_SAMPLE, [&] { return launch_noise_vectors(st, t); });
-        if (rc == OK) rc = timed(P_FRAME, [&] { return launch_frame_run(st, t, warps); });
+        int rc = timed(P_SAMPLE, [&] {
+            NvtxRange r("ps noise vectors");
+            return launch_noise_vectors(st, t);
+        });
+        if (rc == OK) rc = timed(P_FRAME, [&] {
+            NvtxRange r("ps sign program");
+            return launch_frame_run(st, t, warps);
+        });
         if (rc != OK) return rc;
-        return timed(P_BROADCAST, [&] { return launch_broadcast_jobs(st, t, bctas); });
+        return timed(P_BROADCAST, [&] {
+            NvtxRange r("ps x/z broadcast");
+            return launch_broadcast_jobs(st, t, bctas);
+        });
     }
     // The broadcast runs beside the noise vectors and the sign program, at
     // the highest priority, so that its CTAs hold their SMs from the start.
     PS_CUDA(cudaEventRecord(fork, st));
     PS_CUDA(cudaStreamWaitEvent(side, fork, 0));
-    int rc = launch_broadcast_jobs(side, t, bctas);
-    if (rc == OK) rc = launch_noise_vectors(st, t);
+    int rc;
+    {
+        NvtxRange r("ps x/z broadcast");
+        rc = launch_broadcast_jobs(side, t, bctas);
+    }
+    if (rc == OK) {
+        NvtxRange r("ps noise vectors");
+        rc = launch_noise_vectors(st, t);
+    }
     if (rc != OK) return rc;
-    rc = launch_frame_run(st, t, warps);
+    {
+        NvtxRange r("ps sign program");
+        rc = launch_frame_run(st, t, warps);
+    }
     if (rc != OK) return rc;
     PS_CUDA(cudaEventRecord(join, side));
     PS_CUDA(cudaStreamWaitEvent(st, join, 0));
@@ -1846,6 +1866,7 @@ ps_status ps_circuit_run(ps_circuit *c, int reset_state) {
     if (!c) return fail(E_ARG, "null circuit");
     ps_state *h = c->h;
     if (h->signs_only && !reset_state) return fail(E_STATE, "a signs-only state runs only from |0...0>");
+    NvtxRange range("ps circuit run");
     const RunParams p = begin_run(c, reset_state != 0);
     set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base, p.word_base);
     PS_CUDA(cudaGetLastError());

@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ps_common.cuh"
 
 namespace ps {
@@ -106,6 +108,17 @@ struct ps_state {
 };
 
 namespace ps {
+// An NVTX range over a host scope (a run's enqueue, a launch kind, a served
+// job): named ranges on the timeline of Nsight tools, a few nanoseconds
+// when no tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    explicit NvtxRange(const std::string &name) { nvtxRangePushA(name.c_str()); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // ps_capi.cpp: records the entry point for error messages, clears the error.
 void ps_enter(const char *method, int line);
 

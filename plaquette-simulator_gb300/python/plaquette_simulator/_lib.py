@@ -81,6 +81,8 @@ _SIGS = {
     "ps_batch_destroy": (C.c_int, [_vp]),
     "ps_server_create": (C.c_int, [_vp, _pp]),
     "ps_server_submit": (C.c_int, [_vp, _vp, _pu64]),
+    "ps_server_submit_parked": (C.c_int, [_vp, _vp, _vp, _pu64]),
+    "ps_server_copy_tableau": (C.c_int, [_vp, _u64, _vp, _vp, _vp, _pu64]),
     "ps_server_wait": (C.c_int, [_vp, _u64, C.c_double, _vp]),
     "ps_server_copy_records": (C.c_int, [_vp, _u64, _vp, _vp]),
     "ps_server_release": (C.c_int, [_vp, _u64]),

@@ -166,6 +166,11 @@ class ServerStats(C.Structure):
                 ("first_submit_s", C.c_double), ("last_done_s", C.c_double)]
 
 
+class JobPark(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("z", C.c_void_p), ("r", C.c_void_p), ("events", C.c_uint64),
+                ("keep_tableau", C.c_int32), ("pad", C.c_int32)]
+
+
 class Server:
     def __init__(self, hbm_budget_bytes: int, max_active: int = 16, autotune: bool = False,
                  hol_wait_s: float = 1.0):
@@ -181,12 +186,40 @@ class Server:
         check(self._L.ps_server_now(self._h, C.byref(t)))
         return t.value
 
-    def submit(self, job: Job) -> int:
+    def submit(self, job: Job, parked: Optional[dict] = None, keep_tableau: bool = False) -> int:
+        """Queues a job.  parked: a tableau to start from instead of |0...0>
+        (what tableau() gives for an earlier job kept with keep_tableau): the
+        circuit then runs without reset and its draws continue from the
+        parked event counter."""
         descs, keep = _descs([job])
         jid = C.c_uint64()
-        check(self._L.ps_server_submit(self._h, descs, C.byref(jid)))
+        if parked is None and not keep_tableau:
+            check(self._L.ps_server_submit(self._h, descs, C.byref(jid)))
+        else:
+            park = JobPark(None, None, None, 0, int(bool(keep_tableau)), 0)
+            if parked is not None:
+                arrs = [np.ascontiguousarray(parked[k], dtype=np.uint64) for k in ("x", "z", "r")]
+                keep += arrs
+                park.x, park.z, park.r = (a.ctypes.data for a in arrs)
+                park.events = int(parked["events"])
+            check(self._L.ps_server_submit_parked(self._h, descs, C.byref(park), C.byref(jid)))
         self._jobs[jid.value] = job
         return jid.value
+
+    def tableau(self, job_id: int) -> dict:
+        """The final packed tableau (x, z [2n+1, n, words], r [2n+1, words]
+        uint64) and event counter of a job submitted with keep_tableau."""
+        self.wait(job_id)
+        job = self._jobs[job_id]
+        n, w = job.num_qubits, ((job.shots + 63) // 64 + 1) & ~1
+        x = np.zeros((2 * n + 1, n, w), np.uint64)
+        z = np.zeros_like(x)
+        r = np.zeros((2 * n + 1, w), np.uint64)
+        ev = C.c_uint64()
+        check(self._L.ps_server_copy_tableau(self._h, job_id, x.ctypes.data_as(C.c_void_p),
+                                             z.ctypes.data_as(C.c_void_p), r.ctypes.data_as(C.c_void_p),
+                                             C.byref(ev)))
+        return {"x": x, "z": z, "r": r, "events": ev.value}
 
     def wait(self, job_id: int, timeout_s: float = -1.0) -> dict:
         r = JobResult()

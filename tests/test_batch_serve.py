@@ -228,6 +228,42 @@ def test_server_signs_only_and_feed_forward_jobs(ps):
 
 
 @pytest.mark.gpu
+def test_server_park_and_resume(ps):
+    """A job served in two parts -- the first kept parked (its tableau and
+    event counter in host memory, its device memory freed), the second
+    resumed from it -- gives the second part's records, the final tableau
+    and event counter exactly as one state running both parts straight
+    through.  Feed-forward gates included, so both plans are crossed."""
+    from plaquette_simulator.batch import Job, Server
+    from plaquette_simulator.circuit import CompiledCircuit
+    from drivers import random_mixed_circuit
+    n, shots, seed = 10, 64 * 3 + 7, 4242
+    a = random_mixed_circuit(n, 250, seed=71)
+    b = random_mixed_circuit(n, 250, seed=72)
+    with Server(hbm_budget_bytes=1 << 30, max_active=2) as srv:
+        i1 = srv.submit(Job(a, shots, seed, 0, 0.0), keep_tableau=True)
+        parked = srv.tableau(i1)
+        srv.release(i1)
+        i2 = srv.submit(Job(b, shots, seed, 0, 0.0), parked=parked, keep_tableau=True)
+        res2, det2 = srv.records(i2)
+        final = srv.tableau(i2)
+        with pytest.raises(Exception):
+            srv.tableau(srv.submit(Job(a, shots, seed, 0, 0.0)))  # not kept
+    st = ps.CliffordState(n, shots, seed, True)
+    CompiledCircuit(a, st, fused=True).run(reset=True)
+    assert parked["events"] == st.event_counter()
+    cb = CompiledCircuit(b, st, fused=True)
+    cb.run(reset=False)
+    nm, w = b.num_measurements(), ((shots + 63) // 64 + 1) & ~1
+    rres, rdet = np.zeros((nm, w), np.uint64), np.zeros((nm, w), np.uint64)
+    cb.copy_records_words(rres, rdet)
+    assert np.array_equal(res2, rres) and np.array_equal(det2, rdet)
+    x, z, r = st.tableau_words(0, st.words())
+    assert np.array_equal(final["x"], x) and np.array_equal(final["z"], z) and np.array_equal(final["r"], r)
+    assert final["events"] == st.event_counter()
+
+
+@pytest.mark.gpu
 def test_server_d25_job_matches_oracle(ps, O):
     """The largest serving size (d=25, 1249 qubits): its schedule and tile
     must share one CTA's shared memory; one round, 64 shots, against the

@@ -547,9 +547,8 @@ __global__ void __launch_bounds__(256, 8) broadcast_jobs_kernel(const BroadcastJ
                     ulonglong2 *zo = reinterpret_cast<ulonglong2 *>(B.Z + lc * B.w);
                     // the shared bits of 64 qubits at a time: the stores of a
                     // chunk wait on no load
-                    u64 xw = __ldg(xr + (q >> 6)), zw = __ldg(xr + nw64 + (q >> 6));
                     for (; c < jend; ++c) {
-                        const u64 xb = (xw >> (q & 63)) & 1ull, zb = (zw >> (q & 63)) & 1ull;
+                        const u64 xb = (xr[q >> 6] >> (q & 63)) & 1ull, zb = (xr[nw64 + (q >> 6)] >> (q & 63)) & 1ull;
                         const ulonglong2 xv = make_ulonglong2(0ull - xb, 0ull - xb),
                                          zv = make_ulonglong2(0ull - zb, 0ull - zb);
                         for (int kp = lane; kp < hw; kp += 32) {
@@ -561,10 +560,6 @@ __global__ void __launch_bounds__(256, 8) broadcast_jobs_kernel(const BroadcastJ
                         if (++q == n) {
                             q = 0;
                             xr += 2 * nw64;
-                        }
-                        if ((q & 63) == 0 && c + 1 < jend) {
-                            xw = __ldg(xr + (q >> 6));
-                            zw = __ldg(xr + nw64 + (q >> 6));
                         }
                     }
                 } else {

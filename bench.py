@@ -60,6 +60,8 @@ def parse():
                     help="capacity leg: arrivals per second (the same job mix, well above the serving rate)")
     ap.add_argument("--capacity-seconds", type=float, default=10.0,
                     help="capacity leg: seconds of arrivals (0 = skip)")
+    ap.add_argument("--ff-blocks", type=int, default=90,
+                    help="feed-forward leg: distillation blocks side by side (5 qubits each; 0 = skip)")
     return ap.parse_args()
 
 
@@ -371,6 +373,73 @@ def serving_leg(args, rank, rate=None, seconds=None):
             "errors": {k: v[:4] for k, v in errors.items()}}
 
 
+def _stream_of(st, torch):
+    from plaquette_simulator import _lib
+    sp = ctypes.c_void_p()
+    _lib.check(_lib.load().ps_get_stream(st.handle, ctypes.byref(sp)))
+    return torch.cuda.ExternalStream(sp.value)
+
+
+def feed_forward_leg(args, shots, seed, torch, stream_of):
+    """Circuits with per-shot feed-forward (H / S conditioned on each shot's
+    own measurement: the reference's ApplyFlag gates) take the per-shot
+    plan.  Workload: the batched low-space S-state distillation protocol
+    (Test_CliffordState.hpp:675-741), --ff-blocks blocks of 5 qubits side by
+    side, every shot of the headline's shot count.  Each step starts from
+    |0...0>; the protocol's own check (data qubits 0..2 read 0, qubit 3
+    reads 1, all determined, in every shot) is verified on the last step."""
+    import numpy as np
+    from plaquette_simulator import CliffordState, circuits as C
+    from plaquette_simulator.circuit import CompiledCircuit
+    circ = C.distillation_blocks(args.ff_blocks)
+    flag = sum(1 for o in circ.ops if o[0] in (C.OP_H_IF, C.OP_S_IF))
+    gates = circ.num_gates() + flag
+    st = CliffordState(circ.num_qubits, shots, seed, True)
+    stream = stream_of(st, torch)
+    out = {"workload": f"S-state distillation, {args.ff_blocks} blocks of 5 qubits ({circ.num_qubits} qubits), "
+                       f"{shots} shots, per-shot plan (H_IF / S_IF feed-forward)",
+           "num_qubits": circ.num_qubits, "gates_per_shot": gates, "flag_gates_per_shot": flag,
+           "measurements": circ.num_measurements(), "unit": "shot-gates/s"}
+    for name, fused in (("fused", True), ("plain", False)):
+        cc = CompiledCircuit(circ, st, fused=fused, graph=True)
+        for _ in range(2 if fused else 1):
+            cc.run(reset=True)
+        k = max(1, min(args.steps, 5 if fused else 1))
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            cc.run(reset=True)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        out[name] = {"ms_per_step": ms, "value": gates * shots / (ms / 1e3), "steps": k,
+                     "shared_xz": int(cc.stats["shared_xz"])}
+        if fused:
+            nm = circ.num_measurements()
+            w = ((shots + 63) // 64 + 1) & ~1
+            res, det = np.zeros((nm, w), np.uint64), np.zeros((nm, w), np.uint64)
+            cc.copy_records_words(res, det)
+            b = args.ff_blocks
+            tail = slice(nm - 4 * b, nm)
+            full = np.uint64(0xFFFFFFFFFFFFFFFF)
+            last = shots % 64
+            mask = np.full(w, full, np.uint64)
+            mask[shots // 64:] = 0
+            if last:
+                mask[shots // 64] = np.uint64((1 << last) - 1)
+            want = np.zeros((4 * b, w), np.uint64)
+            want[3 * b:] = mask
+            out["protocol_holds"] = bool(np.array_equal(res[tail] & mask, want) and
+                                         np.array_equal(det[tail] & mask, np.broadcast_to(mask, det[tail].shape)))
+            out["value"] = out["fused"]["value"]
+        del cc
+    out["speedup_vs_plain"] = out["plain"]["ms_per_step"] / out["fused"]["ms_per_step"]
+    del st
+    torch.cuda.synchronize()
+    return out
+
+
 def compile_leg(circ, shots, first_shot, seed, gates, world, torch):
     """The host work the timed steps leave out.  compile_ms: ps_circuit_compile
     of the workload on a fresh state, with the compile cache cleared (cold)
@@ -619,6 +688,8 @@ def main():
 
     del fused, st
     torch.cuda.synchronize()
+    if args.ff_blocks > 0 and world == 1:
+        line["feed_forward"] = feed_forward_leg(args, shots, seed, torch, stream_of=_stream_of)
     if args.batch_jobs > 0:
         line["batch"] = batch_leg(args, rank, torch)
     if args.serve_seconds > 0:

@@ -293,11 +293,14 @@ ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *de
 ps_status ps_circuit_detectors(ps_circuit *c, const uint32_t *idx, const uint64_t *off, uint64_t ndet,
                                uint64_t *out);
 
-/* The project's autotuner (no counterpart in the reference): times the
- * fused-segment tile shapes (rows x shot-words x threads) on the circuit's
- * first segment and the measurement kernel's shot-words per CTA on its first
- * measurement phase, on the circuit's own state, and keeps the fastest
- * (re-capturing the CUDA graphs).  The tableau and records are left holding
+/* The project's autotuner (no counterpart in the reference): for a circuit
+ * with the shared-x/z plan, times its runs over the sign-kernel warps (4, 8)
+ * and broadcast CTAs per SM (1, 2); for the per-shot plan (when the
+ * circuit's runs take it, or it is built already) times the fused-segment
+ * tile shapes (rows x shot-words x threads) on the circuit's first segment
+ * and the measurement kernel's shot-words per CTA on its first measurement
+ * phase; all on the circuit's own state, keeping the fastest (re-capturing
+ * the CUDA graphs).  The tableau and records are left holding
  * valid but meaningless data (runs with reset_state = 1 start over); the
  * event counter is not advanced.  Results are cached per process by
  * (qubits, shot-words, touched qubits), so circuits of one shape are timed

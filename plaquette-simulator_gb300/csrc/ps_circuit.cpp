@@ -189,6 +189,11 @@ struct ps_circuit {
     // has no per-shot conditional gates.
     bool frame_ok = false;
     bool force_per_shot = false;    // measurement statistics need the per-shot plan
+    // The per-shot plan's device schedules (ensure_segments_dev): -1 not
+    // built yet, else the status of the one attempt.
+    int seg_dev_status = -1;
+    bool seg_dev_ready = false;
+    size_t max_slots = 0;           // channels of the largest segment
     FrameProgram fprog;
     FrameOp *d_fops = nullptr;
     uint32_t *d_ftab = nullptr;
@@ -810,6 +815,92 @@ struct Profiler {
 enum ProfKind { P_INIT = 0, P_SAMPLE = 1, P_SEGMENT = 2, P_MEASURE = 3, P_GATE = 4, P_CHANNEL = 5, P_FRAME = 6, P_BROADCAST = 7 };
 
 // Enqueues plan steps [from, to) on `st`.
+// The per-shot plan's device schedules and channel scratch: built on first
+// use -- a run without reset, measurement statistics, the tile tuner, or at
+// compile time when the shared-x/z plan does not apply -- so circuits that
+// only run from |0...0> in the shared-x/z plan never upload them.  Not
+// during stream capture (it uploads with synchronous copies).
+int build_segments_dev(ps_circuit *c);
+int ensure_segments_dev(ps_circuit *c) {
+    if (c->seg_dev_ready || c->opts.mode != PS_MODE_FUSED) return OK;
+    if (c->h->signs_only) return fail(E_STATE, "a signs-only state runs only the shared-x/z plan");
+    if (c->seg_dev_status >= 0)
+        return fail(c->seg_dev_status, "the per-shot plan of this circuit does not fit its kernels");
+    c->seg_dev_status = build_segments_dev(c);
+    c->seg_dev_ready = c->seg_dev_status == OK;
+    return c->seg_dev_status;
+}
+
+int build_segments_dev(ps_circuit *c) {
+    ps_state *h = c->h;
+    c->entry_cap = (int32_t)std::max<size_t>(1, c->max_slots);
+    void *p = nullptr;
+    if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * sizeof(NoiseEntry)) != OK)
+        return fail(E_NOMEM, "device allocation of channel entries failed");
+    c->owned.push_back(p);
+    c->d_entries = (NoiseEntry *)p;
+    if (dev_alloc(h, &p, (size_t)h->w * sizeof(int32_t)) != OK) return E_NOMEM;
+    c->owned.push_back(p);
+    c->d_entry_count = (int32_t *)p;
+    if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * 4 * sizeof(u64)) != OK)
+        return fail(E_NOMEM, "device allocation of channel sampling scratch failed");
+    c->owned.push_back(p);
+    c->d_dense = (u64 *)p;
+    for (SegHost &sg : c->segs) {
+        SegmentDev d{};
+        SegLayer *dl;
+        SegRun *drn;
+        SegGate *dg;
+        SegSign *ds;
+        int32_t *dc;
+        NoiseSlot *dsl;
+        int32_t *drr;
+        if (upload(h, c->owned, sg.layers, &dl) || upload(h, c->owned, sg.runs, &drn) || upload(h, c->owned, sg.gates, &dg) ||
+            upload(h, c->owned, sg.signs, &ds) ||
+            upload(h, c->owned, sg.cols, &dc) || upload(h, c->owned, sg.slots, &dsl) ||
+            upload(h, c->owned, sg.recsig_rec, &drr))
+            return E_CUDA;
+        d.recsig_rec = drr;
+        d.nrecsig = (int32_t)sg.recsig_rec.size();
+        d.word_vector = c->opts.seg_resident == 2 ? 1 : 0;
+        if (sg.res_slots > 0) {
+            uint16_t *drc;
+            ResOp *dro;
+            uint32_t *dpd, *dps;
+            if (upload(h, c->owned, sg.res_cols, &drc) || upload(h, c->owned, sg.res_ops, &dro) ||
+                upload(h, c->owned, sg.prop_desc, &dpd) || upload(h, c->owned, sg.prop_sup, &dps))
+                return E_CUDA;
+            d.res_slots = sg.res_slots;
+            d.res_cols = drc;
+            d.res_ops = dro;
+            d.prop_desc = dpd;
+            d.prop_sup = dps;
+        }
+        d.layers = dl;
+        d.nlayers = (int32_t)sg.layers.size();
+        d.runs = drn;
+        d.nruns = (int32_t)sg.runs.size();
+        d.gates = dg;
+        d.signs = ds;
+        d.cols = dc;
+        d.nq = (int32_t)sg.cols.size();
+        d.ngates = (int32_t)sg.gates.size();
+        d.nsigns = (int32_t)sg.signs.size();
+        d.slots = dsl;
+        d.nslots = (int32_t)sg.slots.size();
+        d.thr = c->d_thr;
+        d.entries = sg.slots.empty() ? nullptr : c->d_entries;
+        d.entry_count = c->d_entry_count;
+        d.cap = c->entry_cap;
+        d.dense = c->d_dense;
+        sg.dev = d;
+        if (segment_launch_smem(d.nlayers, d.nruns, d.ngates, d.nsigns, d.nq, d.nrecsig, c->opts.seg_rows,
+                                c->opts.seg_words, d.res_slots) > kSegSmemMax)
+            return fail(E_ARG, "segment schedule and tile do not fit in shared memory");
+    }
+    return OK;
+}
+
 int enqueue_steps(ps_circuit *c, cudaStream_t st, size_t from, size_t to, Profiler *prof = nullptr) {
     ps_state *h = c->h;
     auto timed = [&](int kind, auto &&launch) -> int {
@@ -1109,6 +1200,10 @@ int tune_frame_table(const FrameTable &t, cudaStream_t st, cudaStream_t side, cu
 
 int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nullptr) {
     if (reset && c->frame_ok && !c->force_per_shot) return enqueue_frame(c, st, prof);
+    {
+        int rc = ensure_segments_dev(c);  // (captures call it before they begin)
+        if (rc != OK) return rc;
+    }
     if (reset) {
         if (prof && prof->begin(P_INIT) != OK) return E_CUDA;
         int rc = launch_init_zero_on(st, c->h);
@@ -1118,7 +1213,37 @@ int enqueue_plan(ps_circuit *c, cudaStream_t st, bool reset, Profiler *prof = nu
     return enqueue_steps(c, st, 0, c->steps.size(), prof);
 }
 
-// Captures the plan into the two CUDA graphs (without / with the reset).
+// Captures the plan of runs without (reset = 0) or with the reset into its
+// CUDA graph, replacing an earlier one.
+int capture_graph(ps_circuit *c, int reset) {
+    if (c->exec[reset]) cudaGraphExecDestroy(c->exec[reset]);
+    if (c->graph[reset]) cudaGraphDestroy(c->graph[reset]);
+    c->exec[reset] = nullptr;
+    c->graph[reset] = nullptr;
+    cudaStream_t cs;
+    PS_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    int rc = e == cudaSuccess ? enqueue_plan(c, cs, reset != 0) : cuda_fail(e, "cudaStreamBeginCapture");
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (rc != OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    c->graph[reset] = g;
+    // node priorities kept: the broadcast's CTAs go first
+    e = cudaGraphInstantiateWithFlags(&c->exec[reset], g, cudaGraphInstantiateFlagUseNodePriority);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    return OK;
+}
+
+// Captures both graphs.  Without reset, a circuit with the shared-x/z plan
+// runs its per-shot plan, which is built and captured at the first such run
+// (unless it is built already).  A register the per-shot kernels cannot take
+// (more qubits than the measurement kernel holds) still runs from |0...0> in
+// the shared-x/z plan; a run without reset reports the error.
 int capture_graphs(ps_circuit *c) {
     for (int reset = 0; reset < 2; ++reset) {
         if (c->exec[reset]) cudaGraphExecDestroy(c->exec[reset]);
@@ -1126,26 +1251,19 @@ int capture_graphs(ps_circuit *c) {
         c->exec[reset] = nullptr;
         c->graph[reset] = nullptr;
         if (reset == 0 && c->h->signs_only) continue;  // runs only from |0...0>
-        cudaStream_t cs;
-        PS_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        int rc = e == cudaSuccess ? enqueue_plan(c, cs, reset != 0) : cuda_fail(e, "cudaStreamBeginCapture");
-        cudaGraph_t g = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(cs, &g);
-        cudaStreamDestroy(cs);
+        if (reset == 0 && c->frame_ok && !c->seg_dev_ready) continue;
+        if (reset == 0 || !c->frame_ok) {
+            int rc = ensure_segments_dev(c);  // (uploads: not inside the capture)
+            if (rc != OK) {
+                if (reset == 0 && c->frame_ok && rc == E_ARG) continue;
+                return rc;
+            }
+        }
+        int rc = capture_graph(c, reset);
         if (rc != OK) {
-            if (g) cudaGraphDestroy(g);
-            // A register the per-shot kernels cannot take (more qubits than
-            // the measurement kernel holds) still runs from |0...0> in the
-            // shared-x/z plan; a run without reset reports the error.
             if (reset == 0 && c->frame_ok && rc == E_ARG) continue;
             return rc;
         }
-        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-        c->graph[reset] = g;
-        // node priorities kept: the broadcast's CTAs go first
-        e = cudaGraphInstantiateWithFlags(&c->exec[reset], g, cudaGraphInstantiateFlagUseNodePriority);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     }
     return OK;
 }
@@ -1560,75 +1678,11 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         if (upload(h, c->owned, psurv, &c->d_psurv) != OK) return bail(E_CUDA);
     }
     pick_tile(c);
-    if (fused && !h->signs_only) {  // per-shot channel scratch (a signs-only state never runs that plan)
-        c->entry_cap = (int32_t)std::max<size_t>(1, max_slots);
-        void *p = nullptr;
-        if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * sizeof(NoiseEntry)) != OK)
-            return bail(fail(E_NOMEM, "device allocation of channel entries failed"));
-        c->owned.push_back(p);
-        c->d_entries = (NoiseEntry *)p;
-        if (dev_alloc(h, &p, (size_t)h->w * sizeof(int32_t)) != OK) return bail(E_NOMEM);
-        c->owned.push_back(p);
-        c->d_entry_count = (int32_t *)p;
-        if (dev_alloc(h, &p, (size_t)c->entry_cap * h->w * 4 * sizeof(u64)) != OK)
-            return bail(fail(E_NOMEM, "device allocation of channel sampling scratch failed"));
-        c->owned.push_back(p);
-        c->d_dense = (u64 *)p;
-        for (SegHost &sg : c->segs) {
-            SegmentDev d{};
-            SegLayer *dl;
-            SegRun *drn;
-            SegGate *dg;
-            SegSign *ds;
-            int32_t *dc;
-            NoiseSlot *dsl;
-            int32_t *drr;
-            if (upload(h, c->owned, sg.layers, &dl) || upload(h, c->owned, sg.runs, &drn) || upload(h, c->owned, sg.gates, &dg) ||
-                upload(h, c->owned, sg.signs, &ds) ||
-                upload(h, c->owned, sg.cols, &dc) || upload(h, c->owned, sg.slots, &dsl) ||
-                upload(h, c->owned, sg.recsig_rec, &drr))
-                return bail(E_CUDA);
-            d.recsig_rec = drr;
-            d.nrecsig = (int32_t)sg.recsig_rec.size();
-            d.word_vector = c->opts.seg_resident == 2 ? 1 : 0;
-            if (sg.res_slots > 0) {
-                uint16_t *drc;
-                ResOp *dro;
-                uint32_t *dpd, *dps;
-                if (upload(h, c->owned, sg.res_cols, &drc) || upload(h, c->owned, sg.res_ops, &dro) ||
-                    upload(h, c->owned, sg.prop_desc, &dpd) || upload(h, c->owned, sg.prop_sup, &dps))
-                    return bail(E_CUDA);
-                d.res_slots = sg.res_slots;
-                d.res_cols = drc;
-                d.res_ops = dro;
-                d.prop_desc = dpd;
-                d.prop_sup = dps;
-            }
-            d.layers = dl;
-            d.nlayers = (int32_t)sg.layers.size();
-            d.runs = drn;
-            d.nruns = (int32_t)sg.runs.size();
-            d.gates = dg;
-            d.signs = ds;
-            d.cols = dc;
-            d.nq = (int32_t)sg.cols.size();
-            d.ngates = (int32_t)sg.gates.size();
-            d.nsigns = (int32_t)sg.signs.size();
-            d.slots = dsl;
-            d.nslots = (int32_t)sg.slots.size();
-            d.thr = c->d_thr;
-            d.entries = sg.slots.empty() ? nullptr : c->d_entries;
-            d.entry_count = c->d_entry_count;
-            d.cap = c->entry_cap;
-            d.dense = c->d_dense;
-            sg.dev = d;
-            const double W = (double)h->W, B8 = (double)h->S / 8.0;
-            c->stats.segment_bytes += 2.0 * (2.0 * (double)sg.cols.size() + 1.0) * W * B8;
-            if (segment_launch_smem(d.nlayers, d.nruns, d.ngates, d.nsigns, d.nq, d.nrecsig, c->opts.seg_rows,
-                                    c->opts.seg_words, d.res_slots) > kSegSmemMax)
-                return bail(fail(E_ARG, "segment schedule and tile do not fit in shared memory"));
-        }
+    for (const SegHost &sg : c->segs) {  // algorithmic bytes of the per-shot segments (host data)
+        const double W = (double)h->W, B8 = (double)h->S / 8.0;
+        c->stats.segment_bytes += 2.0 * (2.0 * (double)sg.cols.size() + 1.0) * W * B8;
     }
+    c->max_slots = max_slots;
     if (upload(h, c->owned, c->meas, &c->d_meas) != OK) return bail(E_CUDA);
 
     // ---- shared-x/z plan of runs from |0...0> (no per-shot conditional gates)
@@ -1763,6 +1817,10 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     }
     if (h->signs_only && !c->frame_ok)
         return bail(fail(E_STATE, "the circuit needs per-shot tableaux, which a signs-only state does not hold"));
+    if (fused && !c->frame_ok) {  // every run takes the per-shot plan
+        int rc = ensure_segments_dev(c);
+        if (rc != OK) return bail(rc);
+    }
 
     // ---- stats
     ps_circuit_stats &st = c->stats;
@@ -1870,6 +1928,13 @@ ps_status ps_circuit_run(ps_circuit *c, int reset_state) {
     const RunParams p = begin_run(c, reset_state != 0);
     set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base, p.word_base);
     PS_CUDA(cudaGetLastError());
+    if (!reset_state && c->opts.use_graph && !c->exec[0] && c->frame_ok && !h->signs_only &&
+        c->seg_dev_status < 0) {
+        // the first run without reset of a shared-x/z circuit: build and capture its per-shot plan
+        int rc = ensure_segments_dev(c);
+        if (rc == OK) rc = capture_graph(c, 0);
+        if (rc != OK) return rc;
+    }
     if (c->exec[reset_state ? 1 : 0]) {
         PS_CUDA(cudaGraphLaunch(c->exec[reset_state ? 1 : 0], h->stream));
         return OK;
@@ -1952,7 +2017,11 @@ ps_status ps_circuit_autotune(ps_circuit *c, ps_circuit_options *chosen, double 
     ps_enter(__func__, __LINE__);
     if (!c) return fail(E_ARG, "null circuit");
     if (tune_ms) *tune_ms = 0.0;
-    if (c->opts.mode == PS_MODE_FUSED && c->frame_ok) {  // the shared-x/z kernels that runs from |0...0> use
+    if (c->opts.mode != PS_MODE_FUSED) {
+        if (chosen) *chosen = c->opts;
+        return OK;
+    }
+    if (c->frame_ok) {  // the shared-x/z kernels that runs from |0...0> use
         double ms = 0.0;
         int rc = autotune_frame(c, &ms);
         if (rc != OK) return rc;
@@ -1960,17 +2029,20 @@ ps_status ps_circuit_autotune(ps_circuit *c, ps_circuit_options *chosen, double 
         c->stats.frame_warps = c->opts.frame_warps;
         c->stats.bcast_ctas = c->opts.bcast_ctas;
     }
-    if (c->opts.mode == PS_MODE_FUSED && !c->h->signs_only) {  // the per-shot plan's tiles
-        int rc = autotune(c, tune_ms);
+    // the per-shot plan's tiles, when its runs take that plan (or it is built already)
+    if (!c->h->signs_only && (!c->frame_ok || c->seg_dev_ready)) {
+        double ms = 0.0;
+        int rc = autotune(c, &ms);
         if (rc != OK) return rc;
+        if (tune_ms) *tune_ms += ms;
         c->stats.seg_rows = c->opts.seg_rows;
         c->stats.seg_words = c->opts.seg_words;
         c->stats.seg_threads = c->opts.seg_threads;
         c->stats.meas_words = c->opts.meas_words;
-        if (c->opts.use_graph) {
-            rc = capture_graphs(c);
-            if (rc != OK) return rc;
-        }
+    }
+    if (c->opts.use_graph) {
+        int rc = capture_graphs(c);
+        if (rc != OK) return rc;
     }
     if (chosen) *chosen = c->opts;
     return OK;

@@ -406,3 +406,51 @@ def layered_circuit(width: int, depth: int, seed: int) -> Circuit:
         for q in range(width):
             c.m(q)
     return c
+
+
+# The seven phasors of the low-space S-state distillation protocol
+# (Test_CliffordState.hpp:675-741), over the block's data qubits 0..3.
+DISTILLATION_PHASORS = ((0,), (1,), (2,), (0, 1, 2), (0, 1, 3), (0, 2, 3), (1, 2, 3))
+
+
+def distillation_blocks(blocks: int) -> Circuit:
+    """`blocks` independent copies of the batched low-space S-state
+    distillation protocol (Test_CliffordState.hpp:675-741) side by side:
+    block b holds data qubits 5b..5b+3 and ancilla 5b+4.  For each phasor
+    every block entangles its ancilla with the phasor's data qubits, rotates
+    and measures it, then undoes the rotation on every qubit involved with
+    H / S gates conditioned on that measurement (H_IF, S_IF: per-shot
+    feed-forward, so the circuit runs the per-shot plan).  The blocks step
+    through the phasors together, so each phasor's measurements form one
+    measurement phase.  Afterwards data qubits 0..2 of every block measure
+    0 and qubit 3 (after S, H) measures 1, all determined, in every shot."""
+    c = Circuit(5 * blocks)
+    nrec = 0
+    for phasor in DISTILLATION_PHASORS:
+        for b in range(blocks):
+            a = 5 * b + 4
+            c.h(a)
+            for k in phasor:
+                c.cx(a, 5 * b + k)
+            c.h(a)
+            c.s(a)
+            c.h(a)
+        for b in range(blocks):
+            c.m(5 * b + 4)
+        for b in range(blocks):
+            rec = nrec + b
+            for q in [5 * b + k for k in phasor] + [5 * b + 4]:
+                c.h_if(q, rec)
+                c.s_if(q, rec)
+                c.s_if(q, rec)
+                c.h_if(q, rec)
+        nrec += blocks
+    for b in range(blocks):
+        for k in range(3):
+            c.m(5 * b + k)
+    for b in range(blocks):
+        c.s(5 * b + 3)
+        c.h(5 * b + 3)
+    for b in range(blocks):
+        c.m(5 * b + 3)
+    return c

@@ -283,6 +283,20 @@ ps_status ps_circuit_measure_stats(ps_circuit *c, int reset_state, int32_t *rand
  * host memory: num_measurements rows of `words` uint64 each (bit s of word
  * k = shot 64k+s).  Either pointer may be NULL.  Waits for the stream. */
 ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *determined, uint64_t *words);
+/* Pipelined sampling (no counterpart in the reference): enqueues the copy of
+ * the records of c's latest run to host memory on copy_stream (a
+ * cudaStream_t as void*; NULL = a stream of the circuit's own) after that
+ * run, and returns at once.  The next ps_circuit_run of c waits on the
+ * device for the copy to finish reading (it rewrites the same records);
+ * runs of other circuits on the same state do not.  Two compiled copies of
+ * one circuit on one state, run in turn, so send the records of one run
+ * while the next one computes, every run drawing fresh outcomes exactly as
+ * consecutive runs of one circuit do.  results / determined (pinned memory
+ * for a truly asynchronous copy) must stay valid until ps_circuit_wait_records. */
+ps_status ps_circuit_copy_records_async(ps_circuit *c, uint64_t *results, uint64_t *determined, void *copy_stream);
+/* Waits for that copy; PS_E_TIMEOUT when the run's sign program gave up on a
+ * bounded wait (its records are void). */
+ps_status ps_circuit_wait_records(ps_circuit *c);
 /* Detectors and observables, computed on the device from the last run's
  * records (no counterpart in the reference, whose callers read records one
  * shot at a time with GetMeasurement): output row d is the XOR of the

@@ -207,6 +207,13 @@ struct ps_circuit {
     BroadcastJobDev fbjob{};
     cudaStream_t fstream = nullptr;  // the broadcast's side stream
     cudaEvent_t fev[2] = {nullptr, nullptr};
+    // ps_circuit_copy_records_async: the copy stream (own or the caller's),
+    // the end of the run it copies, the end of the copy, and the error word
+    // in pinned host memory.
+    cudaStream_t cstream_own = nullptr;
+    cudaEvent_t ev_ran = nullptr, ev_copied = nullptr;
+    bool copy_pending = false;
+    int32_t *h_err = nullptr;
     cudaGraph_t graph[2] = {nullptr, nullptr};      // [reset_state]
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
 };
@@ -1925,6 +1932,7 @@ ps_status ps_circuit_run(ps_circuit *c, int reset_state) {
     ps_state *h = c->h;
     if (h->signs_only && !reset_state) return fail(E_STATE, "a signs-only state runs only from |0...0>");
     NvtxRange range("ps circuit run");
+    if (c->copy_pending) PS_CUDA(cudaStreamWaitEvent(h->stream, c->ev_copied, 0));  // it rewrites those records
     const RunParams p = begin_run(c, reset_state != 0);
     set_params_kernel<<<1, 1, 0, h->stream>>>(c->d_params, p.seed, p.event_base, p.word_base);
     PS_CUDA(cudaGetLastError());
@@ -2010,6 +2018,42 @@ ps_status ps_circuit_copy_records(ps_circuit *c, uint64_t *results, uint64_t *de
     if (c->d_ferr) PS_CUDA(cudaMemcpyAsync(&err, c->d_ferr, sizeof err, cudaMemcpyDeviceToHost, h->stream));
     PS_CUDA(cudaStreamSynchronize(h->stream));
     if (err) return fail(E_TIMEOUT, "a copy of the sign program did not arrive in time; the run's records are void");
+    return OK;
+}
+
+ps_status ps_circuit_copy_records_async(ps_circuit *c, uint64_t *results, uint64_t *determined, void *copy_stream) {
+    ps_enter(__func__, __LINE__);
+    if (!c) return fail(E_ARG, "null circuit");
+    ps_state *h = c->h;
+    if (!c->ev_ran) {
+        PS_CUDA(cudaEventCreateWithFlags(&c->ev_ran, cudaEventDisableTiming));
+        PS_CUDA(cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming));
+        PS_CUDA(cudaMallocHost(&c->h_err, sizeof(int32_t)));
+    }
+    cudaStream_t cs = static_cast<cudaStream_t>(copy_stream);
+    if (!cs) {
+        if (!c->cstream_own) PS_CUDA(cudaStreamCreateWithFlags(&c->cstream_own, cudaStreamNonBlocking));
+        cs = c->cstream_own;
+    }
+    const size_t bytes = c->rec_ids.size() * (size_t)h->w * sizeof(u64);
+    *c->h_err = 0;
+    PS_CUDA(cudaEventRecord(c->ev_ran, h->stream));
+    PS_CUDA(cudaStreamWaitEvent(cs, c->ev_ran, 0));
+    if (results && bytes) PS_CUDA(cudaMemcpyAsync(results, c->d_res_block, bytes, cudaMemcpyDeviceToHost, cs));
+    if (determined && bytes) PS_CUDA(cudaMemcpyAsync(determined, c->d_det_block, bytes, cudaMemcpyDeviceToHost, cs));
+    if (c->d_ferr) PS_CUDA(cudaMemcpyAsync(c->h_err, c->d_ferr, sizeof(int32_t), cudaMemcpyDeviceToHost, cs));
+    PS_CUDA(cudaEventRecord(c->ev_copied, cs));
+    c->copy_pending = true;
+    return OK;
+}
+
+ps_status ps_circuit_wait_records(ps_circuit *c) {
+    ps_enter(__func__, __LINE__);
+    if (!c) return fail(E_ARG, "null circuit");
+    if (!c->copy_pending) return OK;
+    PS_CUDA(cudaEventSynchronize(c->ev_copied));
+    c->copy_pending = false;
+    if (*c->h_err) return fail(E_TIMEOUT, "a copy of the sign program did not arrive in time; the run's records are void");
     return OK;
 }
 
@@ -2116,6 +2160,11 @@ ps_status ps_circuit_destroy(ps_circuit *c) {
     }
     for (cudaEvent_t e : c->fev)
         if (e) cudaEventDestroy(e);
+    if (c->ev_copied) cudaEventSynchronize(c->ev_copied);
+    if (c->cstream_own) cudaStreamDestroy(c->cstream_own);
+    if (c->ev_ran) cudaEventDestroy(c->ev_ran);
+    if (c->ev_copied) cudaEventDestroy(c->ev_copied);
+    if (c->h_err) cudaFreeHost(c->h_err);
     for (void *p : c->owned) dev_free(c->h, p);
     dev_free(c->h, c->d_forced);
     delete c;

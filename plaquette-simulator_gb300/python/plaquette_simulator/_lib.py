@@ -69,6 +69,8 @@ _SIGS = {
     "ps_circuit_destroy": (C.c_int, [_vp]),
     "ps_circuit_profile": (C.c_int, [_vp, C.c_int, _vp]),
     "ps_circuit_copy_records": (C.c_int, [_vp, _vp, _vp, _pu64]),
+    "ps_circuit_copy_records_async": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "ps_circuit_wait_records": (C.c_int, [_vp]),
     "ps_circuit_measure_stats": (C.c_int, [_vp, C.c_int, _vp, _vp]),
     "ps_circuit_detectors": (C.c_int, [_vp, _vp, _vp, _u64, _vp]),
     "ps_circuit_autotune": (C.c_int, [_vp, _vp, C.POINTER(C.c_double)]),

@@ -153,6 +153,17 @@ class CompiledCircuit:
         check(self._L.ps_circuit_copy_records(self._handle, _ptr(results), _ptr(determined), C.byref(words)))
         return words.value
 
+    def copy_records_async(self, results: np.ndarray, determined: np.ndarray, stream: Optional[int] = None) -> None:
+        """Enqueue the copy of the latest run's records into pinned host arrays
+        [num_measurements, words] uint64 and return at once; the arrays hold
+        them after wait_records().  The next run of this circuit waits on the
+        device for the copy; two compiled copies of one circuit, run in turn,
+        overlap one run's copy with the next run."""
+        check(self._L.ps_circuit_copy_records_async(self._handle, _ptr(results), _ptr(determined), stream))
+
+    def wait_records(self) -> None:
+        check(self._L.ps_circuit_wait_records(self._handle))
+
     def detectors(self, definitions) -> np.ndarray:
         """XOR of measurement records per detector, computed on the device:
         definitions is a list of lists of measurement indices (program

@@ -605,6 +605,8 @@ int run_job(ps_server *s, SrvJob *j) {
         ps_circuit_get_stats(c, &cs);
         j->nm = cs.num_measurements;
         j->words = (uint64_t)h->w;
+        // (filled first: with the buffers left unfilled, the copy into pages
+        // never touched before made the serving capacity fall by a third)
         j->res.assign(j->nm * j->words, 0);
         j->det.assign(j->nm * j->words, 0);
         uint64_t wds = 0;

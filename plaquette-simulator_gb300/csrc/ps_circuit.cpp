@@ -1510,6 +1510,11 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
     std::vector<int32_t> rec_of(ops.size(), -1), thr_off(ops.size(), -1);
     std::vector<uint64_t> thr;
     std::map<std::vector<uint64_t>, int32_t> thr_index;
+    // the last probabilities of each channel kind and their table: a noise
+    // model puts the same ones on every channel, so most channels are a
+    // 12- or 60-byte compare
+    float last_p[2][15];
+    int32_t last_off[2] = {-1, -1};
     uint32_t ev = 0;
     int32_t nrec = 0;
     for (size_t i = 0; i < ops.size(); ++i) {
@@ -1527,9 +1532,14 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
         if (o.code == OP_M && o.c >= 0 && !(params[o.c] >= 0.0f && params[o.c] <= 1.0f))
             return bail(fail(E_ARG, "op " + std::to_string(i) + ": bias is not a number in [0, 1]"));
         if (is_channel(o.code)) {
-            const int cnt = o.code == OP_PAULI2 ? 15 : 3;
+            const int cnt = o.code == OP_PAULI2 ? 15 : 3, kind = o.code == OP_PAULI2 ? 1 : 0;
             if (o.c < 0 || (uint64_t)o.c + cnt > nparams)
                 return bail(fail(E_ARG, "op " + std::to_string(i) + ": channel parameters out of range"));
+            if (last_off[kind] >= 0 && std::memcmp(last_p[kind], params + o.c, (size_t)cnt * sizeof(float)) == 0) {
+                thr_off[i] = last_off[kind];  // checked and tabled already
+                event_of[i] = ev++;
+                continue;
+            }
             if (check_channel_probs(params + o.c, cnt) != OK)
                 return bail(fail(E_ARG, "op " + std::to_string(i) + ": " + ps_last_error()));
             uint64_t t[16];
@@ -1543,6 +1553,8 @@ ps_status ps_circuit_compile(ps_state *h, const ps_op *ops_in, uint64_t nops, co
                 thr.insert(thr.end(), t, t + cnt + 1);
             }
             thr_off[i] = it->second;
+            std::memcpy(last_p[kind], params + o.c, (size_t)cnt * sizeof(float));
+            last_off[kind] = it->second;
         }
         if (is_meas(o.code)) rec_of[i] = nrec++;
         if (is_meas(o.code) || is_channel(o.code)) event_of[i] = ev++;

@@ -305,7 +305,8 @@ def serving_leg(args, rank, rate=None, seconds=None):
     cache0 = compile_cache_stats()
     import queue
     errors = {}
-    with Server(hbm_budget_bytes=int(args.serve_budget_gb * 1e9), max_active=16, autotune=False) as srv:
+    with Server(hbm_budget_bytes=int(args.serve_budget_gb * 1e9), max_active=16, autotune=False,
+                host_pool_bytes=8 << 30) as srv:
         # A client thread takes each job's result as it finishes and releases
         # its host records (as a caller that consumes its results would), so
         # host memory holds only the jobs in flight.

@@ -391,6 +391,9 @@ typedef struct {
     int32_t autotune;           /* tune each new job shape on its first job   */
     double hol_wait_s;          /* a queued job that waited this long stops
                                    smaller later jobs from overtaking it      */
+    uint64_t host_pool_bytes;   /* pinned host memory for finished jobs'
+                                   records (0 = 1 GiB); records that do not
+                                   fit go to pageable memory                 */
 } ps_server_options;
 
 typedef struct {

@@ -526,6 +526,8 @@ struct SrvJob {
     std::string err;
     uint64_t nm = 0, words = 0;
     std::vector<uint64_t> res, det;
+    uint64_t *pin_res = nullptr, *pin_det = nullptr;  // records in the server's pinned pool (else res / det)
+    size_t rec_words = 0;
 };
 
 }  // namespace
@@ -536,6 +538,10 @@ struct ps_server {
     int device = 0;
     ps::DevPool pool;
     void *region = nullptr;
+    // Pinned host memory for finished jobs' records: the device-to-host copy
+    // runs at DMA speed into pages that are resident already.
+    ps::DevPool hpool;
+    void *hregion = nullptr;
     std::chrono::steady_clock::time_point t0;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -605,12 +611,30 @@ int run_job(ps_server *s, SrvJob *j) {
         ps_circuit_get_stats(c, &cs);
         j->nm = cs.num_measurements;
         j->words = (uint64_t)h->w;
-        // (filled first: with the buffers left unfilled, the copy into pages
-        // never touched before made the serving capacity fall by a third)
-        j->res.assign(j->nm * j->words, 0);
-        j->det.assign(j->nm * j->words, 0);
+        j->rec_words = j->nm * j->words;
+        const size_t rb = j->rec_words * sizeof(uint64_t);
+        void *pr = nullptr, *pd = nullptr;
+        if (rb && s->hpool.cap && s->hpool.alloc(&pr, rb) && !s->hpool.alloc(&pd, rb)) {
+            s->hpool.release(pr);
+            pr = nullptr;
+        }
         uint64_t wds = 0;
-        rc = ps_circuit_copy_records(c, j->res.data(), j->det.data(), &wds);
+        if (pr) {
+            j->pin_res = static_cast<uint64_t *>(pr);
+            j->pin_det = static_cast<uint64_t *>(pd);
+            rc = ps_circuit_copy_records(c, j->pin_res, j->pin_det, &wds);
+        } else {
+            // (filled first: with the buffers left unfilled, the copy into pages
+            // never touched before made the serving capacity fall by a third)
+            j->res.assign(j->rec_words, 0);
+            j->det.assign(j->rec_words, 0);
+            rc = ps_circuit_copy_records(c, j->res.data(), j->det.data(), &wds);
+        }
+        if (rc != OK && j->pin_res) {  // a failed job keeps no records
+            s->hpool.release(j->pin_res);
+            s->hpool.release(j->pin_det);
+            j->pin_res = j->pin_det = nullptr;
+        }
     }
     if (rc == OK && j->keep) {  // park: the final tableau and event counter to host memory
         const size_t plane = (size_t)h->W * (size_t)h->n * (size_t)h->w, rw = (size_t)h->W * (size_t)h->w;
@@ -721,6 +745,15 @@ ps_status ps_server_create(const ps_server_options *opts, ps_server **out) {
         return fail(E_NOMEM, std::string("cannot reserve the HBM budget: ") + cudaGetErrorString(e));
     }
     s->pool.reset(s->region, opts->hbm_budget_bytes);
+    {  // the pinned record pool (without it, records go to pageable memory)
+        const size_t hb = opts->host_pool_bytes ? (size_t)opts->host_pool_bytes : (size_t)1 << 30;
+        if (cudaMallocHost(&s->hregion, hb) == cudaSuccess) {
+            s->hpool.reset(s->hregion, hb);
+        } else {
+            cudaGetLastError();
+            s->hregion = nullptr;
+        }
+    }
     s->t0 = std::chrono::steady_clock::now();
     for (int i = 0; i < s->opts.max_active; ++i) s->workers.emplace_back(worker_main, s);
     *out = s;
@@ -814,8 +847,9 @@ ps_status ps_server_copy_records(ps_server *s, uint64_t job_id, uint64_t *result
     SrvJob *j = it->second.get();
     if (!j->done) return fail(E_STATE, "job not finished");
     if (j->status != OK) return fail(j->status, "job failed: " + j->err);
-    if (results) std::memcpy(results, j->res.data(), j->res.size() * sizeof(uint64_t));
-    if (determined) std::memcpy(determined, j->det.data(), j->det.size() * sizeof(uint64_t));
+    const uint64_t *rs = j->pin_res ? j->pin_res : j->res.data(), *ds = j->pin_res ? j->pin_det : j->det.data();
+    if (results && j->rec_words) std::memcpy(results, rs, j->rec_words * sizeof(uint64_t));
+    if (determined && j->rec_words) std::memcpy(determined, ds, j->rec_words * sizeof(uint64_t));
     return OK;
 }
 
@@ -844,6 +878,10 @@ ps_status ps_server_release(ps_server *s, uint64_t job_id) {
     auto it = s->jobs.find(job_id);
     if (it == s->jobs.end()) return fail(E_RANGE, "unknown job id");
     if (!it->second->done) return fail(E_STATE, "job not finished");
+    if (it->second->pin_res) {
+        s->hpool.release(it->second->pin_res);
+        s->hpool.release(it->second->pin_det);
+    }
     s->jobs.erase(it);
     return OK;
 }
@@ -936,6 +974,7 @@ ps_status ps_server_destroy(ps_server *s) {
     for (auto &t : s->workers) t.join();
     s->cv_done.notify_all();
     cudaFree(s->region);
+    if (s->hregion) cudaFreeHost(s->hregion);
     delete s;
     return OK;
 }

@@ -146,7 +146,7 @@ class Batch:
 # ----------------------------------------------------------------- server
 class ServerOptions(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active", C.c_int32), ("autotune", C.c_int32),
-                ("hol_wait_s", C.c_double)]
+                ("hol_wait_s", C.c_double), ("host_pool_bytes", C.c_uint64)]
 
 
 class JobResult(C.Structure):
@@ -173,11 +173,11 @@ class JobPark(C.Structure):
 
 class Server:
     def __init__(self, hbm_budget_bytes: int, max_active: int = 16, autotune: bool = False,
-                 hol_wait_s: float = 1.0):
+                 hol_wait_s: float = 1.0, host_pool_bytes: int = 0):
         self._L = _lib.load()
         h = C.c_void_p()
         check(self._L.ps_server_create(C.byref(ServerOptions(hbm_budget_bytes, max_active, int(autotune),
-                                                             hol_wait_s)), C.byref(h)))
+                                                             hol_wait_s, host_pool_bytes)), C.byref(h)))
         self._h = h
         self._jobs = {}
 

@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving leg: arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="serving leg: HBM admission budget")
     ap.add_argument("--serve-drain-s", type=float, default=180.0, help="serving leg: longest wait for the backlog")
-    ap.add_argument("--capacity-rate", type=float, default=2000.0,
+    ap.add_argument("--capacity-rate", type=float, default=4000.0,
                     help="capacity leg: arrivals per second (the same job mix, well above the serving rate)")
     ap.add_argument("--capacity-seconds", type=float, default=10.0,
                     help="capacity leg: seconds of arrivals (0 = skip)")

@@ -63,6 +63,31 @@ CHECK = textwrap.dedent("""
 """)
 
 
+def test_reference_shaped_package_imports_the_bindings(tmp_path):
+    """Without a GPU: with a reference-shaped ``plaquette_simulator`` first on
+    the path, its CliffordState is the bindings' class, and the bindings
+    never bound the name ``plaquette_simulator`` to this repository's package."""
+    import build as psbuild
+    psbuild.build()
+    pkg = tmp_path / "plaquette_simulator"
+    pkg.mkdir()
+    (pkg / "__init__.py").write_text(REF_SHAPED_INIT)
+    (pkg / "simulator.py").write_text(REF_SHAPED_SIMULATOR)
+    code = textwrap.dedent(f"""
+        import sys
+        import plaquette_simulator as ps
+        import plaquette_simulator_bindings as b
+        assert ps.__file__.startswith({str(tmp_path)!r}), ps.__file__
+        assert ps.CliffordState is b.CliffordState
+        assert sys.modules["plaquette_simulator"] is ps
+        print("OK")
+    """)
+    env = dict(os.environ, PYTHONPATH=os.pathsep.join([str(tmp_path), PYDIR]))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=120,
+                         cwd=str(tmp_path))
+    assert out.returncode == 0 and "OK" in out.stdout, out.stdout + out.stderr
+
+
 @pytest.mark.gpu
 def test_reference_shaped_package_runs_on_the_bindings(gpu_lib, tmp_path):
     pkg = tmp_path / "plaquette_simulator"
